@@ -1,0 +1,304 @@
+"""hbi_gb300 -- GB300 (sm_103a) implementation of HBI's per-step hot path.
+
+Host-side mirror of the HACApK entry points the HBI driver calls
+(HACApK_init / _generate / _construct_LH / _gen_lattice_vector /
+_adot_lattice_hyp, and the derivs/rkck/rkqs loop of main_LH.f90), bound to
+the C ABI in include/hbi_gpu.h through ctypes.  The library is built in-tree
+by hbi_gb300/_build.py; importing this module on a machine without it, or
+calling a compute entry point without a GPU, raises HBIError -- there is no
+CPU fallback.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libhbigpu.so")
+
+HBI_2DVS, HBI_3DPH, HBI_3DNR, HBI_3DNT = 1, 2, 3, 4
+STORE_F64, STORE_F32, STORE_BF16 = 0, 1, 2
+STORE_NAMES = {"f64": STORE_F64, "f32": STORE_F32, "bf16": STORE_BF16}
+HBI_ERR_CONVERGE = -5
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_i64p = C.POINTER(C.c_int64)
+
+# exported symbols of include/hbi_gpu.h (checked by the CPU test suite)
+EXPORTS = [
+    "hbi_last_error", "hbi_version", "hbi_init", "hbi_param_set", "hbi_param_get", "hbi_finalize",
+    "hbi_generate", "hbi_free_leafmtxp", "hbi_construct_lh", "hbi_free_lh", "hbi_gen_lattice_vector",
+    "hbi_adot_lattice_hyp", "hbi_adot_lattice_hyp_dev", "hbi_entry_ij", "hbi_get_lod", "hbi_leaf_count",
+    "hbi_get_leaves", "hbi_get_body", "hbi_lh_info", "hbi_rk_create", "hbi_rk_free", "hbi_rk_set_state",
+    "hbi_rk_get_state", "hbi_derivs", "hbi_rkck", "hbi_rkqs", "hbi_rk_launches_per_attempt",
+    "hbi_cluster_structure",
+]
+
+
+class HBIError(RuntimeError):
+    pass
+
+
+class Bemv(C.Structure):
+    """hbi_bemv == st_HACApK_calc_entry (m_HACApK_calc_entry_ij.f90:7-19)."""
+    _fields_ = ([("problem", C.c_int), ("nd", C.c_int), ("v", C.c_char), ("md", C.c_char)]
+                + [(f, _dp) for f in ("xcol", "ycol", "zcol", "xel", "xer", "ang", "angd", "dsl", "dsd", "rake")]
+                + [("w", C.c_double)]
+                + [(f, _dp) for f in ("xs1", "xs2", "xs3", "ys1", "ys2", "ys3", "zs1", "zs2", "zs3", "ev11",
+                                      "ev12", "ev13", "ev21", "ev22", "ev23", "ev31", "ev32", "ev33")])
+
+
+class RsfParams(C.Structure):
+    _fields_ = ([("ncell", C.c_int), ("evlaw", C.c_int), ("backslip", C.c_int), ("limitsigma", C.c_int),
+                 ("vref", C.c_double), ("minsig", C.c_double), ("maxsig", C.c_double),
+                 ("scale_s", C.c_double), ("scale_n", C.c_double)]
+                + [(f, _dp) for f in ("a", "b", "dc", "f0", "taudot", "sigdot", "vpl")])
+
+
+_lib = None
+
+
+def lib():
+    """Load libhbigpu.so (built by hbi_gb300._build.build())."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise HBIError(f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+        L = C.CDLL(LIB_PATH)
+        L.hbi_last_error.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+def _check(rc, what):
+    if rc != 0:
+        msg = lib().hbi_last_error().decode(errors="replace")
+        err = HBIError(f"{what} failed ({rc}): {msg}")
+        err.code = rc
+        raise err
+
+
+def _p(a):
+    return a.ctypes.data_as(_dp)
+
+
+class Geometry:
+    """Keeps numpy arrays alive behind an hbi_bemv (global element order)."""
+
+    def __init__(self, problem, nd, v="s", w=0.0, **arrays):
+        self.problem, self.nd, self.w = problem, nd, float(w)
+        self.arrays = {k: np.ascontiguousarray(a, dtype=np.float64) for k, a in arrays.items()}
+        for k, a in self.arrays.items():
+            if a.shape != (nd,):
+                raise ValueError(f"geometry array {k} has shape {a.shape}, expected ({nd},)")
+        self.set_v(v)
+
+    def set_v(self, v):
+        b = Bemv()
+        b.problem, b.nd, b.v, b.md, b.w = self.problem, self.nd, v.encode(), b"s", self.w
+        for k, a in self.arrays.items():
+            setattr(b, k, _p(a))
+        self.bemv, self.v = b, v
+        return self
+
+    def coord(self):
+        z = np.zeros(self.nd)
+        x = self.arrays.get("xcol", z)
+        y = self.arrays.get("ycol", z)
+        zz = self.arrays.get("zcol", z)
+        return np.asfortranarray(np.stack([x, y, zz], 1))
+
+
+class Ctl:
+    """st_HACApK_lcontrol: HACApK_init (m_HACApK_base.f90:246-345)."""
+
+    def __init__(self, nd):
+        self.h = C.c_void_p()
+        _check(lib().hbi_init(int(nd), C.byref(self.h)), "hbi_init")
+        self.nd = nd
+
+    @property
+    def param(self):
+        p = np.zeros(100)
+        _check(lib().hbi_param_get(self.h, _p(p)), "hbi_param_get")
+        return p
+
+    @param.setter
+    def param(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        _check(lib().hbi_param_set(self.h, _p(p)), "hbi_param_set")
+
+    def lod(self):
+        a = np.zeros(self.nd, dtype=np.int32)
+        _check(lib().hbi_get_lod(self.h, a.ctypes.data_as(_ip)), "hbi_get_lod")
+        return a
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.hbi_finalize(self.h)
+            self.h = None
+
+
+class LeafMtxp:
+    """st_HACApK_leafmtxp: result of HACApK_generate."""
+
+    def __init__(self, ctl, geom, ztol):
+        self.ctl, self.h = ctl, C.c_void_p()
+        coord = geom.coord().ravel(order="F")
+        _check(lib().hbi_generate(C.byref(self.h), C.byref(geom.bemv), ctl.h, _p(coord), C.c_double(ztol)),
+               "hbi_generate")
+
+    def leaves(self):
+        n, km = C.c_int(), C.c_int()
+        _check(lib().hbi_leaf_count(self.h, C.byref(n), C.byref(km)), "hbi_leaf_count")
+        a = np.zeros((n.value, 6), dtype=np.int32)
+        _check(lib().hbi_get_leaves(self.h, a.ctypes.data_as(_ip)), "hbi_get_leaves")
+        return a
+
+    def body(self):
+        nl = len(self.leaves())
+        off = np.zeros(nl + 1, dtype=np.int64)
+        _check(lib().hbi_get_body(self.h, off.ctypes.data_as(_i64p), None), "hbi_get_body")
+        body = np.zeros(max(int(off[-1]), 1))
+        _check(lib().hbi_get_body(self.h, off.ctypes.data_as(_i64p), _p(body)), "hbi_get_body")
+        return off, body[:int(off[-1])]
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.hbi_free_leafmtxp(self.h)
+            self.h = None
+
+
+class LHp:
+    """st_HACApK_LHp: the lattice matvec operator (HACApK_construct_LH)."""
+
+    def __init__(self, lf, ctl, storage=STORE_F64):
+        if isinstance(storage, str):
+            storage = STORE_NAMES[storage]
+        self.ctl, self.h, self.storage = ctl, C.c_void_p(), storage
+        _check(lib().hbi_construct_lh(C.byref(self.h), lf.h, ctl.h, int(storage)), "hbi_construct_lh")
+        self.n = ctl.nd
+
+    def matvec(self, u):
+        """HACApK_adot_lattice_hyp: au = H u (cluster order, host arrays)."""
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        au = np.zeros(self.n)
+        _check(lib().hbi_adot_lattice_hyp(_p(au), self.h, self.ctl.h, None, _p(u)), "hbi_adot_lattice_hyp")
+        return au
+
+    def info(self):
+        fe, sb, ab = C.c_int64(), C.c_int64(), C.c_double()
+        _check(lib().hbi_lh_info(self.h, C.byref(fe), C.byref(sb), C.byref(ab)), "hbi_lh_info")
+        return {"factor_elems": fe.value, "store_bytes": sb.value, "alg_bytes": ab.value}
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.hbi_free_lh(self.h)
+            self.h = None
+
+
+# ---- HACApK-named functions (the drop-in surface) -----------------------
+def HACApK_init(nd):
+    return Ctl(nd)
+
+
+def HACApK_generate(ctl, geom, ztol):
+    return LeafMtxp(ctl, geom, ztol)
+
+
+def HACApK_construct_LH(lf, ctl, storage=STORE_F64):
+    return LHp(lf, ctl, storage)
+
+
+def HACApK_gen_lattice_vector(ctl):
+    ndc = C.c_int()
+    lodc = np.zeros(ctl.nd, dtype=np.int32)
+    _check(lib().hbi_gen_lattice_vector(ctl.h, C.byref(ndc), lodc.ctypes.data_as(_ip)), "hbi_gen_lattice_vector")
+    return ndc.value, lodc
+
+
+def HACApK_adot_lattice_hyp(lh, u):
+    return lh.matvec(u)
+
+
+def cluster_structure(coord, param=None):
+    """Host-only tree + admissibility + leaf order (no GPU).  coord (nd,3)."""
+    coord = np.asarray(coord, dtype=np.float64)
+    nd = coord.shape[0]
+    cf = np.asfortranarray(coord).ravel(order="F")
+    lod = np.zeros(nd, dtype=np.int32)
+    nl = C.c_int(0)
+    pp = _p(np.ascontiguousarray(param, dtype=np.float64)) if param is not None else None
+    _check(lib().hbi_cluster_structure(nd, _p(cf), pp, lod.ctypes.data_as(_ip), C.byref(nl), None),
+           "hbi_cluster_structure")
+    leaves = np.zeros((nl.value, 6), dtype=np.int32)
+    _check(lib().hbi_cluster_structure(nd, _p(cf), pp, lod.ctypes.data_as(_ip), C.byref(nl),
+                                       leaves.ctypes.data_as(_ip)), "hbi_cluster_structure")
+    return lod, leaves
+
+
+def entry_ij(geom, i, j):
+    """HACApK_entry_ij on the GPU for arrays of 1-based (i, j)."""
+    i = np.ascontiguousarray(i, dtype=np.int32)
+    j = np.ascontiguousarray(j, dtype=np.int32)
+    out = np.zeros(len(i))
+    _check(lib().hbi_entry_ij(C.byref(geom.bemv), len(i), i.ctypes.data_as(_ip), j.ctypes.data_as(_ip), _p(out)),
+           "hbi_entry_ij")
+    return out
+
+
+class RK:
+    """derivs / rkck / rkqs of main_LH.f90 on the device (state in cluster order)."""
+
+    def __init__(self, lh_s, lh_n=None, evlaw=0, backslip=1, limitsigma=1, vref=float(np.float32(1e-6)),
+                 minsig=1.0, maxsig=300.0, scale=1.0, **params):
+        n = lh_s.n
+        self.keep = {}
+        p = RsfParams()
+        p.ncell, p.evlaw, p.backslip, p.limitsigma = n, evlaw, backslip, limitsigma
+        p.vref, p.minsig, p.maxsig, p.scale_s, p.scale_n = vref, minsig, maxsig, scale, scale
+        for k in ("a", "b", "dc", "f0", "taudot", "sigdot", "vpl"):
+            a = np.ascontiguousarray(np.broadcast_to(params.get(k, 0.0), (n,)), dtype=np.float64)
+            self.keep[k] = a
+            setattr(p, k, _p(a))
+        self.h = C.c_void_p()
+        _check(lib().hbi_rk_create(C.byref(self.h), C.byref(p), lh_s.h, lh_n.h if lh_n is not None else None),
+               "hbi_rk_create")
+        self.n, self.lh = n, (lh_s, lh_n)
+
+    def set_state(self, y):
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        _check(lib().hbi_rk_set_state(self.h, _p(y)), "hbi_rk_set_state")
+
+    def get_state(self):
+        y = np.zeros(3 * self.n)
+        _check(lib().hbi_rk_get_state(self.h, _p(y)), "hbi_rk_get_state")
+        return y
+
+    def derivs(self, y):
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        d = np.zeros(3 * self.n)
+        _check(lib().hbi_derivs(self.h, _p(y), _p(d)), "hbi_derivs")
+        return d
+
+    def rkck(self, h, eps=1.0):
+        yo, ye = np.zeros(3 * self.n), np.zeros(3 * self.n)
+        em = C.c_double()
+        _check(lib().hbi_rkck(self.h, C.c_double(h), C.c_double(eps), _p(yo), _p(ye), C.byref(em)), "hbi_rkck")
+        return yo, ye, em.value
+
+    def rkqs(self, x, htry, eps, dtmax=1e10):
+        xx, hd, hn, em, nr = C.c_double(x), C.c_double(), C.c_double(), C.c_double(), C.c_int()
+        _check(lib().hbi_rkqs(self.h, C.byref(xx), C.c_double(htry), C.c_double(eps), C.c_double(dtmax),
+                              C.byref(hd), C.byref(hn), C.byref(em), C.byref(nr)), "hbi_rkqs")
+        return xx.value, hd.value, hn.value, em.value, nr.value
+
+    @property
+    def launches_per_attempt(self):
+        return lib().hbi_rk_launches_per_attempt(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.hbi_rk_free(self.h)
+            self.h = None

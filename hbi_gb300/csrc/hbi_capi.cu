@@ -1,0 +1,883 @@
+// hbi_capi.cu -- the extern "C" boundary (include/hbi_gpu.h): HACApK-shaped
+// entry points over the GB300 kernels, plus the RK45 driver of the
+// rate-and-state system.  Host orchestration only; every product runs in the
+// kernels of hbi_aca.cu / hbi_matvec.cu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/hbi_gpu.h"
+#include "hbi_kernels.cuh"
+#include "hbi_structure.hpp"
+
+using namespace hbi;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CK(x)                                                                                         \
+  do {                                                                                                \
+    cudaError_t e_ = (x);                                                                             \
+    if (e_ != cudaSuccess) return fail(HBI_ERR_CUDA, "%s: %s (%s:%d)", #x, cudaGetErrorString(e_), __FILE__, __LINE__); \
+  } while (0)
+
+template <class T>
+cudaError_t dalloc(T** p, size_t n) {
+  return cudaMalloc((void**)p, std::max<size_t>(n, 1) * sizeof(T));
+}
+template <class T>
+void dfree(T*& p) {
+  if (p) cudaFree((void*)p);
+  p = nullptr;
+}
+template <class T>
+cudaError_t upload(T** p, const std::vector<T>& v, cudaStream_t st) {
+  cudaError_t e = dalloc(p, v.size());
+  if (e != cudaSuccess) return e;
+  if (v.empty()) return cudaSuccess;
+  e = cudaMemcpyAsync(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  return cudaStreamSynchronize(st);
+}
+
+// geometry of one st_bemv on the device, with per-element trig tables
+struct DevGeom {
+  DevBemv b{};
+  std::vector<void*> allocs;
+  ~DevGeom() {
+    for (void* p : allocs) cudaFree(p);
+  }
+  int put(const double** dst, const double* src, int n, cudaStream_t st) {
+    *dst = nullptr;
+    if (!src) return 0;
+    double* d = nullptr;
+    CK(dalloc(&d, n));
+    allocs.push_back(d);
+    CK(cudaMemcpyAsync(d, src, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    *dst = d;
+    return 0;
+  }
+  int put_vec(const double** dst, const std::vector<double>& v, cudaStream_t st) {
+    return put(dst, v.data(), (int)v.size(), st);
+  }
+  int upload(const hbi_bemv* h, cudaStream_t st) {
+    const int n = h->nd;
+    b.problem = h->problem;
+    b.n = n;
+    b.normal = (h->v == 'n');
+    b.w = h->w;
+    int rc = 0;
+    rc |= put(&b.xcol, h->xcol, n, st); rc |= put(&b.ycol, h->ycol, n, st); rc |= put(&b.zcol, h->zcol, n, st);
+    rc |= put(&b.xel, h->xel, n, st); rc |= put(&b.xer, h->xer, n, st);
+    rc |= put(&b.ang, h->ang, n, st); rc |= put(&b.angd, h->angd, n, st);
+    rc |= put(&b.dsl, h->dsl, n, st); rc |= put(&b.dsd, h->dsd, n, st); rc |= put(&b.rake, h->rake, n, st);
+    rc |= put(&b.xs1, h->xs1, n, st); rc |= put(&b.xs2, h->xs2, n, st); rc |= put(&b.xs3, h->xs3, n, st);
+    rc |= put(&b.ys1, h->ys1, n, st); rc |= put(&b.ys2, h->ys2, n, st); rc |= put(&b.ys3, h->ys3, n, st);
+    rc |= put(&b.zs1, h->zs1, n, st); rc |= put(&b.zs2, h->zs2, n, st); rc |= put(&b.zs3, h->zs3, n, st);
+    rc |= put(&b.ev11, h->ev11, n, st); rc |= put(&b.ev12, h->ev12, n, st); rc |= put(&b.ev13, h->ev13, n, st);
+    rc |= put(&b.ev21, h->ev21, n, st); rc |= put(&b.ev22, h->ev22, n, st); rc |= put(&b.ev23, h->ev23, n, st);
+    rc |= put(&b.ev31, h->ev31, n, st); rc |= put(&b.ev32, h->ev32, n, st); rc |= put(&b.ev33, h->ev33, n, st);
+    // host-evaluated trig of the per-source angles, as okada_ij / okada form them
+    if (h->ang) {
+      std::vector<double> c(n), s(n);
+      for (int i = 0; i < n; i++) { c[i] = std::cos(h->ang[i]); s[i] = std::sin(h->ang[i]); }
+      rc |= put_vec(&b.cang, c, st); rc |= put_vec(&b.sang, s, st);
+    }
+    if (h->rake) {
+      std::vector<double> c(n), s(n);
+      for (int i = 0; i < n; i++) { c[i] = std::cos(h->rake[i]); s[i] = std::sin(h->rake[i]); }
+      rc |= put_vec(&b.crake, c, st); rc |= put_vec(&b.srake, s, st);
+    }
+    if (h->angd) {
+      const double pi = 4 * std::atan(1.0), pi2 = 8.0 * std::atan(1.0);
+      std::vector<double> cd(n), sd(n), dd(n);
+      for (int i = 0; i < n; i++) {
+        double dip = h->angd[i] * 180 / pi;
+        double p18 = pi2 / 360.0;
+        double s_ = std::sin(dip * p18), c_ = std::cos(dip * p18);
+        if (std::fabs(c_) < 1e-6) {
+          c_ = 0.0;
+          if (s_ > 0.0) s_ = 1.0;
+          if (s_ < 0.0) s_ = -1.0;
+        }
+        cd[i] = c_; sd[i] = s_; dd[i] = dip;
+      }
+      rc |= put_vec(&b.cangd, cd, st); rc |= put_vec(&b.sangd, sd, st); rc |= put_vec(&b.dipdeg, dd, st);
+    }
+    if (rc) return HBI_ERR_CUDA;
+    CK(cudaStreamSynchronize(st));
+    return 0;
+  }
+};
+
+int check_bemv(const hbi_bemv* b) {
+  if (!b || b->nd < 1) return fail(HBI_ERR_ARG, "st_bemv: null or nd<1");
+  if (b->md != 's' && b->md != 0) return fail(HBI_ERR_ARG, "st_bemv%%md='%c' is not on the hot path (only 's')", b->md);
+  if (b->v != 's' && b->v != 'n') return fail(HBI_ERR_ARG, "st_bemv%%v must be 's' or 'n'");
+  switch (b->problem) {
+    case HBI_2DVS:
+      if (!b->xcol || !b->xel || !b->xer) return fail(HBI_ERR_ARG, "2dvs needs xcol, xel, xer");
+      break;
+    case HBI_3DPH:
+    case HBI_3DNR:
+      if (!b->xcol || !b->ycol || !b->zcol || !b->ang || !b->angd || !b->dsl || !b->dsd || !b->rake || !(b->w > 0))
+        return fail(HBI_ERR_ARG, "okada problems need xcol,ycol,zcol,ang,angd,dsl,dsd,rake and w>0");
+      break;
+    case HBI_3DNT:
+      if (!b->xcol || !b->ycol || !b->zcol || !b->xs1 || !b->xs2 || !b->xs3 || !b->ys1 || !b->ys2 || !b->ys3 ||
+          !b->zs1 || !b->zs2 || !b->zs3 || !b->ev11 || !b->ev12 || !b->ev13 || !b->ev21 || !b->ev22 || !b->ev23 ||
+          !b->ev31 || !b->ev32 || !b->ev33 || !b->rake)
+        return fail(HBI_ERR_ARG, "3dnt needs collocation points, vertices, ev frames and rake");
+      break;
+    default:
+      return fail(HBI_ERR_ARG, "problem %d is not on the hot path", b->problem);
+  }
+  return 0;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- handles
+struct hbi_ctl_s {
+  int nd = 0;
+  double param[100];
+  int device = 0, sm_count = 152;
+  cudaStream_t stream = nullptr;
+  bool have_tree = false;
+  Structure S;
+  int* d_lod = nullptr;
+  bool have_chains = false;
+  ChainPlan chains;
+  int32_t *d_row_fc = nullptr, *d_chain_ptr = nullptr, *d_chain_leaf = nullptr;
+};
+
+struct hbi_leafmtxp_s {
+  hbi_ctl* ctl = nullptr;
+  std::vector<Leaf> leaves;     // with kt
+  std::vector<int64_t> off;     // reference body offsets (nleaf+1)
+  double* d_body = nullptr;     // FP64 body in HACApK's contiguous packing
+  int ktmax = 0;
+  double t_aca = 0, t_dense = 0;
+};
+
+struct hbi_lhp_s {
+  hbi_ctl* ctl = nullptr;
+  int n = 0, storage = 0;
+  MatPlan plan;
+  void* d_store = nullptr;
+  P1ItemDev* d_p1 = nullptr;
+  LrInfo* d_lr = nullptr;
+  int* d_cnt = nullptr;
+  void* d_part = nullptr;
+  void* d_z = nullptr;
+  LeafDescDev* d_desc = nullptr;
+  double *d_x = nullptr, *d_y = nullptr;
+  MatDev md{};
+  ChainDev cd{};
+  std::vector<Leaf> leaves;
+  size_t store_bytes = 0;
+  double alg_bytes = 0;
+};
+
+extern "C" const char* hbi_last_error(void) { return g_err.c_str(); }
+extern "C" int hbi_version(void) { return 10000; }
+
+extern "C" int hbi_init(int nd, hbi_ctl** out) {
+  if (!out || nd < 1) return fail(HBI_ERR_ARG, "hbi_init: nd<1 or null handle");
+  hbi_ctl* c = new hbi_ctl_s();
+  c->nd = nd;
+  default_params(c->param);
+  cudaError_t e = cudaGetDevice(&c->device);
+  if (e != cudaSuccess) { delete c; return fail(HBI_ERR_CUDA, "no CUDA device: %s", cudaGetErrorString(e)); }
+  cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { delete c; return fail(HBI_ERR_CUDA, "stream: %s", cudaGetErrorString(e)); }
+  *out = c;
+  return HBI_OK;
+}
+
+extern "C" int hbi_param_set(hbi_ctl* c, const double* p) {
+  if (!c || !p) return fail(HBI_ERR_ARG, "hbi_param_set: null");
+  memcpy(c->param, p, sizeof(c->param));
+  return HBI_OK;
+}
+extern "C" int hbi_param_get(const hbi_ctl* c, double* p) {
+  if (!c || !p) return fail(HBI_ERR_ARG, "hbi_param_get: null");
+  memcpy(p, c->param, sizeof(c->param));
+  return HBI_OK;
+}
+
+extern "C" int hbi_finalize(hbi_ctl* c) {
+  if (!c) return HBI_OK;
+  dfree(c->d_lod);
+  dfree(c->d_row_fc); dfree(c->d_chain_ptr); dfree(c->d_chain_leaf);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return HBI_OK;
+}
+
+extern "C" int hbi_get_lod(const hbi_ctl* c, int* lod) {
+  if (!c || !lod) return fail(HBI_ERR_ARG, "hbi_get_lod: null");
+  if (!c->have_tree) return fail(HBI_ERR_STATE, "hbi_get_lod before hbi_generate");
+  memcpy(lod, c->S.lod.data(), sizeof(int) * c->nd);
+  return HBI_OK;
+}
+
+extern "C" int hbi_cluster_structure(int nd, const double* coord, const double* param, int* lod, int* nleaf,
+                                     int* leaves6) {
+  if (nd < 1 || !coord || !nleaf) return fail(HBI_ERR_ARG, "hbi_cluster_structure: bad arguments");
+  Structure S;
+  if (build_structure(nd, coord, param, S) != 0) return fail(HBI_ERR_ARG, "structure");
+  if (lod) memcpy(lod, S.lod.data(), sizeof(int) * nd);
+  if (leaves6) {
+    if (*nleaf < (int)S.leaves.size()) return fail(HBI_ERR_ARG, "leaves6 too small (%d < %d)", *nleaf, (int)S.leaves.size());
+    for (size_t i = 0; i < S.leaves.size(); i++) {
+      const Leaf& L = S.leaves[i];
+      int* o = leaves6 + 6 * i;
+      o[0] = L.ltmtx; o[1] = 0; o[2] = L.nstrtl; o[3] = L.ndl; o[4] = L.nstrtt; o[5] = L.ndt;
+    }
+  }
+  *nleaf = (int)S.leaves.size();
+  return HBI_OK;
+}
+
+extern "C" int hbi_gen_lattice_vector(const hbi_ctl* c, int* ndc, int* lodc) {
+  if (!c || !ndc) return fail(HBI_ERR_ARG, "hbi_gen_lattice_vector: null");
+  if (!c->have_tree) return fail(HBI_ERR_STATE, "hbi_gen_lattice_vector before hbi_generate");
+  // one lattice block: ndc = nd and lodc = lod (m_HACApK_base.f90:3481-3488)
+  *ndc = c->nd;
+  if (lodc) memcpy(lodc, c->S.lod.data(), sizeof(int) * c->nd);
+  return HBI_OK;
+}
+
+// ------------------------------------------------------------ generate
+static int run_aca(hbi_ctl* c, const DevGeom& G, std::vector<Leaf>& leaves, std::vector<double*>& chunk_of,
+                   std::vector<int64_t>& choff, std::vector<double*>& chunks) {
+  cudaStream_t st = c->stream;
+  const int kmax = (int)c->param[62];
+  AcaParams P;
+  P.eps = c->param[70];
+  P.pACA_EPS = c->param[71] * P.eps;
+  P.znrmmat = (double)(1.0f / (float)c->nd);  // znrm=1.0/nd in default real (m_HACApK_use.f90:200)
+  P.kmin = c->param[63];
+  P.kmax = kmax;
+  struct Pend { int leaf, kcap; };
+  std::vector<Pend> todo;
+  for (int i = 0; i < (int)leaves.size(); i++)
+    if (leaves[i].ltmtx == 1) {
+      int kc = std::min(leaves[i].ndl, leaves[i].ndt) + 2;
+      kc = std::min(kc, std::min(kmax, 48));
+      todo.push_back({i, std::max(kc, 2)});
+    }
+  const char* env = getenv("HBI_ACA_ARENA_MB");
+  int64_t arena_elems = (int64_t)(env ? atoll(env) : 2048) * 1024 * 1024 / 8;
+  double* arena = nullptr;
+  int64_t arena_cap = 0;
+  AcaTask* d_tasks = nullptr;
+  int* d_res = nullptr;
+  int64_t* d_off = nullptr;
+  int rc = HBI_OK;
+  while (!todo.empty() && rc == HBI_OK) {
+    std::sort(todo.begin(), todo.end(), [&](const Pend& a, const Pend& b) {
+      int64_t sa = aca_scratch_elems(leaves[a.leaf].ndl, leaves[a.leaf].ndt, a.kcap);
+      int64_t sb = aca_scratch_elems(leaves[b.leaf].ndl, leaves[b.leaf].ndt, b.kcap);
+      return sa != sb ? sa > sb : a.leaf < b.leaf;
+    });
+    std::vector<Pend> retry;
+    size_t pos = 0;
+    while (pos < todo.size()) {
+      std::vector<AcaTask> tasks;
+      int64_t used = 0;
+      while (pos < todo.size()) {
+        const Leaf& L = leaves[todo[pos].leaf];
+        int64_t need = aca_scratch_elems(L.ndl, L.ndt, todo[pos].kcap);
+        need = (need + 31) / 32 * 32;
+        if (!tasks.empty() && used + need > arena_elems) break;
+        AcaTask t{L.ndl, L.ndt, L.nstrtl, L.nstrtt, todo[pos].kcap, todo[pos].leaf, used};
+        tasks.push_back(t);
+        used += need;
+        pos++;
+        if (tasks.size() >= 65535) break;
+      }
+      if (used > arena_cap) {
+        dfree(arena);
+        if (dalloc(&arena, used) != cudaSuccess) { rc = fail(HBI_ERR_NOMEM, "ACA arena of %lld doubles", (long long)used); break; }
+        arena_cap = used;
+      }
+      const int nt = (int)tasks.size();
+      dfree(d_tasks); dfree(d_res); dfree(d_off);
+      if (upload(&d_tasks, tasks, st) != cudaSuccess || dalloc(&d_res, nt) != cudaSuccess ||
+          dalloc(&d_off, nt) != cudaSuccess) { rc = fail(HBI_ERR_CUDA, "ACA task upload"); break; }
+      if (cudaMemsetAsync(arena, 0, sizeof(double) * used, st) != cudaSuccess) { rc = fail(HBI_ERR_CUDA, "memset"); break; }
+      launch_aca(G.b, c->d_lod, d_tasks, nt, arena, d_res, P, st);
+      std::vector<int> res(nt);
+      cudaError_t e = cudaMemcpyAsync(res.data(), d_res, sizeof(int) * nt, cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) { rc = fail(HBI_ERR_CUDA, "ACA kernel: %s", cudaGetErrorString(e)); break; }
+      std::vector<int64_t> off(nt, 0);
+      int64_t tot = 0;
+      for (int t = 0; t < nt; t++) {
+        const AcaTask& T = tasks[t];
+        if (res[t] == -2) {
+          int kc = std::min(std::min(T.ndl, T.ndt) + 2, std::min(kmax, T.kcap * 4));
+          if (kc <= T.kcap) { rc = fail(HBI_ERR_LIMIT, "ACA rank cap reached for leaf %d", T.leaf); break; }
+          retry.push_back({T.leaf, kc});
+          continue;
+        }
+        leaves[T.leaf].kt = res[t];
+        off[t] = tot;
+        tot += (int64_t)res[t] * (T.ndl + T.ndt);
+      }
+      if (rc != HBI_OK) break;
+      double* chunk = nullptr;
+      if (dalloc(&chunk, tot) != cudaSuccess) { rc = fail(HBI_ERR_NOMEM, "ACA chunk"); break; }
+      chunks.push_back(chunk);
+      if (cudaMemcpyAsync(d_off, off.data(), sizeof(int64_t) * nt, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+        rc = fail(HBI_ERR_CUDA, "offsets"); break;
+      }
+      launch_aca_compact(d_tasks, nt, d_res, d_off, arena, chunk, st);
+      e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) { rc = fail(HBI_ERR_CUDA, "ACA compact: %s", cudaGetErrorString(e)); break; }
+      for (int t = 0; t < nt; t++)
+        if (res[t] >= 0) { chunk_of[tasks[t].leaf] = chunk; choff[tasks[t].leaf] = off[t]; }
+    }
+    todo.swap(retry);
+  }
+  dfree(arena); dfree(d_tasks); dfree(d_res); dfree(d_off);
+  return rc;
+}
+
+extern "C" int hbi_generate(hbi_leafmtxp** out, const hbi_bemv* bv, hbi_ctl* c, const double* coord, double ztol) {
+  if (!out || !c || !coord) return fail(HBI_ERR_ARG, "hbi_generate: null argument");
+  int rc = check_bemv(bv);
+  if (rc) return rc;
+  if (bv->nd != c->nd) return fail(HBI_ERR_ARG, "st_bemv%%nd=%d differs from hbi_init nd=%d", bv->nd, c->nd);
+  c->param[70] = ztol;
+  if (c->param[20] < 2) c->param[20] = 3;  // HACApK_chk_st_ctl
+  if (build_structure(c->nd, coord, c->param, c->S) != 0) return fail(HBI_ERR_ARG, "structure");
+  c->have_tree = true;
+  c->have_chains = false;
+  dfree(c->d_lod);
+  CK(upload(&c->d_lod, c->S.lod, c->stream));
+  DevGeom G;
+  rc = G.upload(bv, c->stream);
+  if (rc) return rc;
+
+  hbi_leafmtxp* lf = new hbi_leafmtxp_s();
+  lf->ctl = c;
+  lf->leaves = c->S.leaves;
+  const int nl = (int)lf->leaves.size();
+  std::vector<double*> chunk_of(nl, nullptr), chunks;
+  std::vector<int64_t> choff(nl, 0);
+  cudaEvent_t e0, e1, e2;
+  cudaEventCreate(&e0); cudaEventCreate(&e1); cudaEventCreate(&e2);
+  cudaEventRecord(e0, c->stream);
+  rc = run_aca(c, G, lf->leaves, chunk_of, choff, chunks);
+  if (rc) {
+    for (double* p : chunks) cudaFree(p);
+    delete lf;
+    return rc;
+  }
+  cudaEventRecord(e1, c->stream);
+  // body offsets in HACApK's contiguous packing
+  lf->off.assign(nl + 1, 0);
+  int64_t tot = 0;
+  for (int i = 0; i < nl; i++) {
+    lf->off[i] = tot;
+    const Leaf& L = lf->leaves[i];
+    tot += L.ltmtx == 1 ? (int64_t)L.kt * (L.ndl + L.ndt) : (int64_t)L.ndl * L.ndt;
+    if (L.ltmtx == 1) lf->ktmax = std::max(lf->ktmax, L.kt);
+  }
+  lf->off[nl] = tot;
+  cudaError_t ce = dalloc(&lf->d_body, tot);
+  if (ce != cudaSuccess) {
+    for (double* p : chunks) cudaFree(p);
+    delete lf;
+    return fail(HBI_ERR_NOMEM, "H-matrix body of %lld doubles", (long long)tot);
+  }
+  // gather low-rank factors into place
+  {
+    std::vector<const double*> src;
+    std::vector<int64_t> dof, len;
+    for (int i = 0; i < nl; i++) {
+      const Leaf& L = lf->leaves[i];
+      if (L.ltmtx == 1 && L.kt > 0) {
+        src.push_back(chunk_of[i] + choff[i]);
+        dof.push_back(lf->off[i]);
+        len.push_back((int64_t)L.kt * (L.ndl + L.ndt));
+      }
+    }
+    const double** d_src = nullptr;
+    int64_t *d_dof = nullptr, *d_len = nullptr;
+    std::vector<const double*> srcv(src.begin(), src.end());
+    if (upload(&d_src, srcv, c->stream) != cudaSuccess || upload(&d_dof, dof, c->stream) != cudaSuccess ||
+        upload(&d_len, len, c->stream) != cudaSuccess)
+      return fail(HBI_ERR_CUDA, "segment upload");
+    launch_copy_segments(d_src, d_dof, d_len, (int)src.size(), lf->d_body, c->stream);
+    CK(cudaStreamSynchronize(c->stream));
+    dfree(d_src); dfree(d_dof); dfree(d_len);
+    for (double* p : chunks) cudaFree(p);
+  }
+  // dense near field
+  {
+    std::vector<DenseTask> dt;
+    std::vector<int64_t> start;
+    int64_t acc = 0;
+    for (int i = 0; i < nl; i++) {
+      const Leaf& L = lf->leaves[i];
+      if (L.ltmtx != 2) continue;
+      dt.push_back(DenseTask{L.ndl, L.ndt, L.nstrtl, L.nstrtt, lf->off[i]});
+      start.push_back(acc);
+      acc += (int64_t)L.ndl * L.ndt;
+    }
+    DenseTask* d_dt = nullptr;
+    int64_t* d_start = nullptr;
+    CK(upload(&d_dt, dt, c->stream));
+    CK(upload(&d_start, start, c->stream));
+    launch_dense_fill(G.b, c->d_lod, d_dt, (int)dt.size(), d_start, acc, lf->d_body, c->stream);
+    cudaEventRecord(e2, c->stream);
+    CK(cudaStreamSynchronize(c->stream));
+    dfree(d_dt); dfree(d_start);
+  }
+  float ms1 = 0, ms2 = 0;
+  cudaEventElapsedTime(&ms1, e0, e1);
+  cudaEventElapsedTime(&ms2, e1, e2);
+  lf->t_aca = ms1 * 1e-3;
+  lf->t_dense = ms2 * 1e-3;
+  cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(e2);
+  *out = lf;
+  return HBI_OK;
+}
+
+extern "C" int hbi_free_leafmtxp(hbi_leafmtxp* lf) {
+  if (!lf) return HBI_OK;
+  dfree(lf->d_body);
+  delete lf;
+  return HBI_OK;
+}
+
+extern "C" int hbi_leaf_count(const hbi_leafmtxp* lf, int* nleaf, int* ktmax) {
+  if (!lf) return fail(HBI_ERR_ARG, "null");
+  if (nleaf) *nleaf = (int)lf->leaves.size();
+  if (ktmax) *ktmax = lf->ktmax;
+  return HBI_OK;
+}
+
+extern "C" int hbi_get_leaves(const hbi_leafmtxp* lf, int* o) {
+  if (!lf || !o) return fail(HBI_ERR_ARG, "null");
+  for (size_t i = 0; i < lf->leaves.size(); i++) {
+    const Leaf& L = lf->leaves[i];
+    o[6 * i + 0] = L.ltmtx; o[6 * i + 1] = L.kt; o[6 * i + 2] = L.nstrtl;
+    o[6 * i + 3] = L.ndl; o[6 * i + 4] = L.nstrtt; o[6 * i + 5] = L.ndt;
+  }
+  return HBI_OK;
+}
+
+extern "C" int hbi_get_body(const hbi_leafmtxp* lf, int64_t* offsets, double* body) {
+  if (!lf || !offsets) return fail(HBI_ERR_ARG, "null");
+  memcpy(offsets, lf->off.data(), sizeof(int64_t) * lf->off.size());
+  if (body) CK(cudaMemcpy(body, lf->d_body, sizeof(double) * lf->off.back(), cudaMemcpyDeviceToHost));
+  return HBI_OK;
+}
+
+extern "C" int hbi_entry_ij(const hbi_bemv* bv, int n, const int* i, const int* j, double* out) {
+  int rc = check_bemv(bv);
+  if (rc) return rc;
+  if (n < 0 || (n > 0 && (!i || !j || !out))) return fail(HBI_ERR_ARG, "hbi_entry_ij: null arrays");
+  if (n == 0) return HBI_OK;
+  cudaStream_t st;
+  CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  DevGeom G;
+  rc = G.upload(bv, st);
+  if (rc) { cudaStreamDestroy(st); return rc; }
+  std::vector<int> ii(n), jj(n);
+  for (int k = 0; k < n; k++) {
+    if (i[k] < 1 || i[k] > bv->nd || j[k] < 1 || j[k] > bv->nd) { cudaStreamDestroy(st); return fail(HBI_ERR_ARG, "index out of range"); }
+    ii[k] = i[k] - 1; jj[k] = j[k] - 1;
+  }
+  int *di = nullptr, *dj = nullptr;
+  double* dout = nullptr;
+  CK(upload(&di, ii, st));
+  CK(upload(&dj, jj, st));
+  CK(dalloc(&dout, n));
+  launch_entries(G.b, di, dj, n, dout, st);
+  CK(cudaMemcpyAsync(out, dout, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  dfree(di); dfree(dj); dfree(dout);
+  cudaStreamDestroy(st);
+  return HBI_OK;
+}
+
+// ---------------------------------------------------------- construct
+static int ensure_chains(hbi_ctl* c) {
+  if (c->have_chains) return HBI_OK;
+  plan_chains(c->nd, c->S.leaves, c->chains);
+  dfree(c->d_row_fc); dfree(c->d_chain_ptr); dfree(c->d_chain_leaf);
+  CK(upload(&c->d_row_fc, c->chains.row_fc, c->stream));
+  CK(upload(&c->d_chain_ptr, c->chains.chain_ptr, c->stream));
+  CK(upload(&c->d_chain_leaf, c->chains.chain_leaf, c->stream));
+  c->have_chains = true;
+  return HBI_OK;
+}
+
+extern "C" int hbi_construct_lh(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* c, int storage) {
+  if (!out || !lf || !c) return fail(HBI_ERR_ARG, "hbi_construct_lh: null");
+  if (storage < 0 || storage > 2) return fail(HBI_ERR_ARG, "storage must be HBI_STORE_F64/F32/BF16");
+  if (lf->ctl != c || !c->have_tree) return fail(HBI_ERR_STATE, "construct_LH needs the ctl used by generate");
+  int rc = ensure_chains(c);
+  if (rc) return rc;
+  hbi_lhp* h = new hbi_lhp_s();
+  h->ctl = c;
+  h->n = c->nd;
+  h->storage = storage;
+  h->leaves = lf->leaves;
+  const int esz = storage == ST_F64 ? 8 : storage == ST_F32 ? 4 : 2;
+  const int chunk_rows = getenv("HBI_P1_CHUNK") ? atoi(getenv("HBI_P1_CHUNK")) : 2048;
+  plan_matrix(lf->leaves, 16 / esz, chunk_rows, 8, h->plan);
+  MatPlan& P = h->plan;
+  const int nl = (int)lf->leaves.size();
+  // factor store in the requested precision
+  h->store_bytes = (size_t)P.store_elems * esz;
+  CK(cudaMalloc(&h->d_store, std::max<size_t>(h->store_bytes, 16)));
+  CK(cudaMemsetAsync(h->d_store, 0, std::max<size_t>(h->store_bytes, 16), c->stream));
+  {
+    std::vector<int64_t> so(nl), dof(nl);
+    std::vector<int32_t> kind(nl), rows(nl), cols(nl), kts(nl);
+    for (int i = 0; i < nl; i++) {
+      so[i] = lf->off[i]; dof[i] = P.leaf_off[i];
+      kind[i] = lf->leaves[i].ltmtx; rows[i] = lf->leaves[i].ndl; cols[i] = lf->leaves[i].ndt; kts[i] = lf->leaves[i].kt;
+    }
+    int64_t *d_so = nullptr, *d_dof = nullptr;
+    int32_t *d_kind = nullptr, *d_rows = nullptr, *d_cols = nullptr, *d_kts = nullptr;
+    CK(upload(&d_so, so, c->stream)); CK(upload(&d_dof, dof, c->stream));
+    CK(upload(&d_kind, kind, c->stream)); CK(upload(&d_rows, rows, c->stream));
+    CK(upload(&d_cols, cols, c->stream)); CK(upload(&d_kts, kts, c->stream));
+    launch_store_convert(lf->d_body, nullptr, nl, d_so, d_dof, d_kind, d_rows, d_cols, d_kts, h->d_store, storage, c->stream);
+    CK(cudaStreamSynchronize(c->stream));
+    dfree(d_so); dfree(d_dof); dfree(d_kind); dfree(d_rows); dfree(d_cols); dfree(d_kts);
+  }
+  // phase-1 items and low-rank leaf table
+  const int nlr = (int)P.lr_leaf.size();
+  std::vector<LrInfo> lr(nlr);
+  for (int q = 0; q < nlr; q++) {
+    lr[q].kt = lf->leaves[P.lr_leaf[q]].kt;
+    lr[q].nparts = P.lr_nparts[q];
+    lr[q].nitems = 0;
+    lr[q].poff = P.lr_poff[q];
+    lr[q].zoff = P.lr_zoff[q];
+    lr[q].pad = 0;
+  }
+  std::vector<P1ItemDev> items(P.p1.size());
+  for (size_t t = 0; t < P.p1.size(); t++) {
+    const P1Item& I = P.p1[t];
+    P1ItemDev& d = items[t];
+    d.voff = I.voff; d.ldv = I.ldv; d.nt = I.nt; d.x0 = I.x0; d.k0 = I.k0; d.nk = I.nk; d.lr = I.leaf; d.pad = 0;
+    const LrInfo& L = lr[I.leaf];
+    d.pout = L.nparts == 1 ? L.zoff + I.k0 : L.poff + I.part * L.kt + I.k0;
+    lr[I.leaf].nitems++;
+  }
+  std::vector<LeafDescDev> desc(nl);
+  for (int i = 0; i < nl; i++) {
+    const LeafDesc& s = P.desc[i];
+    desc[i] = LeafDescDev{s.off, s.row0, s.ndl, s.kind, s.kt_or_ndt, s.aux, 0};
+  }
+  const size_t accsz = storage == ST_F64 ? 8 : 4;
+  CK(upload(&h->d_p1, items, c->stream));
+  CK(upload(&h->d_lr, lr, c->stream));
+  CK(upload(&h->d_desc, desc, c->stream));
+  CK(dalloc(&h->d_cnt, nlr));
+  CK(cudaMemset(h->d_cnt, 0, sizeof(int) * std::max(nlr, 1)));
+  CK(cudaMalloc(&h->d_part, std::max<size_t>(P.plen, 1) * accsz));
+  CK(cudaMalloc(&h->d_z, std::max<size_t>(P.zlen, 1) * accsz));
+  CK(cudaMemset(h->d_z, 0, std::max<size_t>(P.zlen, 1) * accsz));
+  CK(dalloc(&h->d_x, h->n));
+  CK(dalloc(&h->d_y, h->n));
+  h->md.store = h->d_store;
+  h->md.storage = storage;
+  h->md.p1 = h->d_p1;
+  h->md.np1 = (int)items.size();
+  h->md.lr = h->d_lr;
+  h->md.lr_cnt = h->d_cnt;
+  h->md.part = h->d_part;
+  h->md.z = h->d_z;
+  h->md.desc = h->d_desc;
+  h->md.scale = 1.0;
+  h->cd = ChainDev{c->nd, c->d_row_fc, c->d_chain_ptr, c->d_chain_leaf};
+  h->alg_bytes = (double)P.factor_elems * esz + (double)h->n * 8 * 2;
+  *out = h;
+  return HBI_OK;
+}
+
+extern "C" int hbi_free_lh(hbi_lhp* h) {
+  if (!h) return HBI_OK;
+  if (h->d_store) cudaFree(h->d_store);
+  dfree(h->d_p1); dfree(h->d_lr); dfree(h->d_cnt); dfree(h->d_desc); dfree(h->d_x); dfree(h->d_y);
+  if (h->d_part) cudaFree(h->d_part);
+  if (h->d_z) cudaFree(h->d_z);
+  delete h;
+  return HBI_OK;
+}
+
+extern "C" int hbi_lh_info(const hbi_lhp* h, int64_t* fe, int64_t* sb, double* ab) {
+  if (!h) return fail(HBI_ERR_ARG, "null");
+  if (fe) *fe = h->plan.factor_elems;
+  if (sb) *sb = (int64_t)h->store_bytes;
+  if (ab) *ab = h->alg_bytes;
+  return HBI_OK;
+}
+
+extern "C" int hbi_adot_lattice_hyp_dev(double* d_au, hbi_lhp* h, const double* d_u, void* stream) {
+  if (!h || !d_au || !d_u) return fail(HBI_ERR_ARG, "hbi_adot_lattice_hyp_dev: null");
+  cudaStream_t st = stream ? (cudaStream_t)stream : h->ctl->stream;
+  launch_phase1(&h->md, 1, d_u, h->ctl->sm_count, st);
+  double* ys[2] = {d_au, nullptr};
+  launch_phase2_plain(&h->md, 1, h->cd, d_u, ys, st);
+  CK(cudaGetLastError());
+  return HBI_OK;
+}
+
+extern "C" int hbi_adot_lattice_hyp(double* au, hbi_lhp* h, hbi_ctl* c, double* wws, const double* u) {
+  (void)wws;
+  if (!h || !au || !u) return fail(HBI_ERR_ARG, "hbi_adot_lattice_hyp: null");
+  if (c && c != h->ctl) return fail(HBI_ERR_ARG, "st_ctl does not own st_LHp");
+  cudaStream_t st = h->ctl->stream;
+  CK(cudaMemcpyAsync(h->d_x, u, sizeof(double) * h->n, cudaMemcpyHostToDevice, st));
+  int rc = hbi_adot_lattice_hyp_dev(h->d_y, h, h->d_x, st);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(au, h->d_y, sizeof(double) * h->n, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return HBI_OK;
+}
+
+// ---------------------------------------------------------------- RK45
+struct hbi_rk_s {
+  hbi_lhp* ls = nullptr;
+  hbi_lhp* ln = nullptr;
+  int n = 0, nmat = 1;
+  RkDev R{};
+  MatDev mats[2];
+  std::vector<double*> allocs;
+  double* h_ctl = nullptr;  // pinned: h, eps, emax, huge index
+  cudaStream_t st = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int launches = 0;
+};
+
+static void cash_karp(double* B, double* C, double* DC) {
+  // the reference's PARAMETER statements (main_LH.f90:2490-2496) evaluate
+  // 3./40., .3, 37./378. ... in default real, then widen to real(8)
+  B[0] = .2;
+  B[1] = (double)(3.f / 40.f); B[2] = (double)(9.f / 40.f);
+  B[3] = (double).3f; B[4] = (double)-.9f; B[5] = (double)1.2f;
+  B[6] = (double)(-(11.f / 54.f)); B[7] = 2.5; B[8] = (double)(-(70.f / 27.f)); B[9] = (double)(35.f / 27.f);
+  B[10] = (double)(1631.f / 55296.f); B[11] = (double)(175.f / 512.f); B[12] = (double)(575.f / 13824.f);
+  B[13] = (double)(44275.f / 110592.f); B[14] = (double)(253.f / 4096.f);
+  const double C1 = (double)(37.f / 378.f), C3 = (double)(250.f / 621.f), C4 = (double)(125.f / 594.f),
+               C6 = (double)(512.f / 1771.f);
+  C[0] = C1; C[1] = 0; C[2] = C3; C[3] = C4; C[4] = 0; C[5] = C6;
+  DC[0] = C1 - (double)(2825.f / 27648.f); DC[1] = 0;
+  DC[2] = C3 - (double)(18575.f / 48384.f);
+  DC[3] = C4 - (double)(13525.f / 55296.f);
+  DC[4] = (double)(-(277.f / 14336.f));
+  DC[5] = C6 - (double).25f;
+}
+
+extern "C" int hbi_rk_create(hbi_rk** out, const hbi_rsf_params* p, hbi_lhp* ls, hbi_lhp* ln) {
+  if (!out || !p || !ls) return fail(HBI_ERR_ARG, "hbi_rk_create: null");
+  if (p->ncell != ls->n) return fail(HBI_ERR_ARG, "ncell %d != operator size %d", p->ncell, ls->n);
+  if (!p->a || !p->b || !p->dc || !p->f0 || !p->taudot || !p->sigdot || !p->vpl)
+    return fail(HBI_ERR_ARG, "rsf parameter arrays must be non-null");
+  if (ln) {
+    if (ln->n != ls->n || ln->storage != ls->storage) return fail(HBI_ERR_ARG, "H_s and H_n differ in size or storage");
+    if (ln->leaves.size() != ls->leaves.size()) return fail(HBI_ERR_ARG, "H_s and H_n have different leaf lists");
+    for (size_t i = 0; i < ls->leaves.size(); i++) {
+      const Leaf &a = ls->leaves[i], &b = ln->leaves[i];
+      if (a.ltmtx != b.ltmtx || a.nstrtl != b.nstrtl || a.ndl != b.ndl || a.nstrtt != b.nstrtt || a.ndt != b.ndt)
+        return fail(HBI_ERR_ARG, "H_s and H_n have different leaf lists");
+    }
+  }
+  hbi_rk* r = new hbi_rk_s();
+  r->ls = ls; r->ln = ln; r->n = p->ncell; r->nmat = ln ? 2 : 1;
+  r->st = ls->ctl->stream;
+  const int n = r->n;
+  auto mk = [&](double** d, size_t cnt) -> int {
+    if (dalloc(d, cnt) != cudaSuccess) return 1;
+    r->allocs.push_back(*d);
+    return 0;
+  };
+  auto cp = [&](const double** d, const double* h) -> int {
+    double* t;
+    if (mk(&t, n)) return 1;
+    if (cudaMemcpy(t, h, sizeof(double) * n, cudaMemcpyHostToDevice) != cudaSuccess) return 1;
+    *d = t;
+    return 0;
+  };
+  RkDev& R = r->R;
+  R.n = n; R.nmat = r->nmat; R.evlaw = p->evlaw; R.backslip = p->backslip; R.limitsigma = p->limitsigma;
+  R.vref = p->vref; R.minsig = p->minsig; R.maxsig = p->maxsig;
+  R.rigid_over_2vs = 0.5 * 32.04 / 3.464;
+  int bad = 0;
+  bad |= cp(&R.a, p->a); bad |= cp(&R.b, p->b); bad |= cp(&R.dc, p->dc); bad |= cp(&R.f0, p->f0);
+  bad |= cp(&R.taudot, p->taudot); bad |= cp(&R.sigdot, p->sigdot); bad |= cp(&R.vpl, p->vpl);
+  bad |= mk(&R.y, 3 * n); bad |= mk(&R.ys, 3 * n); bad |= mk(&R.vs, n); bad |= mk(&R.x0, n);
+  bad |= mk(&R.xb[0], n); bad |= mk(&R.xb[1], n); bad |= mk(&R.K, 18 * (size_t)n);
+  bad |= mk(&R.yout, 3 * n); bad |= mk(&R.yerr, 3 * n); bad |= mk(&R.ebuf, 3 * n); bad |= mk(&R.ctl, 4);
+  if (bad || cudaMallocHost(&r->h_ctl, 4 * sizeof(double)) != cudaSuccess) {
+    hbi_rk_free(r);
+    return fail(HBI_ERR_NOMEM, "RK state allocation");
+  }
+  r->mats[0] = ls->md; r->mats[0].scale = p->scale_s;
+  if (ln) { r->mats[1] = ln->md; r->mats[1].scale = p->scale_n; }
+  double B[15], C[6], DC[6];
+  cash_karp(B, C, DC);
+  set_tableau(B, C, DC);
+  r->launches = 1 + 6 * (r->nmat + 1);
+  *out = r;
+  return HBI_OK;
+}
+
+extern "C" int hbi_rk_free(hbi_rk* r) {
+  if (!r) return HBI_OK;
+  if (r->gexec) cudaGraphExecDestroy(r->gexec);
+  for (double* p : r->allocs) cudaFree(p);
+  if (r->h_ctl) cudaFreeHost(r->h_ctl);
+  delete r;
+  return HBI_OK;
+}
+
+extern "C" int hbi_rk_launches_per_attempt(const hbi_rk* r) { return r ? r->launches : 0; }
+
+extern "C" int hbi_rk_set_state(hbi_rk* r, const double* y) {
+  if (!r || !y) return fail(HBI_ERR_ARG, "null");
+  CK(cudaMemcpy(r->R.y, y, sizeof(double) * 3 * r->n, cudaMemcpyHostToDevice));
+  return HBI_OK;
+}
+extern "C" int hbi_rk_get_state(hbi_rk* r, double* y) {
+  if (!r || !y) return fail(HBI_ERR_ARG, "null");
+  CK(cudaStreamSynchronize(r->st));
+  CK(cudaMemcpy(y, r->R.y, sizeof(double) * 3 * r->n, cudaMemcpyDeviceToHost));
+  return HBI_OK;
+}
+
+// the six stages of one Cash-Karp attempt (rkck) as a fixed launch sequence
+static void enqueue_attempt(hbi_rk* r, cudaStream_t st) {
+  RkDev& R = r->R;
+  const ChainDev& ch = r->ls->cd;
+  const int sm = r->ls->ctl->sm_count;
+  launch_rk_prepare(R, st);
+  for (int s = 0; s < 6; s++) {
+    const double* xin = s == 0 ? R.x0 : R.xb[s & 1];
+    double* xout = R.xb[(s + 1) & 1];
+    launch_phase1(r->mats, r->nmat, xin, sm, st);
+    launch_phase2_rk(r->mats, r->nmat, ch, xin, R, s, xout, st);
+  }
+}
+
+static int run_attempt(hbi_rk* r, double h, double eps, double* errmax) {
+  cudaStream_t st = r->st;
+  r->h_ctl[0] = h;
+  r->h_ctl[1] = eps;
+  CK(cudaMemcpyAsync(r->R.ctl, r->h_ctl, 2 * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (!r->gexec) {
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    enqueue_attempt(r, st);
+    CK(cudaStreamEndCapture(st, &g));
+    CK(cudaGraphInstantiate(&r->gexec, g, 0));
+    cudaGraphDestroy(g);
+  }
+  CK(cudaGraphLaunch(r->gexec, st));
+  CK(cudaMemcpyAsync(r->h_ctl + 2, r->R.ctl + 2, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  double e = r->h_ctl[2];
+  long long hidx;
+  memcpy(&hidx, &r->h_ctl[3], sizeof(hidx));
+  if (hidx >= 0) {
+    // a component with ytemp-1 == ytemp: the reference resets errmax to 10 at
+    // that index, so only later components can raise it (main_LH.f90:2309-2313)
+    std::vector<double> eb(3 * (size_t)r->n);
+    CK(cudaMemcpy(eb.data(), r->R.ebuf, sizeof(double) * eb.size(), cudaMemcpyDeviceToHost));
+    e = 10.0;
+    for (size_t c = (size_t)hidx + 1; c < eb.size(); c++)
+      if (eb[c] > e) e = eb[c];
+  }
+  *errmax = e;
+  return HBI_OK;
+}
+
+extern "C" int hbi_rkck(hbi_rk* r, double h, double eps, double* yout, double* yerr, double* errmax) {
+  if (!r) return fail(HBI_ERR_ARG, "null");
+  double e;
+  int rc = run_attempt(r, h, eps, &e);
+  if (rc) return rc;
+  if (errmax) *errmax = e;
+  if (yout) CK(cudaMemcpy(yout, r->R.yout, sizeof(double) * 3 * r->n, cudaMemcpyDeviceToHost));
+  if (yerr) CK(cudaMemcpy(yerr, r->R.yerr, sizeof(double) * 3 * r->n, cudaMemcpyDeviceToHost));
+  return HBI_OK;
+}
+
+extern "C" int hbi_derivs(hbi_rk* r, const double* y, double* dydx) {
+  if (!r || !y || !dydx) return fail(HBI_ERR_ARG, "null");
+  // stage 0 of an attempt from y gives k1 = f(y)
+  std::vector<double> keep(3 * (size_t)r->n);
+  CK(cudaMemcpy(keep.data(), r->R.y, sizeof(double) * keep.size(), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(r->R.y, y, sizeof(double) * keep.size(), cudaMemcpyHostToDevice));
+  double e;
+  int rc = run_attempt(r, 0.0, 1.0, &e);
+  if (rc) return rc;
+  CK(cudaMemcpy(dydx, r->R.K, sizeof(double) * keep.size(), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(r->R.y, keep.data(), sizeof(double) * keep.size(), cudaMemcpyHostToDevice));
+  return HBI_OK;
+}
+
+extern "C" int hbi_rkqs(hbi_rk* r, double* x, double htry, double eps, double dtmax, double* hdid, double* hnext,
+                        double* errmax, int* nrjct) {
+  if (!r || !x) return fail(HBI_ERR_ARG, "null");
+  // rkqs constants: SAFETY=0.9, PGROW=-0.2, PSHRNK=-0.25, tiny=1e-20 written as
+  // default-real literals (main_LH.f90:2290)
+  const double SAFETY = (double)0.9f, PGROW = (double)-0.2f, PSHRNK = -0.25, tiny = (double)1e-20f;
+  double h = htry, e = 0.0;
+  int nr = 0;
+  for (;;) {
+    int rc = run_attempt(r, h, eps, &e);
+    if (rc) return rc;
+    if ((e < 1.0) && (e > tiny)) break;
+    nr++;
+    if (e > tiny) h = std::max(0.5 * h, SAFETY * h * std::pow(e, PSHRNK));
+    else h = 0.5 * h;
+    const double xnew = *x + h;
+    if (xnew - *x < 1.e-15) {
+      if (errmax) *errmax = e;
+      if (nrjct) *nrjct = nr;
+      return fail(HBI_ERR_CONVERGE, "Runge-Kutta step size underflow at x=%.17g", *x);
+    }
+  }
+  double hn = std::min(2 * h, SAFETY * h * std::pow(e, PGROW));
+  hn = std::min(hn, dtmax);
+  CK(cudaMemcpyAsync(r->R.y, r->R.yout, sizeof(double) * 3 * r->n, cudaMemcpyDeviceToDevice, r->st));
+  CK(cudaStreamSynchronize(r->st));
+  if (hdid) *hdid = h;
+  if (hnext) *hnext = hn;
+  if (errmax) *errmax = e;
+  if (nrjct) *nrjct = nr;
+  *x = *x + h;
+  return HBI_OK;
+}

@@ -1,0 +1,109 @@
+// hbi_kernels.cuh -- device-side task records and kernel launchers shared by
+// the C ABI (hbi_capi.cu) and the kernel translation units.
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "hbi_entries.cuh"
+
+#ifndef HBI_ACA_NT
+#define HBI_ACA_NT 128
+#endif
+
+namespace hbi {
+
+// ---- assembly ------------------------------------------------------------
+struct AcaTask {
+  int ndl, ndt, nstrtl, nstrtt, kcap, leaf;
+  int64_t scratch;  // element offset of this task's scratch in the arena
+};
+struct DenseTask {
+  int ndl, ndt, nstrtl, nstrtt;
+  int64_t off;  // element offset in the FP64 store (a1(ndt,ndl))
+};
+struct AcaParams {
+  double eps, pACA_EPS, znrmmat, kmin;
+  int kmax;
+};
+inline int64_t aca_scratch_elems(int ndl, int ndt, int kcap) {
+  // zaa, zab, pa_ref, pb_ref (doubles) + two int masks (rounded to doubles)
+  return (int64_t)(ndl + ndt) * kcap + (ndl + ndt) + ((int64_t)(ndl + ndt) + 1) / 2 + 2;
+}
+
+void launch_aca(const DevBemv& b, const int* lod, const AcaTask* tasks, int ntask, double* arena, int* result,
+                const AcaParams& P, cudaStream_t st);
+void launch_aca_compact(const AcaTask* tasks, int ntask, const int* kt, const int64_t* dst_off, const double* arena,
+                        double* dst, cudaStream_t st);
+void launch_dense_fill(const DevBemv& b, const int* lod, const DenseTask* tasks, int ntask, const int64_t* task_start,
+                       int64_t total, double* store, cudaStream_t st);
+void launch_entries(const DevBemv& b, const int* ii, const int* jj, int n, double* out, cudaStream_t st);
+
+// ---- matvec ----------------------------------------------------------------
+enum { ST_F64 = 0, ST_F32 = 1, ST_BF16 = 2 };
+
+struct P1ItemDev {
+  int64_t voff;
+  int32_t ldv, nt, x0, k0, nk, lr, pout, pad;
+};
+struct LeafDescDev {
+  int64_t off;
+  int32_t row0, ndl, kind, kt_or_ndt, aux, pad;
+};
+// per low-rank leaf, for the multi-chunk reduction of phase 1
+struct LrInfo {
+  int32_t kt, nparts, nitems, poff, zoff, pad;
+};
+
+struct MatDev {            // one H-matrix on the device
+  const void* store;       // factor store, element type per `storage`
+  int storage;
+  const P1ItemDev* p1;
+  int np1;
+  const LrInfo* lr;
+  int* lr_cnt;             // arrival counters (self-resetting)
+  void* part;              // partial sums (Acc type)
+  void* z;                 // z = V^T x per low-rank leaf (Acc type)
+  const LeafDescDev* desc;
+  double scale;            // result multiplier (1/ds0 for 3dph, else 1)
+};
+struct ChainDev {
+  int n;
+  const int32_t* row_fc;
+  const int32_t* chain_ptr;
+  const int32_t* chain_leaf;
+};
+
+// RK (Cash-Karp) stage state on the device; all arrays in cluster order
+struct RkDev {
+  int n, nmat, evlaw, backslip, limitsigma;
+  double vref, minsig, maxsig, rigid_over_2vs;
+  const double *a, *b, *dc, *f0, *taudot, *sigdot, *vpl;
+  double* y;       // accepted state (3n): psi,tau,sigma interleaved
+  double* ys;      // stage state (3n)
+  double* vs;      // slip rate of the stage state (n)
+  double* x0;      // matvec input of stage 0 (n)
+  double* xb[2];   // ping-pong matvec inputs of stages 1..5 (n)
+  double* K;       // stage derivatives, 6 x 3n
+  double* yout;    // 5th-order solution (3n)
+  double* yerr;    // embedded error (3n)
+  double* ebuf;    // |yerr/yout|/eps per component (3n)
+  double* ctl;     // [0]=h [1]=eps  [2]=emax (as bits) [3]=huge index (as int64)
+};
+
+void launch_phase1(const MatDev* mats, int nmat, const double* x, int sm_count, cudaStream_t st);
+void launch_phase2_plain(const MatDev* mats, int nmat, const ChainDev& ch, const double* x, double* const* y,
+                         cudaStream_t st);
+void launch_phase2_rk(const MatDev* mats, int nmat, const ChainDev& ch, const double* x, const RkDev& rk, int stage,
+                      double* xnext, cudaStream_t st);
+void launch_rk_prepare(const RkDev& rk, cudaStream_t st);
+void set_tableau(const double* B15, const double* C6, const double* DC6);
+// dst[dst_off[i] : +len[i]] = src[i][0 : len[i]]
+void launch_copy_segments(const double* const* src, const int64_t* dst_off, const int64_t* len, int nseg,
+                          double* dst, cudaStream_t st);
+void launch_store_convert(const double* src, const LeafDescDev* desc_src_dense_transpose, int nleaf,
+                          const int64_t* src_off, const int64_t* dst_off, const int32_t* kind, const int32_t* rows,
+                          const int32_t* cols, const int32_t* kts, void* dst, int storage, cudaStream_t st);
+
+}  // namespace hbi

@@ -1,0 +1,345 @@
+// hbi_matvec.cu -- lattice H-matrix-vector product and the fused
+// rate-and-state / Cash-Karp stage epilogue.
+//
+// Replaces HACApK_adot_lattice_hyp + HACApK_adot_body_lfmtx_hyp_contiguous
+// (m_HACApK_solve.f90:220-337, 2108-2164).  Two kernels per product:
+//   phase 1  z_l = V_l^T x for every low-rank leaf: one warp per (leaf, row
+//            chunk, column group) item; leaves split over several chunks are
+//            summed by the last-arriving warp in a fixed order;
+//   phase 2  one thread per row walks the leaves covering its row (coarse to
+//            fine) and accumulates U_l z_l and A_l x; the sum order per row is
+//            fixed, so the product is deterministic without atomics.
+// Factors are stored column-major (U, V: ndl/ndt x kt; dense A: ndl x ndt) in
+// FP64, FP32 or BF16; FP32/BF16 storage accumulates in FP32.
+// Phase 2 optionally runs the RK stage epilogue (derivs/deriv/rkck of
+// main_LH.f90:2053-2244, 2472-2554) for its row, so a Cash-Karp attempt is
+// 6 x (phase 1, phase 2) launches.
+#include <cuda_bf16.h>
+
+#include "hbi_kernels.cuh"
+
+namespace hbi {
+
+__constant__ double cB[15];   // B21 B31 B32 B41 B42 B43 B51..B54 B61..B65
+__constant__ double cC[6];    // C1 0 C3 C4 0 C6
+__constant__ double cDC[6];   // DC1 0 DC3 DC4 DC5 DC6
+
+void set_tableau(const double* B, const double* C, const double* DC) {
+  cudaMemcpyToSymbol(cB, B, sizeof(double) * 15);
+  cudaMemcpyToSymbol(cC, C, sizeof(double) * 6);
+  cudaMemcpyToSymbol(cDC, DC, sizeof(double) * 6);
+}
+
+template <typename T> struct AccOf { typedef float type; };
+template <> struct AccOf<double> { typedef double type; };
+
+__device__ __forceinline__ double ld_acc(const double* p) { return __ldg(p); }
+__device__ __forceinline__ float ld_acc(const float* p) { return __ldg(p); }
+__device__ __forceinline__ float ld_acc(const __nv_bfloat16* p) { return __bfloat162float(__ldg(p)); }
+
+// ---------------------------------------------------------------- phase 1
+template <typename T, int KG>
+__global__ void __launch_bounds__(256) p1_kernel(MatDev m, const double* __restrict__ x) {
+  typedef typename AccOf<T>::type Acc;
+  const int lane = threadIdx.x & 31;
+  const int warp = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  const int nwarps = (int)((gridDim.x * (int64_t)blockDim.x) >> 5);
+  const T* store = (const T*)m.store;
+  Acc* part = (Acc*)m.part;
+  Acc* z = (Acc*)m.z;
+  for (int it = warp; it < m.np1; it += nwarps) {
+    const P1ItemDev I = m.p1[it];
+    Acc acc[KG];
+#pragma unroll
+    for (int kk = 0; kk < KG; kk++) acc[kk] = 0;
+    const T* V = store + I.voff;
+    if (I.nk == KG) {
+      for (int t = lane; t < I.nt; t += 32) {
+        const Acc xv = (Acc)__ldg(&x[I.x0 + t]);
+#pragma unroll
+        for (int kk = 0; kk < KG; kk++) acc[kk] += ld_acc(&V[(int64_t)kk * I.ldv + t]) * xv;
+      }
+    } else {
+      for (int t = lane; t < I.nt; t += 32) {
+        const Acc xv = (Acc)__ldg(&x[I.x0 + t]);
+#pragma unroll
+        for (int kk = 0; kk < KG; kk++)
+          if (kk < I.nk) acc[kk] += ld_acc(&V[(int64_t)kk * I.ldv + t]) * xv;
+      }
+    }
+#pragma unroll
+    for (int kk = 0; kk < KG; kk++)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc[kk] += __shfl_xor_sync(0xffffffffu, acc[kk], o);
+    Acc mine = 0;
+#pragma unroll
+    for (int kk = 0; kk < KG; kk++)
+      if (lane == kk) mine = acc[kk];
+    const LrInfo L = m.lr[I.lr];
+    if (L.nparts == 1) {
+      if (lane < I.nk) z[I.pout + lane] = mine;
+    } else {
+      if (lane < I.nk) part[I.pout + lane] = mine;
+      __threadfence();
+      int last = 0;
+      if (lane == 0) last = (atomicAdd(&m.lr_cnt[I.lr], 1) == L.nitems - 1);
+      last = __shfl_sync(0xffffffffu, last, 0);
+      if (last) {
+        __threadfence();
+        for (int k = lane; k < L.kt; k += 32) {
+          Acc s = 0;
+          for (int p = 0; p < L.nparts; p++) s += __ldcg(&part[L.poff + p * L.kt + k]);
+          z[L.zoff + k] = s;
+        }
+        if (lane == 0) m.lr_cnt[I.lr] = 0;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------- phase 2
+template <typename T>
+__device__ __forceinline__ typename AccOf<T>::type row_sum(const MatDev& m, const ChainDev& ch, int r,
+                                                          const double* __restrict__ x) {
+  typedef typename AccOf<T>::type Acc;
+  const T* store = (const T*)m.store;
+  const Acc* z = (const Acc*)m.z;
+  const int f = __ldg(&ch.row_fc[r]);
+  const int e0 = __ldg(&ch.chain_ptr[f]), e1 = __ldg(&ch.chain_ptr[f + 1]);
+  Acc acc = 0;
+  for (int e = e0; e < e1; e++) {
+    const LeafDescDev L = m.desc[__ldg(&ch.chain_leaf[e])];
+    const int lr = r - L.row0;
+    const T* P = store + L.off + lr;
+    const int cnt = L.kt_or_ndt;
+    if (L.kind == 1) {
+      const Acc* zz = z + L.aux;
+      for (int k = 0; k < cnt; k++) acc += ld_acc(P + (int64_t)k * L.ndl) * zz[k];
+    } else {
+      const double* xx = x + L.aux;
+      for (int t = 0; t < cnt; t++) acc += ld_acc(P + (int64_t)t * L.ndl) * (Acc)__ldg(&xx[t]);
+    }
+  }
+  return acc;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) p2_plain_kernel(MatDev m0, MatDev m1, int nmat, ChainDev ch,
+                                                       const double* __restrict__ x, double* y0, double* y1) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= ch.n) return;
+  y0[r] = (double)row_sum<T>(m0, ch, r, x) * m0.scale;
+  if (nmat == 2) y1[r] = (double)row_sum<T>(m1, ch, r, x) * m1.scale;
+}
+
+// deriv (main_LH.f90:2165-2244): aging (0) and slip (1) laws
+__device__ __forceinline__ void deriv_dev(const RkDev& R, double sum_gs, double sum_gn, double psi, double tau,
+                                          double sig, double vel, double a, double b, double dc, double f0,
+                                          double* out) {
+  double dsig = sum_gn;
+  if (R.limitsigma) {
+    if (sig < R.minsig) dsig = 0;
+    if (sig > R.maxsig) dsig = 0;
+  }
+  const double vref = R.vref;
+  double dpsi;
+  if (R.evlaw == 0) {
+    dpsi = (b == 0) ? 0.0 : b / dc * vref * exp((f0 - psi) / b) - b * fabs(vel) / dc;
+  } else {
+    const double fss = f0 + (a - b) * log(fabs(vel) / vref);
+    dpsi = -(fabs(vel) / dc * (fabs(tau) / sig - fss));
+  }
+  const double e = exp(-psi / a), ch = cosh(tau / sig / a);
+  const double dvdtau = 2 * vref * e * ch / (a * sig);
+  const double dvdsig = -(2 * vref * e * ch * tau / (a * (sig * sig)));
+  const double dvdpsi = -vel / a;
+  const double t = sum_gs - R.rigid_over_2vs * (dvdpsi * dpsi + dvdsig * dsig);
+  out[0] = dpsi;
+  out[1] = t / (1.0 + R.rigid_over_2vs * dvdtau);
+  out[2] = dsig;
+}
+
+__device__ __forceinline__ double slip_rate(double vref, double psi, double tau, double sig, double a) {
+  return 2 * vref * exp(-psi / a) * sinh(tau / sig / a);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) p2_rk_kernel(MatDev m0, MatDev m1, ChainDev ch, const double* __restrict__ x,
+                                                    RkDev R, int s, double* __restrict__ xnext) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  double emax = -1.0;
+  long long hidx = -1;
+  if (r < ch.n) {
+    const double gs = (double)row_sum<T>(m0, ch, r, x) * m0.scale + R.taudot[r];
+    const double gn = (R.nmat == 2 ? (double)row_sum<T>(m1, ch, r, x) * m1.scale : 0.0) + R.sigdot[r];
+    const int n3 = 3 * R.n;
+    const double psi = R.ys[3 * r], tau = R.ys[3 * r + 1], sig = R.ys[3 * r + 2];
+    double k[3];
+    deriv_dev(R, gs, gn, psi, tau, sig, R.vs[r], R.a[r], R.b[r], R.dc[r], R.f0[r], k);
+    double* Ks = R.K + (size_t)s * n3 + 3 * r;
+    Ks[0] = k[0]; Ks[1] = k[1]; Ks[2] = k[2];
+    const double h = R.ctl[0];
+    const double* K0 = R.K + 3 * r;
+    if (s < 5) {
+      double yn[3];
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const double y = R.y[3 * r + c];
+        const double k1 = K0[c];
+        double v;
+        if (s == 0) {
+          v = y + cB[0] * h * k[c];
+        } else if (s == 1) {
+          v = y + h * (cB[1] * k1 + cB[2] * k[c]);
+        } else if (s == 2) {
+          const double k2 = K0[n3 + c];
+          v = y + h * (cB[3] * k1 + cB[4] * k2 + cB[5] * k[c]);
+        } else if (s == 3) {
+          const double k2 = K0[n3 + c], k3 = K0[2 * n3 + c];
+          v = y + h * (cB[6] * k1 + cB[7] * k2 + cB[8] * k3 + cB[9] * k[c]);
+        } else {
+          const double k2 = K0[n3 + c], k3 = K0[2 * n3 + c], k4 = K0[3 * n3 + c];
+          v = y + h * (cB[10] * k1 + cB[11] * k2 + cB[12] * k3 + cB[13] * k4 + cB[14] * k[c]);
+        }
+        yn[c] = v;
+      }
+      R.ys[3 * r] = yn[0]; R.ys[3 * r + 1] = yn[1]; R.ys[3 * r + 2] = yn[2];
+      const double vn = slip_rate(R.vref, yn[0], yn[1], yn[2], R.a[r]);
+      R.vs[r] = vn;
+      xnext[r] = R.backslip ? (vn + 0.0) - R.vpl[r] : vn + 0.0;
+    } else {
+      const double eps = R.ctl[1];
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const double y = R.y[3 * r + c];
+        const double k1 = K0[c], k3 = K0[2 * n3 + c], k4 = K0[3 * n3 + c], k5 = K0[4 * n3 + c], k6 = k[c];
+        const double yo = y + h * (cC[0] * k1 + cC[2] * k3 + cC[3] * k4 + cC[5] * k6);
+        const double ye = h * (cDC[0] * k1 + cDC[2] * k3 + cDC[3] * k4 + cDC[4] * k5 + cDC[5] * k6);
+        R.yout[3 * r + c] = yo;
+        R.yerr[3 * r + c] = ye;
+        const double e = fabs(ye / yo) / eps;
+        R.ebuf[3 * r + c] = e;
+        if (e > emax) emax = e;
+        if (yo - 1 == yo) hidx = 3 * r + c;
+      }
+    }
+  }
+  if (s == 5) {
+    // block-wide max of e (NaN never wins) and of the last huge index
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double oe = __shfl_xor_sync(0xffffffffu, emax, o);
+      if (oe > emax) emax = oe;
+      const long long oh = __shfl_xor_sync(0xffffffffu, hidx, o);
+      if (oh > hidx) hidx = oh;
+    }
+    if ((threadIdx.x & 31) == 0) {
+      if (emax >= 0.0) atomicMax((unsigned long long*)&R.ctl[2], (unsigned long long)__double_as_longlong(emax));
+      if (hidx >= 0) atomicMax((long long*)&R.ctl[3], hidx);
+    }
+  }
+}
+
+// start of an attempt: stage state = accepted state, its slip rate and the
+// stage-0 matvec input; clear the attempt's error accumulators
+__global__ void rk_prepare_kernel(RkDev R) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r == 0) {
+    R.ctl[2] = 0.0;
+    ((long long*)R.ctl)[3] = -1;
+  }
+  if (r >= R.n) return;
+  const double psi = R.y[3 * r], tau = R.y[3 * r + 1], sig = R.y[3 * r + 2];
+  R.ys[3 * r] = psi; R.ys[3 * r + 1] = tau; R.ys[3 * r + 2] = sig;
+  const double v = slip_rate(R.vref, psi, tau, sig, R.a[r]);
+  R.vs[r] = v;
+  R.x0[r] = R.backslip ? (v + 0.0) - R.vpl[r] : v + 0.0;
+}
+
+// FP64 HACApK body -> matvec store (type T): low rank [V][U] unchanged,
+// dense a1(ndt,ndl) transposed to column-major ndl x ndt
+template <typename T>
+__device__ __forceinline__ T cvt(double v);
+template <> __device__ __forceinline__ double cvt<double>(double v) { return v; }
+template <> __device__ __forceinline__ float cvt<float>(double v) { return (float)v; }
+template <> __device__ __forceinline__ __nv_bfloat16 cvt<__nv_bfloat16>(double v) { return __double2bfloat16(v); }
+
+template <typename T>
+__global__ void store_convert_kernel(const double* __restrict__ src, int nleaf, const int64_t* src_off,
+                                     const int64_t* dst_off, const int32_t* kind, const int32_t* rows,
+                                     const int32_t* cols, const int32_t* kts, T* dst) {
+  for (int lf = blockIdx.x; lf < nleaf; lf += gridDim.x) {
+    const double* s = src + src_off[lf];
+    T* d = dst + dst_off[lf];
+    const int ndl = rows[lf], ndt = cols[lf];
+    if (kind[lf] == 1) {
+      const int64_t ne = (int64_t)kts[lf] * (ndl + ndt);
+      for (int64_t e = threadIdx.x; e < ne; e += blockDim.x) d[e] = cvt<T>(s[e]);
+    } else {
+      const int64_t ne = (int64_t)ndl * ndt;
+      for (int64_t e = threadIdx.x; e < ne; e += blockDim.x) {
+        const int il = (int)(e % ndl), it = (int)(e / ndl);  // dst (il,it), column-major
+        d[e] = cvt<T>(s[(int64_t)il * ndt + it]);
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------- launchers
+static int p1_blocks(int sm, int nitems) {
+  int b = sm * 8;
+  int need = (nitems + 7) / 8;
+  return need < b ? (need > 0 ? need : 1) : b;
+}
+
+template <typename T>
+static void p1_launch_t(const MatDev& m, const double* x, int sm, cudaStream_t st) {
+  if (m.np1 == 0) return;
+  p1_kernel<T, 8><<<p1_blocks(sm, m.np1), 256, 0, st>>>(m, x);
+}
+
+void launch_phase1(const MatDev* mats, int nmat, const double* x, int sm, cudaStream_t st) {
+  for (int i = 0; i < nmat; i++) {
+    if (mats[i].storage == ST_F64) p1_launch_t<double>(mats[i], x, sm, st);
+    else if (mats[i].storage == ST_F32) p1_launch_t<float>(mats[i], x, sm, st);
+    else p1_launch_t<__nv_bfloat16>(mats[i], x, sm, st);
+  }
+}
+
+void launch_phase2_plain(const MatDev* mats, int nmat, const ChainDev& ch, const double* x, double* const* y,
+                         cudaStream_t st) {
+  const int blocks = (ch.n + 127) / 128;
+  const MatDev& m1 = nmat == 2 ? mats[1] : mats[0];
+  double* y1 = nmat == 2 ? y[1] : nullptr;
+  if (mats[0].storage == ST_F64) p2_plain_kernel<double><<<blocks, 128, 0, st>>>(mats[0], m1, nmat, ch, x, y[0], y1);
+  else if (mats[0].storage == ST_F32) p2_plain_kernel<float><<<blocks, 128, 0, st>>>(mats[0], m1, nmat, ch, x, y[0], y1);
+  else p2_plain_kernel<__nv_bfloat16><<<blocks, 128, 0, st>>>(mats[0], m1, nmat, ch, x, y[0], y1);
+}
+
+void launch_phase2_rk(const MatDev* mats, int nmat, const ChainDev& ch, const double* x, const RkDev& rk, int stage,
+                      double* xnext, cudaStream_t st) {
+  const int blocks = (ch.n + 127) / 128;
+  const MatDev& m1 = nmat == 2 ? mats[1] : mats[0];
+  if (mats[0].storage == ST_F64) p2_rk_kernel<double><<<blocks, 128, 0, st>>>(mats[0], m1, ch, x, rk, stage, xnext);
+  else if (mats[0].storage == ST_F32) p2_rk_kernel<float><<<blocks, 128, 0, st>>>(mats[0], m1, ch, x, rk, stage, xnext);
+  else p2_rk_kernel<__nv_bfloat16><<<blocks, 128, 0, st>>>(mats[0], m1, ch, x, rk, stage, xnext);
+}
+
+void launch_rk_prepare(const RkDev& rk, cudaStream_t st) {
+  rk_prepare_kernel<<<(rk.n + 255) / 256, 256, 0, st>>>(rk);
+}
+
+void launch_store_convert(const double* src, const LeafDescDev*, int nleaf, const int64_t* src_off,
+                          const int64_t* dst_off, const int32_t* kind, const int32_t* rows, const int32_t* cols,
+                          const int32_t* kts, void* dst, int storage, cudaStream_t st) {
+  int blocks = nleaf < 152 * 16 ? (nleaf > 0 ? nleaf : 1) : 152 * 16;
+  if (storage == ST_F64)
+    store_convert_kernel<double><<<blocks, 256, 0, st>>>(src, nleaf, src_off, dst_off, kind, rows, cols, kts, (double*)dst);
+  else if (storage == ST_F32)
+    store_convert_kernel<float><<<blocks, 256, 0, st>>>(src, nleaf, src_off, dst_off, kind, rows, cols, kts, (float*)dst);
+  else
+    store_convert_kernel<__nv_bfloat16><<<blocks, 256, 0, st>>>(src, nleaf, src_off, dst_off, kind, rows, cols, kts,
+                                                                (__nv_bfloat16*)dst);
+}
+
+}  // namespace hbi

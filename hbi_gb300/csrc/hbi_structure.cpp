@@ -1,0 +1,293 @@
+// hbi_structure.cpp -- cluster tree, admissibility and leaf list (bit-exact
+// with HACApK on one rank) and the matvec work plans built from them.
+#include "hbi_structure.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace hbi {
+
+void default_params(double* p) {
+  // HACApK_init defaults (m_HACApK_base.f90:271-302) on one rank; the
+  // reference writes 1.0e-6 and 1.0 as default-real literals, widened here
+  // the same way.
+  for (int i = 0; i < 100; i++) p[i] = 0.0;
+  p[0] = 1; p[7] = 20; p[8] = 1; p[9] = 1;
+  p[20] = 15; p[21] = 1.0f;
+  p[42] = 1;  // param(43)=1 when nrank==1
+  p[50] = 2.0f; p[51] = 1; p[52] = 100;
+  p[59] = 2; p[60] = 3; p[61] = 7; p[62] = 1000; p[63] = 1;
+  p[71] = (double)1.0e-6f;
+  p[82] = 10; p[84] = 1; p[86] = 8; p[90] = (double)1.0e-6f; p[97] = 50; p[98] = 10;
+}
+
+namespace {
+
+struct Coord {
+  const double* g;
+  int n;
+  double at(int id1, int dim) const { return g[(size_t)dim * n + (size_t)(id1 - 1)]; }
+};
+
+// squared box distance of the admissibility tests; `tweak` reproduces the
+// 1e-16 offset HACApK applies at the lattice-block level (:2397-2401)
+double box_dist2(const Cluster& a, const Cluster& b, bool tweak) {
+  double zs = 0.0;
+  if (tweak)
+    for (int d = 0; d < 3; d++) {
+      if (a.bmax[d] != b.bmax[d]) zs = 1.0e-16;
+      if (a.bmin[d] != b.bmin[d]) zs = 1.0e-16;
+    }
+  for (int d = 0; d < 3; d++) {
+    if (a.bmax[d] < b.bmin[d]) zs = zs + (b.bmin[d] - a.bmax[d]) * (b.bmin[d] - a.bmax[d]);
+    else if (b.bmax[d] < a.bmin[d]) zs = zs + (a.bmin[d] - b.bmax[d]) * (a.bmin[d] - b.bmax[d]);
+  }
+  return zs;
+}
+
+}  // namespace
+
+int build_structure(int n, const double* coord, const double* param_in, Structure& s) {
+  if (n < 1 || !coord) return -1;
+  double pdef[100];
+  const double* param = param_in;
+  if (!param) { default_params(pdef); param = pdef; }
+  Coord G{coord, n};
+  s.n = n;
+  s.lod.resize(n);
+  for (int i = 0; i < n; i++) s.lod[i] = i + 1;
+  s.clusters.clear();
+  s.clusters.reserve(2 * (size_t)n / std::max(1, (int)param[20]) + 8);
+  const int minsz = (int)param[20];
+  int* lod = s.lod.data();
+
+  // ---- cluster tree: bisection of the longest box axis at its midpoint ----
+  struct Task { int id, lo, nsrt, nd; };
+  std::vector<Task> stack;
+  s.clusters.emplace_back();
+  stack.push_back({0, 0, 1, n});
+  while (!stack.empty()) {
+    Task t = stack.back();
+    stack.pop_back();
+    s.clusters[t.id].nstrt = t.nsrt;
+    s.clusters[t.id].nsize = t.nd;
+    if (t.nd <= minsz) { s.clusters[t.id].nnson = 0; continue; }
+    int* L = lod + t.lo;
+    double zlmin[3], zlmax[3];
+    for (int d = 0; d < 3; d++) {
+      zlmin[d] = zlmax[d] = G.at(L[0], d);
+      for (int il = 1; il < t.nd; il++) {
+        double zg = G.at(L[il], d);
+        if (zg < zlmin[d]) zlmin[d] = zg;
+        else if (zlmax[d] < zg) zlmax[d] = zg;
+      }
+    }
+    double zdiff = zlmax[0] - zlmin[0];
+    int ncut = 0;
+    for (int d = 0; d < 3; d++) {
+      double zi = zlmax[d] - zlmin[d];
+      if (zi > zdiff) { zdiff = zi; ncut = d; }
+    }
+    const double zlmid = (zlmax[ncut] + zlmin[ncut]) / 2;
+    // in-place two-sided partition with the reference's stopping rules
+    int nl = 1, nr = t.nd;
+    while (nl < nr) {
+      while (nl < t.nd && G.at(L[nl - 1], ncut) <= zlmid) nl++;
+      while (nr >= 1 && G.at(L[nr - 1], ncut) > zlmid) nr--;
+      if (nl < nr) std::swap(L[nl - 1], L[nr - 1]);
+    }
+    int a = (int)s.clusters.size();
+    s.clusters.emplace_back();
+    s.clusters.emplace_back();
+    Cluster& c = s.clusters[t.id];
+    c.nnson = 2; c.son[0] = a; c.son[1] = a + 1;
+    stack.push_back({a + 1, t.lo + nl - 1, t.nsrt + nl - 1, t.nd - nl + 1});
+    stack.push_back({a, t.lo, t.nsrt, nl - 1});
+  }
+
+  // ---- bounding boxes, children before parents (sons have larger ids) ----
+  for (int id = (int)s.clusters.size() - 1; id >= 0; id--) {
+    Cluster& c = s.clusters[id];
+    if (c.nnson == 0) {
+      const int* L = lod + (c.nstrt - 1);
+      for (int d = 0; d < 3; d++) c.bmin[d] = c.bmax[d] = G.at(L[0], d);
+      for (int d = 0; d < 3; d++)
+        for (int il = 1; il < c.nsize; il++) {
+          double v = G.at(L[il], d);
+          if (v < c.bmin[d]) c.bmin[d] = v;
+          if (c.bmax[d] < v) c.bmax[d] = v;
+        }
+    } else {
+      const Cluster& s0 = s.clusters[c.son[0]];
+      for (int d = 0; d < 3; d++) { c.bmin[d] = s0.bmin[d]; c.bmax[d] = s0.bmax[d]; }
+      for (int k = 1; k < c.nnson; k++) {
+        const Cluster& sk = s.clusters[c.son[k]];
+        for (int d = 0; d < 3; d++) {
+          if (sk.bmin[d] < c.bmin[d]) c.bmin[d] = sk.bmin[d];
+          if (c.bmax[d] < sk.bmax[d]) c.bmax[d] = sk.bmax[d];
+        }
+      }
+    }
+    double w = (c.bmax[0] - c.bmin[0]) * (c.bmax[0] - c.bmin[0]);
+    for (int d = 1; d < 3; d++) w = w + (c.bmax[d] - c.bmin[d]) * (c.bmax[d] - c.bmin[d]);
+    c.zwdth = std::sqrt(w);
+  }
+
+  // ---- block cluster tree -> leaves ----
+  const int nleaf = (int)(param[20] + 1);
+  const int nlmax = (int)(param[21] * n);
+  const int mdpth = (int)param[52];
+  const int p52 = (int)param[51];
+  const double zeta = param[50];
+  const int nlttcblk = (int)((double)n / param[42] / 1.0 + 1);
+  s.leaves.clear();
+  auto push = [&](int lt, const Cluster& cl, const Cluster& ct) {
+    s.leaves.push_back(Leaf{lt, 0, cl.nstrt, cl.nsize, ct.nstrt, ct.nsize});
+  };
+  const Cluster& r = s.clusters[0];
+  if (r.nsize < nlttcblk) {
+    // the one lattice block (HACApK_generate_blrleaf :2396-2450)
+    double zd = std::sqrt(box_dist2(r, r, true));
+    if (r.zwdth <= zeta * zd) {
+      push(1, r, r);
+    } else if (1 == mdpth || r.nnson == 0 || (r.nsize <= nleaf && r.nsize <= nleaf)) {
+      push(2, r, r);
+    } else {
+      struct Pair { int l, t, depth; };
+      std::vector<Pair> st;
+      for (int a = r.nnson - 1; a >= 0; a--)
+        for (int b = r.nnson - 1; b >= 0; b--) st.push_back({r.son[a], r.son[b], 1});
+      while (!st.empty()) {
+        Pair p = st.back();
+        st.pop_back();
+        const Cluster& cl = s.clusters[p.l];
+        const Cluster& ct = s.clusters[p.t];
+        int depth = p.depth + 1;
+        int ndl = cl.nsize, ndt = ct.nsize;
+        double zd = std::sqrt(box_dist2(cl, ct, false));
+        if ((cl.zwdth <= zeta * zd || ct.zwdth <= zeta * zd) &&
+            (ndl >= nleaf && ndt >= nleaf && ndl <= nlmax && ndt <= nlmax)) {
+          if (p52 == 0 || (p52 == 1 && ((cl.nstrt + ndl) != ct.nstrt && (ct.nstrt + ndt) != cl.nstrt))) {
+            push(1, cl, ct);
+            continue;
+          }
+        }
+        if (depth == mdpth || cl.nnson == 0 || ct.nnson == 0 || ndl <= nleaf || ndt <= nleaf) {
+          push(2, cl, ct);
+          continue;
+        }
+        for (int a = cl.nnson - 1; a >= 0; a--)
+          for (int b = ct.nnson - 1; b >= 0; b--) st.push_back({cl.son[a], ct.son[b], depth});
+      }
+    }
+  }
+  // (nstrtl, nstrtt) is unique per leaf, so any correct sort gives HACApK's order
+  std::sort(s.leaves.begin(), s.leaves.end(), [](const Leaf& a, const Leaf& b) {
+    return a.nstrtl != b.nstrtl ? a.nstrtl < b.nstrtl : a.nstrtt < b.nstrtt;
+  });
+  s.fine_start.clear();
+  for (auto& c : s.clusters)
+    if (c.nnson == 0) s.fine_start.push_back(c.nstrt);
+  std::sort(s.fine_start.begin(), s.fine_start.end());
+  return 0;
+}
+
+static int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
+
+void plan_matrix(const std::vector<Leaf>& leaves, int align, int chunk_rows, int kgroup, MatPlan& mp) {
+  const int nl = (int)leaves.size();
+  mp.leaf_off.assign(nl, 0);
+  mp.p1.clear(); mp.lr_leaf.clear(); mp.lr_zoff.clear(); mp.lr_nparts.clear(); mp.lr_poff.clear();
+  mp.desc.assign(nl, LeafDesc{});
+  int64_t off = 0, z = 0, pz = 0, fe = 0;
+  for (int i = 0; i < nl; i++) {
+    const Leaf& L = leaves[i];
+    off = round_up(off, align);
+    mp.leaf_off[i] = off;
+    LeafDesc& d = mp.desc[i];
+    d.row0 = L.nstrtl - 1;
+    d.ndl = L.ndl;
+    d.kind = L.ltmtx;
+    if (L.ltmtx == 1) {
+      int lr = (int)mp.lr_leaf.size();
+      int nparts = (L.ndt + chunk_rows - 1) / chunk_rows;
+      mp.lr_leaf.push_back(i);
+      mp.lr_nparts.push_back(nparts);
+      mp.lr_zoff.push_back((int32_t)z);
+      mp.lr_poff.push_back((int32_t)pz);
+      for (int p = 0; p < nparts; p++) {
+        int t0 = p * chunk_rows;
+        int nt = std::min(chunk_rows, L.ndt - t0);
+        for (int k0 = 0; k0 < L.kt; k0 += kgroup) {
+          P1Item it;
+          it.voff = off + (int64_t)k0 * L.ndt + t0;
+          it.ldv = L.ndt;
+          it.nt = nt;
+          it.x0 = L.nstrtt - 1 + t0;
+          it.k0 = k0;
+          it.nk = std::min(kgroup, L.kt - k0);
+          it.leaf = lr;
+          it.part = p;
+          mp.p1.push_back(it);
+        }
+      }
+      d.off = off + (int64_t)L.ndt * L.kt;  // U block follows V
+      d.kt_or_ndt = L.kt;
+      d.aux = (int32_t)z;
+      z += L.kt;
+      pz += (int64_t)L.kt * nparts;
+      off += (int64_t)L.kt * (L.ndl + L.ndt);
+      fe += (int64_t)L.kt * (L.ndl + L.ndt);
+    } else {
+      d.off = off;
+      d.kt_or_ndt = L.ndt;
+      d.aux = L.nstrtt - 1;
+      off += (int64_t)L.ndl * L.ndt;
+      fe += (int64_t)L.ndl * L.ndt;
+    }
+  }
+  mp.store_elems = round_up(off, align);
+  mp.zlen = z;
+  mp.plen = pz;
+  mp.factor_elems = fe;
+  // big items first so the static warp schedule ends evenly
+  std::stable_sort(mp.p1.begin(), mp.p1.end(), [](const P1Item& a, const P1Item& b) {
+    return (int64_t)a.nt * a.nk > (int64_t)b.nt * b.nk;
+  });
+}
+
+void plan_chains(int n, const std::vector<Leaf>& leaves, ChainPlan& cp) {
+  std::vector<int> bnd;
+  bnd.reserve(2 * leaves.size() + 2);
+  bnd.push_back(0);
+  bnd.push_back(n);
+  for (const Leaf& L : leaves) {
+    bnd.push_back(L.nstrtl - 1);
+    bnd.push_back(L.nstrtl - 1 + L.ndl);
+  }
+  std::sort(bnd.begin(), bnd.end());
+  bnd.erase(std::unique(bnd.begin(), bnd.end()), bnd.end());
+  const int nf = (int)bnd.size() - 1;
+  cp.row_fc.assign(n, 0);
+  for (int f = 0; f < nf; f++)
+    for (int r = bnd[f]; r < bnd[f + 1]; r++) cp.row_fc[r] = f;
+  std::vector<int> cnt(nf + 1, 0);
+  for (const Leaf& L : leaves) {
+    int f0 = cp.row_fc[L.nstrtl - 1];
+    int f1 = cp.row_fc[L.nstrtl - 1 + L.ndl - 1];
+    for (int f = f0; f <= f1; f++) cnt[f + 1]++;
+  }
+  cp.chain_ptr.assign(nf + 1, 0);
+  for (int f = 0; f < nf; f++) cp.chain_ptr[f + 1] = cp.chain_ptr[f] + cnt[f + 1];
+  cp.chain_leaf.assign(cp.chain_ptr[nf], 0);
+  std::vector<int> fill(cp.chain_ptr.begin(), cp.chain_ptr.end() - 1);
+  for (int i = 0; i < (int)leaves.size(); i++) {
+    const Leaf& L = leaves[i];
+    int f0 = cp.row_fc[L.nstrtl - 1];
+    int f1 = cp.row_fc[L.nstrtl - 1 + L.ndl - 1];
+    for (int f = f0; f <= f1; f++) cp.chain_leaf[fill[f]++] = i;
+  }
+}
+
+}  // namespace hbi

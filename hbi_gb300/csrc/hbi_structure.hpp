@@ -1,0 +1,85 @@
+// hbi_structure.hpp -- host-side H-matrix structure: cluster tree, leaf list
+// and the device work plans derived from it.
+//
+// The tree and the leaf list must be bit-identical to HACApK's one-rank
+// lattice H-matrix (m_HACApK_base.f90:3191-3333 tree and boxes, :2372-2460 and
+// :2937-2995 admissibility, :3114-3166 leaf order).  The construction here is
+// iterative (explicit stacks, node arrays) rather than recursive, but every
+// arithmetic step that decides a split or an admissibility is the reference's.
+#pragma once
+#include <cstdint>
+#include <vector>
+
+namespace hbi {
+
+struct Cluster {
+  int nstrt = 0, nsize = 0, nnson = 0, son[2] = {-1, -1};
+  double bmin[3] = {0, 0, 0}, bmax[3] = {0, 0, 0}, zwdth = 0;
+};
+
+// HACApK leaf record (st_HACApK_leafmtx, m_HACApK_base.f90:57-72); 1-based starts
+struct Leaf {
+  int ltmtx, kt, nstrtl, ndl, nstrtt, ndt;
+};
+
+struct Structure {
+  int n = 0;
+  std::vector<int> lod;          // lod(1:n), 1-based element ids in cluster order
+  std::vector<Cluster> clusters; // node 0 is the root
+  std::vector<Leaf> leaves;      // sorted by (nstrtl, nstrtt)
+  std::vector<int> fine_start;   // start rows (1-based) of the finest row ranges
+};
+
+void default_params(double* p100);
+// coord: coord(n,3) column-major as the reference passes it.
+int build_structure(int n, const double* coord, const double* param, Structure& s);
+
+// ---- matvec plans -------------------------------------------------------
+// Phase 1 (z = V^T x for every low-rank leaf) items and phase 2 (y = U z + A x,
+// one thread per row walking the leaves that cover the row) chains.
+struct P1Item {            // one warp task
+  int64_t voff;            // element offset of V(t0, k0) in the factor store
+  int32_t ldv;             // leading dimension of V (ndt)
+  int32_t nt;              // rows in this chunk
+  int32_t x0;              // 0-based column of x for row t0
+  int32_t k0, nk;          // column range of V
+  int32_t leaf;            // low-rank leaf index (dense-order in lr table)
+  int32_t part;            // 0-based chunk number inside the leaf
+};
+
+struct LeafDesc {          // per leaf, device table (phase 2)
+  int64_t off;             // element offset of U (low rank) or A (dense), column-major ld = ndl
+  int32_t row0;            // 0-based first row
+  int32_t ndl;
+  int32_t kind;            // 1 low rank, 2 dense
+  int32_t kt_or_ndt;       // kt (low rank) or ndt (dense)
+  int32_t aux;             // low rank: z offset; dense: 0-based first column
+  int32_t pad;
+};
+
+struct MatPlan {
+  std::vector<int64_t> leaf_off;     // factor-store offset of each leaf's block
+  int64_t store_elems = 0;           // factor store length (elements)
+  std::vector<P1Item> p1;            // phase-1 items
+  std::vector<int32_t> lr_leaf;      // leaf id of each low-rank leaf
+  std::vector<int32_t> lr_zoff;      // z offset of each low-rank leaf
+  std::vector<int32_t> lr_nparts;    // chunks of each low-rank leaf
+  std::vector<int32_t> lr_poff;      // partial-sum offset of each low-rank leaf
+  int64_t zlen = 0, plen = 0;
+  std::vector<LeafDesc> desc;        // per leaf
+  double alg_bytes_per_elem = 0;     // set by caller
+  int64_t factor_elems = 0;          // sum kt(ndl+ndt) + sum ndl*ndt
+};
+
+struct ChainPlan {                   // shared by matrices with the same leaf list
+  std::vector<int32_t> row_fc;       // 0-based row -> fine range id
+  std::vector<int32_t> chain_ptr;    // fine range -> [ptr, ptr+1) in chain_leaf
+  std::vector<int32_t> chain_leaf;   // leaf ids covering the range, coarse-to-fine order
+};
+
+// align: element alignment of each leaf block in the factor store
+void plan_matrix(const std::vector<Leaf>& leaves, int align, int p1_chunk_rows, int p1_kgroup,
+                 MatPlan& mp);
+void plan_chains(int n, const std::vector<Leaf>& leaves, ChainPlan& cp);
+
+}  // namespace hbi

@@ -1,0 +1,162 @@
+/*
+ * hbi_gpu.h -- C ABI of the GB300 implementation of HBI's per-step hot path.
+ *
+ * Each entry point replaces one HACApK / HBI routine that the Fortran driver
+ * (main_LH.f90) calls; the comment on each names the reference routine by
+ * file:line.  All functions return 0 (HBI_OK) or a negative HBI_ERR_* code and
+ * never abort; hbi_last_error() returns a message for the calling thread.
+ * Arrays are plain C arrays; "cluster order" means the lattice-vector order of
+ * HACApK (element lodc(i) of the global numbering sits at position i), which
+ * is the order every state array of the reference driver lives in.
+ * Integer element ids that the reference keeps 1-based (lod, lodc, leaf starts)
+ * stay 1-based.
+ *
+ * Threading: a handle is used by one host thread at a time.  Every handle
+ * owns its device memory and issues work on its own CUDA stream; the *_dev
+ * variants take device pointers and a stream and do not synchronise.
+ */
+#ifndef HBI_GPU_H
+#define HBI_GPU_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HBI_OK 0
+#define HBI_ERR_ARG (-1)      /* invalid argument */
+#define HBI_ERR_CUDA (-2)     /* CUDA runtime error (see hbi_last_error) */
+#define HBI_ERR_NOMEM (-3)    /* device or host allocation failed */
+#define HBI_ERR_STATE (-4)    /* call out of order (e.g. construct before generate) */
+#define HBI_ERR_CONVERGE (-5) /* Runge-Kutta step size underflow (reference: stop) */
+#define HBI_ERR_LIMIT (-6)    /* a size limit of this entry point was exceeded */
+
+/* problem kinds: st_bemv%problem of m_HACApK_calc_entry_ij.f90:24-90 */
+#define HBI_2DVS 1 /* 2D antiplane, half space (matels2dpa_ij :685-695)   */
+#define HBI_3DPH 2 /* 3D rectangles, Okada half space (okada_ij :1065-1145) */
+#define HBI_3DNR 3 /* 3D rectangles, Okada full space                    */
+#define HBI_3DNT 4 /* 3D triangles, TDstressFS full space (matel3dn_ij :802-851) */
+
+/* factor storage of the matvec operator */
+#define HBI_STORE_F64 0
+#define HBI_STORE_F32 1
+#define HBI_STORE_BF16 2
+
+/* st_HACApK_calc_entry (m_HACApK_calc_entry_ij.f90:7-19): geometry in the
+ * global (input) numbering, all arrays of length nd; unused ones may be NULL. */
+typedef struct {
+  int problem;  /* HBI_2DVS .. HBI_3DNT */
+  int nd;
+  char v;       /* 's' shear or 'n' normal traction (st_bemv%v) */
+  char md;      /* 's' slip along rake (st_bemv%md); only 's' is supported */
+  const double *xcol, *ycol, *zcol;
+  const double *xel, *xer;                      /* 2dvs element ends */
+  const double *ang, *angd, *dsl, *dsd, *rake;  /* okada; rake also for 3dnt (radians) */
+  double w;                                     /* okada length scale (ds0) */
+  const double *xs1, *xs2, *xs3, *ys1, *ys2, *ys3, *zs1, *zs2, *zs3; /* triangles */
+  const double *ev11, *ev12, *ev13, *ev21, *ev22, *ev23, *ev31, *ev32, *ev33;
+} hbi_bemv;
+
+typedef struct hbi_ctl_s hbi_ctl;           /* st_HACApK_lcontrol */
+typedef struct hbi_leafmtxp_s hbi_leafmtxp; /* st_HACApK_leafmtxp (filled leaves) */
+typedef struct hbi_lhp_s hbi_lhp;           /* st_HACApK_LHp (lattice matvec operator) */
+typedef struct hbi_rk_s hbi_rk;             /* RK45 state of the derivs/rkck/rkqs loop */
+
+const char* hbi_last_error(void);
+int hbi_version(void);
+
+/* HACApK_init (m_HACApK_base.f90:246-345): control block with the default
+ * param(1:100) of a one-rank run (param(43)=1).  Binds the current device. */
+int hbi_init(int nd, hbi_ctl** ctl);
+/* HACApK_param_set (m_HACApK_base.f90:348-382): copies param(1:100) */
+int hbi_param_set(hbi_ctl* ctl, const double* param100);
+int hbi_param_get(const hbi_ctl* ctl, double* param100);
+/* HACApK_finalize (m_HACApK_base.f90:385-393) */
+int hbi_finalize(hbi_ctl* ctl);
+
+/* HACApK_generate (m_HACApK_use.f90:133-260): cluster tree, admissibility and
+ * leaf list (bit-exact with HACApK), then ACA+ for admissible leaves and the
+ * dense near field on the GPU in FP64.  coord is coord(nd,3) column-major;
+ * ztol is eps_h.  The tree is stored in ctl (st_ctl%lod). */
+int hbi_generate(hbi_leafmtxp** st_leafmtxp, const hbi_bemv* st_bemv, hbi_ctl* st_ctl,
+                 const double* coord, double ztol);
+/* The structure half of HACApK_generate, host only (no GPU needed): cluster
+ * tree, admissibility and sorted leaf list of generate_frame_blrleaf
+ * (m_HACApK_base.f90:649-951) for one rank.  param100 may be NULL (defaults).
+ * lod receives lod(1:nd); call with leaves6 == NULL to get *nleaf, then again
+ * with room for 6 * *nleaf ints (ltmtx, kt=0, nstrtl, ndl, nstrtt, ndt). */
+int hbi_cluster_structure(int nd, const double* coord, const double* param100, int* lod, int* nleaf,
+                          int* leaves6);
+/* HACApK_free_leafmtxp (m_HACApK_base.f90:3084) */
+int hbi_free_leafmtxp(hbi_leafmtxp* lf);
+
+/* HACApK_construct_LH (m_HACApK_use.f90:263-366) with HACApK_contiguous
+ * (m_HACApK_base.f90:3652-3740): packs the filled leaves into the matvec
+ * operator with the given factor storage (HBI_STORE_*).  The operator keeps
+ * no reference to lf, which may be freed afterwards. */
+int hbi_construct_lh(hbi_lhp** st_LHp, const hbi_leafmtxp* lf, hbi_ctl* st_ctl, int storage);
+int hbi_free_lh(hbi_lhp* lh);
+
+/* HACApK_gen_lattice_vector (m_HACApK_base.f90:3449-3500): ndc = NCELL and
+ * lodc(1:ndc) (1-based global ids of the cluster-ordered vector); lodc may be
+ * NULL to query ndc only. */
+int hbi_gen_lattice_vector(const hbi_ctl* st_ctl, int* ndc, int* lodc);
+
+/* HACApK_adot_lattice_hyp (m_HACApK_solve.f90:220-337): au = H u, host arrays
+ * of length ndc in cluster order.  wws (the reference's row scratch) is
+ * accepted for signature compatibility and may be NULL. */
+int hbi_adot_lattice_hyp(double* au, hbi_lhp* st_LHp, hbi_ctl* st_ctl, double* wws, const double* u);
+/* same product on device arrays, enqueued on `stream` (cudaStream_t, NULL =
+ * the handle's stream); no synchronisation */
+int hbi_adot_lattice_hyp_dev(double* d_au, hbi_lhp* st_LHp, const double* d_u, void* stream);
+
+/* HACApK_entry_ij (m_HACApK_calc_entry_ij.f90:24-90) evaluated on the GPU for
+ * n (i,j) pairs, 1-based global ids. */
+int hbi_entry_ij(const hbi_bemv* st_bemv, int n, const int* i, const int* j, double* out);
+
+/* ---- introspection (parity checks, the reference's own export points) ---- */
+/* st_ctl%lod(1:nd) after hbi_generate */
+int hbi_get_lod(const hbi_ctl* ctl, int* lod);
+/* number of leaves and max rank (st_leafmtxp%nlf, %ktmax) */
+int hbi_leaf_count(const hbi_leafmtxp* lf, int* nleaf, int* ktmax);
+/* leaf table, 6 ints per leaf: ltmtx, kt, nstrtl, ndl, nstrtt, ndt (sorted) */
+int hbi_get_leaves(const hbi_leafmtxp* lf, int* leaves6);
+/* FP64 factors in the reference's contiguous packing: body offsets
+ * (nleaf+1, elements) and the body itself (NULL to query offsets only) */
+int hbi_get_body(const hbi_leafmtxp* lf, int64_t* offsets, double* body);
+/* algorithmic bytes of one product (factor bytes + vector in/out) */
+int hbi_lh_info(const hbi_lhp* lh, int64_t* factor_elems, int64_t* store_bytes, double* alg_bytes);
+
+/* ---- rate-and-state RHS and Cash-Karp RK45 (main_LH.f90:2053-2554) ---- */
+typedef struct {
+  int ncell;        /* NCELL */
+  int evlaw;        /* 0 aging, 1 slip */
+  int backslip;     /* matvec input is V - vpl */
+  int limitsigma;
+  double vref, minsig, maxsig;
+  double scale_s, scale_n; /* multipliers of H_s u and H_n u (1/ds0 for 3dph/3dnr) */
+  /* per-element parameters in cluster order, length ncell */
+  const double *a, *b, *dc, *f0, *taudot, *sigdot, *vpl;
+} hbi_rsf_params;
+
+/* binds one (sigma constant) or two H-matrices; lh_n may be NULL */
+int hbi_rk_create(hbi_rk** rk, const hbi_rsf_params* p, hbi_lhp* lh_s, hbi_lhp* lh_n);
+int hbi_rk_free(hbi_rk* rk);
+/* y(3*ncell) interleaved [psi, tau, sigma] per element (main_LH.f90:1208-1215) */
+int hbi_rk_set_state(hbi_rk* rk, const double* y);
+int hbi_rk_get_state(hbi_rk* rk, double* y);
+/* derivs (main_LH.f90:2053-2163): dydx = f(y) */
+int hbi_derivs(hbi_rk* rk, const double* y, double* dydx);
+/* rkck (main_LH.f90:2472-2554) from the current state; yout/yerr may be NULL */
+int hbi_rkck(hbi_rk* rk, double h, double eps, double* yout, double* yerr, double* errmax);
+/* rkqs (main_LH.f90:2270-2370): one accepted step from the current state.
+ * On success the state advances by *hdid and *x is updated; returns
+ * HBI_ERR_CONVERGE when the step size underflows (the reference stops). */
+int hbi_rkqs(hbi_rk* rk, double* x, double htry, double eps, double dtmax, double* hdid,
+             double* hnext, double* errmax, int* nrjct);
+/* number of kernels the handle launches per RK attempt */
+int hbi_rk_launches_per_attempt(const hbi_rk* rk);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,254 @@
+"""GPU parity: every kernel on the hot path against the CPU oracle, through
+the C ABI (include/hbi_gpu.h).
+
+Tolerances:
+  * tree, admissibility, leaf order, lod: bit-exact;
+  * 2dvs entries: bit-exact (division/subtraction only, rounded as IEEE);
+  * Okada / triangular entries: |gpu - oracle| <= 1e-11 max|entry| (CUDA's
+    libm differs from the C library's in the last ulp);
+  * ACA+ factors: rank per leaf equal for >= 90% of admissible leaves, and
+    ||H_gpu - A||_F within 3x of the oracle's own ||H_oracle - A||_F (+eps);
+  * FP64 matvec: relative 1e-12 against the same factors multiplied on the CPU;
+  * FP32 factors: 1e-5, BF16 factors: 2e-2 relative to the FP64 product;
+  * RK stages (derivs, rkck) on identical factors: relative 1e-10.
+"""
+import numpy as np
+import pytest
+
+import hbi_gb300 as H
+from gpu_cases import case, oracle_geometry, product_geometry
+
+pytestmark = pytest.mark.gpu
+
+KINDS = ["2dvs", "3dph", "3dnr", "3dnt"]
+
+
+@pytest.fixture(scope="module")
+def built(oracle):
+    """Product and oracle H-matrices for each small case, shared by tests."""
+    cache = {}
+
+    def get(kind, v="s"):
+        key = (kind, v)
+        if key not in cache:
+            prob, n, g, w, eps = case(kind)
+            geo = product_geometry(prob, n, g, w, v)
+            ogeo = oracle_geometry(oracle, prob, n, g, w, v)
+            ctl = H.Ctl(n)
+            lf = H.LeafMtxp(ctl, geo, eps)
+            coord = np.stack([g["xcol"], g.get("ycol", np.zeros(n)), g.get("zcol", np.zeros(n))], 1)
+            lod_o, lv_o, _ = oracle.build_structure(coord)
+            p = oracle.default_params()
+            p[70] = eps
+            Ho = oracle.HMatrix(ogeo, lod_o, lv_o, p)
+            cache[key] = dict(n=n, ctl=ctl, lf=lf, geo=geo, ogeo=ogeo, Ho=Ho, lod=lod_o, eps=eps, prob=prob, g=g, w=w)
+        return cache[key]
+
+    return get
+
+
+@pytest.mark.parametrize("kind", KINDS)
+@pytest.mark.parametrize("v", ["s", "n"])
+def test_entries(oracle, built, kind, v):
+    if kind == "2dvs" and v == "n":
+        pytest.skip("2dvs has no normal component (sigma constant)")
+    B = built(kind, v)
+    n = B["n"]
+    rng = np.random.default_rng(7)
+    i = np.concatenate([np.arange(1, n + 1), rng.integers(1, n + 1, 3000)])
+    j = np.concatenate([np.arange(1, n + 1), rng.integers(1, n + 1, 3000)])
+    gpu = H.entry_ij(B["geo"], i, j)
+    ref = np.array([oracle.entry(B["ogeo"], a, b) for a, b in zip(i, j)])
+    assert np.all(np.isfinite(gpu))
+    if kind == "2dvs":
+        assert np.array_equal(gpu, ref)
+    else:
+        # scale: the shear self-interaction (normal entries of a planar fault
+        # in a full space vanish analytically and are pure round-off)
+        scale = max(np.max(np.abs(ref)), abs(oracle.entry(built(kind, "s")["ogeo"], 1, 1)))
+        assert np.max(np.abs(gpu - ref)) <= 1e-11 * scale
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_generate_structure_bitexact(built, kind):
+    B = built(kind)
+    lv = B["lf"].leaves()
+    lo = B["Ho"].leaves
+    assert np.array_equal(B["ctl"].lod(), B["lod"])
+    assert np.array_equal(lv[:, [0, 2, 3, 4, 5]], lo[:, [0, 2, 3, 4, 5]])
+    ndc, lodc = H.HACApK_gen_lattice_vector(B["ctl"])
+    assert ndc == B["n"] and np.array_equal(lodc, B["lod"])
+
+
+def dense_from_body(n, leaves, off, body):
+    A = np.zeros((n, n))
+    for ip, (lt, kt, r0, ndl, c0, ndt) in enumerate(leaves):
+        o = int(off[ip])
+        if lt == 1:
+            V = body[o:o + ndt * kt].reshape(kt, ndt).T
+            U = body[o + ndt * kt:o + (ndt + ndl) * kt].reshape(kt, ndl).T
+            A[r0 - 1:r0 - 1 + ndl, c0 - 1:c0 - 1 + ndt] = U @ V.T
+        else:
+            A[r0 - 1:r0 - 1 + ndl, c0 - 1:c0 - 1 + ndt] = body[o:o + ndl * ndt].reshape(ndl, ndt)
+    return A
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_aca_ranks_and_accuracy(oracle, built, kind):
+    B = built(kind)
+    lv = B["lf"].leaves()
+    lo = B["Ho"].leaves
+    lr = lv[:, 0] == 1
+    same = np.mean(lv[lr, 1] == lo[lr, 1])
+    assert same >= 0.9, same
+    if kind == "2dvs":
+        assert same == 1.0
+    off, body = B["lf"].body()
+    Ag = dense_from_body(B["n"], lv, off, body)
+    A = oracle.dense_matrix(B["ogeo"], B["lod"])
+    Ao = B["Ho"].to_dense()
+    ng = np.linalg.norm(Ag - A)
+    no = np.linalg.norm(Ao - A)
+    assert ng <= 3 * no + 1e-14 * np.linalg.norm(A), (ng, no)
+    # dense near-field blocks are exact entries
+    for ip in np.nonzero(lv[:, 0] == 2)[0][:50]:
+        lt, kt, r0, ndl, c0, ndt = lv[ip]
+        blk = body[off[ip]:off[ip] + ndl * ndt].reshape(ndl, ndt)
+        ref = A[r0 - 1:r0 - 1 + ndl, c0 - 1:c0 - 1 + ndt]
+        assert np.max(np.abs(blk - ref)) <= 1e-11 * max(np.max(np.abs(ref)), 1e-300)
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_matvec_fp64(oracle, built, kind):
+    B = built(kind)
+    lh = H.LHp(B["lf"], B["ctl"], "f64")
+    off, body = B["lf"].body()
+    Hg = oracle.HMatrix.from_body(B["n"], B["lf"].leaves(), off, body)
+    rng = np.random.default_rng(3)
+    for u in (np.ones(B["n"]), rng.standard_normal(B["n"])):
+        y = lh.matvec(u)
+        ref = Hg.matvec(u)
+        assert np.linalg.norm(y - ref) <= 1e-12 * np.linalg.norm(ref)
+        # and against the oracle's own assembly at the ACA tolerance
+        ro = B["Ho"].matvec(u)
+        assert np.linalg.norm(y - ro) <= 50 * B["eps"] * np.linalg.norm(ro) + 1e-12 * np.linalg.norm(ro)
+    # deterministic: bitwise identical on repeat
+    assert np.array_equal(lh.matvec(u), lh.matvec(u))
+
+
+@pytest.mark.parametrize("kind", ["2dvs", "3dph", "3dnt"])
+@pytest.mark.parametrize("store,tol", [("f32", 1e-5), ("bf16", 2e-2)])
+def test_matvec_mixed(built, kind, store, tol):
+    B = built(kind)
+    l64 = H.LHp(B["lf"], B["ctl"], "f64")
+    lm = H.LHp(B["lf"], B["ctl"], store)
+    u = np.random.default_rng(4).standard_normal(B["n"])
+    ref = l64.matvec(u)
+    y = lm.matvec(u)
+    assert np.linalg.norm(y - ref) <= tol * np.linalg.norm(ref)
+    info = lm.info()
+    assert info["store_bytes"] <= info["factor_elems"] * (4 if store == "f32" else 2) * 1.05 + 4096
+
+
+def _rsf_setup(B, oracle, two_mats, evlaw=0):
+    n = B["n"]
+    rng = np.random.default_rng(11)
+    a = np.full(n, 0.01)
+    b = np.where(np.arange(n) % 3 == 0, 0.015, 0.006)
+    dc = np.full(n, 0.01)
+    f0 = np.full(n, 0.6)
+    vpl = np.full(n, 1e-9)
+    vref = float(np.float32(1e-6))
+    sig = np.full(n, 50.0) + rng.uniform(-1, 1, n)
+    vel = 1e-9 * (1 + 0.1 * rng.uniform(-1, 1, n))
+    psi_ss = f0 - b * np.log(vel / vref)
+    tau = a * sig * np.arcsinh(vel / (2 * vref) * np.exp(psi_ss / a))
+    psi = a * np.log(2 * vref / vel * np.sinh(tau / sig / a))
+    y = np.empty(3 * n); y[0::3], y[1::3], y[2::3] = psi, tau, sig
+    return dict(a=a, b=b, dc=dc, f0=f0, vpl=vpl), y
+
+
+@pytest.mark.parametrize("kind", ["2dvs", "3dph", "3dnt"])
+def test_derivs_and_rkck(oracle, built, kind):
+    Bs = built(kind, "s")
+    two = kind != "2dvs"
+    Bn = built(kind, "n") if two else None
+    prm, y = _rsf_setup(Bs, oracle, two)
+    scale = 1.0 / Bs["w"] if kind == "3dph" else 1.0
+    lhs = H.LHp(Bs["lf"], Bs["ctl"], "f64")
+    lhn = H.LHp(Bn["lf"], Bn["ctl"], "f64") if two else None
+    evlaw = 1 if kind == "3dnt" else 0
+    rk = H.RK(lhs, lhn, evlaw=evlaw, scale=scale, **prm)
+    off, body = Bs["lf"].body()
+    Hs = oracle.HMatrix.from_body(Bs["n"], Bs["lf"].leaves(), off, body)
+    Hn = None
+    if two:
+        off, body = Bn["lf"].body()
+        Hn = oracle.HMatrix.from_body(Bn["n"], Bn["lf"].leaves(), off, body)
+    R = oracle.RSF(Bs["n"], Hs, Hn, evlaw=evlaw, divide_ds0=int(kind == "3dph"), ds0=Bs["w"] or 1.0,
+                   vplv=prm["vpl"], a=prm["a"], b=prm["b"], dc=prm["dc"], f0=prm["f0"])
+    d_g = rk.derivs(y)
+    d_o = R.derivs(y)
+    # dpsi/dt near steady state is the difference of two terms of size b V/dc;
+    # its error is measured against that size, not against the difference
+    vref = float(np.float32(1e-6))
+    V = 2 * vref * np.exp(-y[0::3] / prm["a"]) * np.sinh(y[1::3] / y[2::3] / prm["a"])
+    term = np.linalg.norm(prm["b"] * V / prm["dc"])
+    for c in range(3):
+        ref = d_o[c::3]
+        floor = 1e-12 * term if c == 0 else 0.0
+        assert np.linalg.norm(d_g[c::3] - ref) <= 1e-10 * np.linalg.norm(ref) + floor + 1e-300, c
+    rk.set_state(y)
+    h = 1e6
+    yo, ye, em = rk.rkck(h, 1e-4)
+    yo_o, ye_o = R.rkck(y, 0.0, h)
+    assert np.linalg.norm(yo - yo_o) <= 1e-12 * np.linalg.norm(yo_o)
+    assert np.linalg.norm(ye - ye_o) <= 1e-8 * np.linalg.norm(ye_o) + 1e-20
+    em_o = oracle.lib().orc_errmax(3 * Bs["n"], oracle._p(ye_o), oracle._p(yo_o), oracle.C.c_double(1e-4))
+    assert abs(em - em_o) <= 1e-8 * em_o
+
+
+def test_rkqs_trajectory(oracle, built):
+    """30 accepted steps of the 2dvs system: step sizes, rejections and state
+    follow the oracle's controller."""
+    B = built("2dvs")
+    prm, y = _rsf_setup(B, oracle, False)
+    lh = H.LHp(B["lf"], B["ctl"], "f64")
+    rk = H.RK(lh, None, **prm)
+    off, body = B["lf"].body()
+    Ho = oracle.HMatrix.from_body(B["n"], B["lf"].leaves(), off, body)
+    R = oracle.RSF(B["n"], Ho, vplv=prm["vpl"], a=prm["a"], b=prm["b"], dc=prm["dc"], f0=prm["f0"])
+    rk.set_state(y)
+    xg = xo = 0.0
+    hg = ho = 1.0
+    yo = y.copy()
+    for _ in range(30):
+        xg, hd_g, hg, em_g, nr_g = rk.rkqs(xg, hg, 1e-6)
+        rc, yo, xo, hd_o, ho, em_o, nr_o = R.rkqs(yo, xo, ho, 1e-6)
+        assert rc == 0 and nr_g == nr_o
+        assert abs(hd_g - hd_o) <= 1e-9 * hd_o
+    assert abs(xg - xo) <= 1e-9 * xo
+    yg = rk.get_state()
+    assert np.linalg.norm(yg - yo) <= 1e-9 * np.linalg.norm(yo)
+
+
+def test_rkqs_underflow_is_a_status_not_a_stop(built):
+    """The reference stops the program when the step size underflows; the C
+    ABI returns HBI_ERR_CONVERGE and the handle stays usable."""
+    B = built("2dvs")
+    n = B["n"]
+    lh = H.LHp(B["lf"], B["ctl"], "f64")
+    rk = H.RK(lh, None, a=0.01, b=0.005, dc=0.01, f0=0.6, vpl=1e-9)
+    vref = float(np.float32(1e-6))
+    # an exactly steady state: errmax = 0 <= tiny, so every attempt is rejected
+    a, b, f0, sig, v0 = 0.01, 0.005, 0.6, 50.0, 1e-9
+    psi = f0 - b * np.log(v0 / vref)
+    tau = a * sig * np.arcsinh(v0 / (2 * vref) * np.exp(psi / a))
+    y = np.tile([a * np.log(2 * vref / v0 * np.sinh(tau / sig / a)), tau, sig], n)
+    rk.set_state(y)
+    with pytest.raises(H.HBIError) as e:
+        rk.rkqs(0.0, 1.0, 1e-6)
+    assert getattr(e.value, "code", None) == H.HBI_ERR_CONVERGE
+    y[1::3] *= 1 + 1e-3 * np.sin(np.arange(n))
+    rk.set_state(y)
+    rk.rkqs(0.0, 1.0, 1e-6)

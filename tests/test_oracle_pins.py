@@ -1,0 +1,122 @@
+"""Pins of the CPU oracle against known answers that do not depend on it.
+
+The reference cannot be compiled here (Fortran + MPI, no compiler), so these
+are the oracle's anchors: two independent published formulations must agree
+(Okada's rectangle vs two Nikkhoo-Walter triangles; Okada's long vertical
+strike-slip fault vs the 2D antiplane closed form), plus algorithmic identities
+of ACA+ and of the matvec.
+"""
+import math
+
+import numpy as np
+import pytest
+
+MU = LAM = 32.04
+ALPHA = 2.0 / 3.0  # (lambda+mu)/(lambda+2mu) for nu = 0.25
+
+
+def okada_stress(O, x, y, z, d1, d2, dip=90.0, depth=5.0, al=(-1, 1), aw=(-0.5, 0.5), full=True):
+    u = O.okada(ALPHA, x, y, z, depth, dip, al[0], al[1], aw[0], aw[1], d1, d2, 0.0, fullspace=full)
+    uxx, uyx, uzx, uxy, uyy, uzy, uxz, uyz, uzz = u[3:]
+    exx, eyy, ezz = uxx, uyy, uzz
+    exy, eyz, ezx = .5 * (uxy + uyx), .5 * (uyz + uzy), .5 * (uzx + uxz)
+    tr = exx + eyy + ezz
+    return np.array([LAM * tr + 2 * MU * exx, LAM * tr + 2 * MU * eyy, LAM * tr + 2 * MU * ezz,
+                     2 * MU * exy, 2 * MU * ezx, 2 * MU * eyz])
+
+
+@pytest.mark.parametrize("pt", [(0.3, 0.7, -5.2), (2.5, -1.0, -3.0), (-0.4, 0.05, -4.9), (0.0, 3.0, -8.0)])
+@pytest.mark.parametrize("slip", [(1, 0), (0, 1)])
+def test_okada_equals_two_triangles(oracle, pt, slip):
+    """A uniform-slip rectangle equals the two triangles that tile it."""
+    A, B, C, D = (-1, 0, -5.5), (1, 0, -5.5), (1, 0, -4.5), (-1, 0, -4.5)
+    so = okada_stress(oracle, *pt, *slip)
+    st = (oracle.tdstressfs(*pt, A, B, C, slip[0], slip[1], 0, MU, LAM)
+          + oracle.tdstressfs(*pt, A, C, D, slip[0], slip[1], 0, MU, LAM))
+    assert np.max(np.abs(so - st)) <= 1e-12 * np.max(np.abs(so))
+
+
+def test_okada_long_fault_is_2d_antiplane(oracle):
+    """A very long vertical strike-slip rectangle in a half space reproduces the
+    2D antiplane half-space kernel of '2dvs' (matels2dpa_ij minus its image)."""
+    n, ds0 = 64, 0.5
+    xel, xer, xcol, _ = oracle.mesh_2dp(n, ds0)
+    g = oracle.Geometry(oracle.ORC_2DVS, n, "s", xcol=xcol, xel=xel, xer=xer)
+    L = 3.0e4  # long enough that the finite-length error (~L^-2) is below 1e-6, short enough for FP64
+    for (i, j) in [(10, 10), (10, 11), (3, 40), (50, 7), (1, 64)]:
+        e2d = oracle.entry(g, i, j)
+        # source: depth interval [xel_j, xer_j] on the plane y=0; receiver at depth xcol_i
+        w = xer[j - 1] - xel[j - 1]
+        u = oracle.okada(ALPHA, 0.0, 0.0, -xcol[i - 1], xer[j - 1], 90.0, -L, L, 0.0, w, 1.0, 0.0, 0.0,
+                         fullspace=False)
+        sxy = MU * (u[6] + u[4])  # 2 mu e_xy
+        # same magnitude; the 2D kernel's sign convention is opposite to Okada's disl1
+        assert abs(sxy / e2d + 1.0) <= 2e-6, (i, j, sxy, e2d)
+
+
+def test_tdstress_symmetry_and_decay(oracle):
+    """Stress from a triangle is symmetric under reflecting the receiver
+    through the triangle plane (normal-parallel shear flips) and decays as r^-3."""
+    P1, P2, P3 = (0, 0, -1), (1, 0, -1), (0, 0, 0)
+    far1 = oracle.tdstressfs(30, 20, -10, P1, P2, P3, 1, 0, 0, MU, LAM)
+    far2 = oracle.tdstressfs(60, 40, -20, P1, P2, P3, 1, 0, 0, MU, LAM)
+    ratio = np.max(np.abs(far1)) / np.max(np.abs(far2))
+    assert 7.5 < ratio < 8.5
+
+
+def test_aca_recovers_block_and_matvec(oracle):
+    """ACA+ with eps=1e-6 reproduces the dense 2dvs operator; H*1 matches A*1."""
+    n, ds0 = 512, 40.0 / 512
+    xel, xer, xcol, _ = oracle.mesh_2dp(n, ds0)
+    g = oracle.Geometry(oracle.ORC_2DVS, n, "s", xcol=xcol, xel=xel, xer=xer)
+    coord = np.stack([xcol, np.zeros(n), np.zeros(n)], 1)
+    lod, leaves, cnt = oracle.build_structure(coord)
+    assert cnt == len(leaves)
+    p = oracle.default_params()
+    p[70] = 1e-6
+    H = oracle.HMatrix(g, lod, leaves, p)
+    A = oracle.dense_matrix(g, lod)
+    assert np.linalg.norm(H.to_dense() - A) <= 1e-9 * np.linalg.norm(A)
+    u = np.ones(n)
+    assert np.linalg.norm(H.matvec(u) - A @ u) <= 1e-7 * np.linalg.norm(A @ u)
+    # the OpenMP matvec (reference thread ranges, atomic accumulation) agrees
+    assert np.allclose(H.matvec(u, nthreads=4), H.matvec(u), rtol=1e-13, atol=1e-13 * np.abs(H.matvec(u)).max())
+
+
+def test_single_precision_literals(oracle):
+    """Cash-Karp and rkqs constants carry the reference's default-real values."""
+    a, b, c, dc = oracle.cashkarp()
+    assert b[1] == float(np.float32(3.0) / np.float32(40.0))
+    assert c[0] == float(np.float32(37.0) / np.float32(378.0))
+    assert dc[5] == float(np.float32(512.0) / np.float32(1771.0)) - 0.25
+    k = oracle.rkqs_consts()
+    assert k[0] == float(np.float32(0.9)) and k[3] == float(np.float32(1e-20))
+    assert abs(sum(c) - 1.0) < 1e-7  # the fifth-order weights sum to one (to single precision)
+
+
+def test_rkqs_relaxes_to_steady_sliding(oracle):
+    """A velocity-strengthening fault loaded at the plate rate stays at V = vpl."""
+    n = 128
+    ds0 = 40.0 / n
+    xel, xer, xcol, _ = oracle.mesh_2dp(n, ds0)
+    g = oracle.Geometry(oracle.ORC_2DVS, n, "s", xcol=xcol, xel=xel, xer=xer)
+    coord = np.stack([xcol, np.zeros(n), np.zeros(n)], 1)
+    lod, leaves, _ = oracle.build_structure(coord)
+    p = oracle.default_params(); p[70] = 1e-6
+    H = oracle.HMatrix(g, lod, leaves, p)
+    a, b, f0, sig, v0 = 0.015, 0.010, 0.6, 50.0, 1e-9
+    vref = float(np.float32(1e-6))
+    psi = f0 - b * math.log(v0 / vref)
+    tau = a * sig * math.asinh(v0 / (2 * vref) * math.exp(psi / a))
+    y = np.tile([a * math.log(2 * vref / v0 * math.sinh(tau / sig / a)), tau, sig], n)
+    # perturb the state: an exactly steady state has errmax = 0 <= tiny, which
+    # the reference's controller rejects until the step underflows
+    y[1::3] *= 1.0 + 1e-3 * np.sin(np.arange(n))
+    R = oracle.RSF(n, H, a=np.full(n, a), b=np.full(n, b), dc=np.full(n, 0.01), f0=np.full(n, f0),
+                   vplv=np.full(n, v0))
+    x, h = 0.0, 1.0
+    for _ in range(60):
+        rc, y, x, hdid, h, em, nr = R.rkqs(y, x, h, 1e-6)
+        assert rc == 0
+    V = 2 * vref * np.exp(-y[0::3] / a) * np.sinh(y[1::3] / y[2::3] / a)
+    assert np.allclose(V, v0, rtol=1e-3), (x, V.min(), V.max())

@@ -1,0 +1,93 @@
+"""Bit-exact cluster tree, admissibility and leaf order: the product's host
+builder (hbi_cluster_structure in libhbigpu.so, no GPU needed) against the
+oracle restatement of HACApK (m_HACApK_base.f90:2372-2460, 2937-2995,
+3114-3166, 3191-3333)."""
+import numpy as np
+import pytest
+
+import hbi_gb300 as H
+from hbi_gb300 import mesh
+
+
+def _both(oracle, coord, param=None):
+    lod_o, lv_o, cnt = oracle.build_structure(coord, param)
+    lod_p, lv_p = H.cluster_structure(coord, param)
+    return lod_o, lv_o, cnt, lod_p, lv_p
+
+
+def _check(oracle, coord, param=None):
+    lod_o, lv_o, cnt, lod_p, lv_p = _both(oracle, coord, param)
+    assert np.array_equal(lod_o, lod_p)
+    assert np.array_equal(lv_o[:, [0, 2, 3, 4, 5]], lv_p[:, [0, 2, 3, 4, 5]])
+    assert cnt == len(lv_o)
+    n = len(coord)
+    # the leaves tile the matrix exactly once
+    area = (lv_p[:, 3].astype(np.int64) * lv_p[:, 5]).sum()
+    assert area == n * n
+    assert sorted(lod_p) == list(range(1, n + 1))
+    return lv_p
+
+
+@pytest.mark.parametrize("n", [1, 15, 16, 17, 100, 1024, 1600])
+def test_2dvs_structure(oracle, n):
+    xel, xer, xcol, _ = mesh.mesh_2dp(n, 40.0 / n)
+    _check(oracle, np.stack([xcol, np.zeros(n), np.zeros(n)], 1))
+
+
+@pytest.mark.parametrize("imax,jmax", [(16, 16), (64, 32), (150, 30)])
+def test_3dph_structure(oracle, imax, jmax):
+    xcol, ycol, zcol, angd, ang = mesh.mesh_3ddip(imax, jmax, 0.1, 30.0)
+    _check(oracle, np.stack([xcol, ycol, zcol], 1))
+
+
+def test_rough_triangle_structure(oracle):
+    tri = mesh.rough_fault(40, 20, 6.0, 3.0, seed=3)
+    g, _ = mesh.tri_geometry(tri)
+    _check(oracle, np.stack([g["xcol"], g["ycol"], g["zcol"]], 1))
+
+
+def test_degenerate_points(oracle):
+    """Coincident points and ties on the cut plane follow the reference loop."""
+    rng = np.random.default_rng(1)
+    c = np.round(rng.uniform(0, 4, (500, 3)))  # many exact ties
+    _check(oracle, c)
+    _check(oracle, np.zeros((40, 3)))
+
+
+def test_params_change_leaves(oracle):
+    xel, xer, xcol, _ = mesh.mesh_2dp(512, 0.1)
+    c = np.stack([xcol, np.zeros(512), np.zeros(512)], 1)
+    p = oracle.default_params()
+    p[20] = 7        # leaf size param(21)
+    p[50] = 1.0      # eta param(51)
+    lv = _check(oracle, c, p)
+    lv0 = _check(oracle, c)
+    assert len(lv) != len(lv0)
+
+
+def test_mesh_builders_match_oracle(oracle):
+    a = mesh.mesh_2dp(1000, 0.04)
+    b = oracle.mesh_2dp(1000, 0.04)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+    a = mesh.mesh_3ddip(20, 12, 0.2, 30.0)
+    b = oracle.mesh_3ddip(20, 12, 0.2, 30.0)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+    tri = mesh.rough_fault(10, 6, 3.0, 2.0, seed=0)
+    xs = [tri[:, k, 0] for k in range(3)] + [tri[:, k, 1] for k in range(3)] + [tri[:, k, 2] for k in range(3)]
+    ev_p = mesh.evcalc(*xs)
+    ev_o = oracle.evcalc(*xs)
+    for x, y in zip(ev_p, ev_o):
+        assert np.array_equal(x, y)
+
+
+def test_stl_roundtrip(tmp_path):
+    tri = mesh.rough_fault(5, 4, 2.0, 1.0, seed=2)
+    p = tmp_path / "f.stl"
+    mesh.write_stl(str(p), tri)
+    xs, ys, zs = mesh.read_stl(str(p))
+    assert xs.shape == (3, len(tri))
+    assert np.array_equal(xs[0], tri[:, 0, 0]) and np.array_equal(zs[2], tri[:, 2, 2])
+    # the reference counts facets as lines/7
+    assert len(open(p).read().splitlines()) // 7 == len(tri)

@@ -1,0 +1,361 @@
+#!/usr/bin/env python
+"""bench.py -- H-matvec GB/s inside Cash-Karp RK45 attempts of HBI's hot path.
+
+Workload (default): the 3D planar thrust fault of the second benchmark
+configuration -- a 30-degree dipping fault in a half space, Okada kernel,
+256 x 256 = 65,536 elements, two H-matrices (shear 's' and normal 'n'),
+velocity-weakening central patch, ACA eps 1e-5; seeded synthetic inputs.
+
+A step is one Cash-Karp attempt (rkck, main_LH.f90:2472-2554): six stages,
+each evaluating derivs (main_LH.f90:2053-2163) with one product per
+H-matrix, i.e. 12 lattice H-matrix-vector products plus the fused
+rate-and-state / stage epilogue.  value = 12 x (algorithmic bytes of one
+product) per second, the bytes being the stored factor bytes
+(sum_LR kt(ndl+ndt) + sum_dense ndl*ndt, times the storage size) plus the
+FP64 input and output vectors.  The factor stores (> 1 GB) exceed the 126 MB
+L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--store f32|bf16|f64]
+  python bench.py --impl reference ...   # the CPU oracle port, all host cores
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NSMI_Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+          "clocks_event_reasons.sw_power_cap")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--store", default="f32", choices=["f64", "f32", "bf16"])
+    ap.add_argument("--imax", type=int, default=256)
+    ap.add_argument("--jmax", type=int, default=256)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mode", default="step", choices=["step", "matvec"])
+    return ap.parse_args()
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={NSMI_Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+
+    def summary(self):
+        self.f.flush()
+        rows = [l.split(",") for l in open(self.f.name).read().splitlines() if l.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1])); mx = max(mx, float(r[2]))
+                for k, nm in enumerate(names):
+                    if r[5 + k].strip().lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                pass
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(args):
+    from hbi_gb300 import configs
+    return configs.c2_3dph(args.imax, args.jmax)
+
+
+def out_line(d):
+    print(json.dumps(d), flush=True)
+
+
+def time_phases(torch, lh, n, reps):
+    """Mean device time of the two product kernels, timed with CUDA events on
+    the (non-default) stream they are launched on."""
+    x = torch.randn(n, dtype=torch.float64, device="cuda")
+    y = torch.empty(n, dtype=torch.float64, device="cuda")
+    ts = torch.cuda.Stream()
+    for _ in range(3):
+        lh.matvec_dev(y.data_ptr(), x.data_ptr(), ts.cuda_stream)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3 * reps)]
+    torch.cuda.synchronize()
+    for r in range(reps):
+        ev[3 * r].record(ts)
+        lh.matvec_dev(y.data_ptr(), x.data_ptr(), ts.cuda_stream, phase=1)
+        ev[3 * r + 1].record(ts)
+        lh.matvec_dev(y.data_ptr(), x.data_ptr(), ts.cuda_stream, phase=2)
+        ev[3 * r + 2].record(ts)
+    torch.cuda.synchronize()
+    t1 = float(np.mean([ev[3 * r].elapsed_time(ev[3 * r + 1]) for r in range(reps)])) * 1e-3
+    t2 = float(np.mean([ev[3 * r + 1].elapsed_time(ev[3 * r + 2]) for r in range(reps)])) * 1e-3
+    b1, b2 = lh.phase_bytes()
+    return t1, t2, b1, b2
+
+
+def run_matvec_mode(args):
+    """Products only (no RK, no CPU baseline): the target of kernel profiles."""
+    import torch
+
+    import hbi_gb300 as H
+    w = workload(args)
+    n = w.nd
+    ctl = H.Ctl(n)
+    lf = H.LeafMtxp(ctl, w.geometry("s"), w.eps_h)
+    lh = H.LHp(lf, ctl, args.store)
+    t1, t2, b1, b2 = time_phases(torch, lh, n, args.steps)
+    out_line({"mode": "matvec", "elements": n, "storage": args.store, "phase1_us": round(t1 * 1e6, 2),
+              "phase2_us": round(t2 * 1e6, 2), "phase1_gbs": round(b1 / t1 / 1e9, 1),
+              "phase2_gbs": round(b2 / t2 / 1e9, 1), "both_gbs": round((b1 + b2) / (t1 + t2) / 1e9, 1),
+              "bytes": b1 + b2})
+
+
+# --------------------------------------------------------------------- ours
+def run_ours(args):
+    import torch
+
+    import hbi_gb300 as H
+
+    rank, world, local = dist_init(args)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    H.set_device(local)
+    w = workload(args)
+    n = w.nd
+    t0 = time.perf_counter()
+    ctl_s, ctl_n = H.Ctl(n), H.Ctl(n)
+    lf_s = H.LeafMtxp(ctl_s, w.geometry("s"), w.eps_h)
+    lf_n = H.LeafMtxp(ctl_n, w.geometry("n"), w.eps_h)
+    t_gen = time.perf_counter() - t0
+    lh_s = H.LHp(lf_s, ctl_s, args.store)
+    lh_n = H.LHp(lf_n, ctl_n, args.store)
+    ndc, lodc = H.HACApK_gen_lattice_vector(ctl_s)
+    y0, p = w.initial_state(lodc)
+    rk = H.RK(lh_s, lh_n, evlaw=w.evlaw, scale=w.scale, a=p["a"], b=p["b"], dc=p["dc"], f0=p["f0"], vpl=p["vpl"],
+              taudot=p["taudot"], sigdot=p["sigdot"])
+    rk.set_state(y0)
+    t_setup = time.perf_counter() - t0
+    info_s, info_n = lh_s.info(), lh_n.info()
+    bytes_attempt = 6.0 * (info_s["alg_bytes"] + info_n["alg_bytes"])
+    stream = torch.cuda.ExternalStream(rk.stream)
+    h, eps = 1.0e5, 1e-5
+
+    # ---- device-resident throughput: K back-to-back attempts ----
+    for _ in range(args.warmup):
+        rk.attempt_async(h, eps)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as ck:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            rk.attempt_async(h, eps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clocks = ck.summary()
+    if world > 1:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    ms_step = ms / args.steps
+    value = world * args.steps * bytes_attempt / (ms * 1e-3) / 1e9
+
+    # ---- roofline of the two matvec kernels (phase 1, phase 2) on lh_s ----
+    t1, t2, b1, b2 = time_phases(torch, lh_s, n, 20)
+    peak, peak_kind = peaks()
+    dominant = "phase2" if t2 >= t1 else "phase1"
+    ach = (b2 / t2 if dominant == "phase2" else b1 / t1) / 1e9
+    mv_gbs = (b1 + b2) / (t1 + t2) / 1e9
+
+    # ---- end to end through the C ABI with host buffers ----
+    yh = torch.empty(3 * n, dtype=torch.float64, pin_memory=True).numpy()
+    yh[:] = y0
+    yo = torch.empty(3 * n, dtype=torch.float64, pin_memory=True).numpy()
+    ye = torch.empty(3 * n, dtype=torch.float64, pin_memory=True).numpy()
+    for _ in range(2):
+        rk.set_state(yh)
+        rk.rkck_into(h, eps, yo, ye)
+    torch.cuda.synchronize()
+    te = time.perf_counter()
+    for _ in range(args.steps):
+        rk.set_state(yh)
+        rk.rkck_into(h, eps, yo, ye)
+    te = time.perf_counter() - te
+    if world > 1:
+        tt = torch.tensor([te], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        te = float(tt.item())
+    e2e = world * args.steps * bytes_attempt / te / 1e9
+
+    # ---- CPU baseline: the oracle port on the host cores (rank 0, N=1) ----
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args, w, lf_s, lf_n, y0, p, lodc)
+
+    if rank == 0:
+        d = {
+            "metric": "H-matvec GB/s", "value": round(value, 2), "unit": "GB/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.store,
+            "data": "synthetic (seeded 3D planar thrust, Okada half space)",
+            "config": {"workload": f"{w.name}: 3dph Okada half space, {n} elements, 2 H-matrices (s,n), "
+                                   f"ACA eps {w.eps_h}, one Cash-Karp attempt per step (12 products)",
+                       "elements": n, "storage": args.store, "products_per_step": 12,
+                       "l2": "inputs larger than L2 (factor stores %.2f GB)" % ((info_s["store_bytes"] + info_n["store_bytes"]) / 1e9),
+                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+            "roofline": {"bound": "hbm", "kernel": f"matvec {dominant}", "achieved": round(ach, 1),
+                         "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4), "peak_kind": peak_kind,
+                         "traffic": None, "matvec_gbs_both_phases": round(mv_gbs, 1),
+                         "phase1_us": round(t1 * 1e6, 2), "phase2_us": round(t2 * 1e6, 2),
+                         "phase1_bytes": b1, "phase2_bytes": b2},
+            "e2e": {"value": round(e2e, 2), "unit": "GB/s", "h2d_bytes_per_step": 3 * n * 8,
+                    "d2h_bytes_per_step": 2 * 3 * n * 8 + 32},
+            "gpu_launches": args.steps * rk.launches_per_attempt,
+            "clocks": clocks,
+            "setup": {"generate_s": round(t_gen, 2), "total_s": round(t_setup, 2),
+                      "factor_elems_s": info_s["factor_elems"], "factor_elems_n": info_n["factor_elems"],
+                      "compression_s": info_s["factor_elems"] / n / n},
+        }
+        if cpu:
+            d["cpu_baseline"] = cpu
+        out_line(d)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def cpu_baseline(args, w, lf_s, lf_n, y0, p, lodc):
+    """The oracle's RK attempt (OpenMP products mirroring the reference's
+    thread ranges and atomics) on the same FP64 factors, all host cores."""
+    from oracle import oracle as O
+    O.build()
+    n = w.nd
+    off, body = lf_s.body()
+    Hs = O.HMatrix.from_body(n, lf_s.leaves(), off, body)
+    off, body = lf_n.body()
+    Hn = O.HMatrix.from_body(n, lf_n.leaves(), off, body)
+    cores = os.cpu_count() or 1
+    R = O.RSF(n, Hs, Hn, evlaw=w.evlaw, divide_ds0=1, ds0=w.w, nthreads=cores, a=p["a"], b=p["b"], dc=p["dc"],
+              f0=p["f0"], vplv=p["vpl"], taudot=p["taudot"], sigdot=p["sigdot"])
+    R.rkck(y0, 0.0, 1e5)
+    t = time.perf_counter()
+    k = 0
+    while True:
+        R.rkck(y0, 0.0, 1e5)
+        k += 1
+        if time.perf_counter() - t > args.cpu_seconds or k >= 200:
+            break
+    t = time.perf_counter() - t
+    bytes_attempt = 6.0 * ((Hs.body.size + Hn.body.size) * 8 + 2 * 2 * n * 8)
+    return {"value": round(k * bytes_attempt / t / 1e9, 3), "unit": "GB/s", "cores": cores, "kind": "port",
+            "sample": f"{k} Cash-Karp attempts of the same workload on the same FP64 factors "
+                      f"({(Hs.body.size + Hn.body.size) * 8 / 1e9:.2f} GB), oracle rkck with OpenMP products",
+            "ms_per_step": round(t / k * 1e3, 2)}
+
+
+# ---------------------------------------------------------------- reference
+def run_reference(args):
+    rank, world, local = dist_init(args)
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    w = workload(args)
+    n = w.nd
+    cores = os.cpu_count() or 1
+    coord = np.stack([w.geom_kw["xcol"], w.geom_kw["ycol"], w.geom_kw["zcol"]], 1)
+    t0 = time.perf_counter()
+    lod, lv, _ = O.build_structure(coord)
+    p = O.default_params()
+    p[70] = w.eps_h
+    Hs = O.HMatrix(O.Geometry(2, n, "s", w=w.w, **w.geom_kw), lod, lv, p, nthreads=cores)
+    Hn = O.HMatrix(O.Geometry(2, n, "n", w=w.w, **w.geom_kw), lod, lv, p, nthreads=cores)
+    t_setup = time.perf_counter() - t0
+    y0, pp = w.initial_state(lod)
+    R = O.RSF(n, Hs, Hn, evlaw=w.evlaw, divide_ds0=1, ds0=w.w, nthreads=cores, a=pp["a"], b=pp["b"], dc=pp["dc"],
+              f0=pp["f0"], vplv=pp["vpl"], taudot=pp["taudot"], sigdot=pp["sigdot"])
+    for _ in range(args.warmup):
+        R.rkck(y0, 0.0, 1e5)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        R.rkck(y0, 0.0, 1e5)
+    t = time.perf_counter() - t
+    bytes_attempt = 6.0 * ((Hs.body.size + Hn.body.size) * 8 + 2 * 2 * n * 8)
+    v = args.steps * bytes_attempt / t / 1e9
+    out_line({
+        "impl": "reference", "metric": "H-matvec GB/s", "value": round(v, 3), "unit": "GB/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t / args.steps * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded 3D planar thrust, Okada half space)",
+        "config": {"workload": f"{w.name}: 3dph Okada half space, {n} elements, 2 H-matrices (s,n), "
+                               f"ACA eps {w.eps_h}, one Cash-Karp attempt per step (12 products)",
+                   "elements": n, "storage": "f64", "products_per_step": 12},
+        "cpu_baseline": {"value": round(v, 3), "unit": "GB/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} Cash-Karp attempts on the oracle's own ACA+ H-matrices "
+                                   f"(setup {t_setup:.1f} s), OpenMP products on all host cores"},
+        "e2e": {"value": round(v, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    })
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    elif args.mode == "matvec":
+        run_matvec_mode(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

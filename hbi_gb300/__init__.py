@@ -8,8 +8,10 @@ by hbi_gb300/_build.py; importing this module on a machine without it, or
 calling a compute entry point without a GPU, raises HBIError -- there is no
 CPU fallback.
 """
+import atexit
 import ctypes as C
 import os
+import weakref
 
 import numpy as np
 
@@ -32,8 +34,14 @@ EXPORTS = [
     "hbi_adot_lattice_hyp", "hbi_adot_lattice_hyp_dev", "hbi_entry_ij", "hbi_get_lod", "hbi_leaf_count",
     "hbi_get_leaves", "hbi_get_body", "hbi_lh_info", "hbi_rk_create", "hbi_rk_free", "hbi_rk_set_state",
     "hbi_rk_get_state", "hbi_derivs", "hbi_rkck", "hbi_rkqs", "hbi_rk_launches_per_attempt",
-    "hbi_cluster_structure",
+    "hbi_cluster_structure", "hbi_rk_stream", "hbi_rk_attempt_async", "hbi_set_device",
+    "hbi_adot_lattice_hyp_phase_dev", "hbi_lh_phase_bytes",
 ]
+
+
+def set_device(device):
+    """Bind subsequent handles of this thread to CUDA device `device`."""
+    _check(lib().hbi_set_device(int(device)), "hbi_set_device")
 
 
 class HBIError(RuntimeError):
@@ -57,6 +65,25 @@ class RsfParams(C.Structure):
 
 
 _lib = None
+_live = weakref.WeakValueDictionary()  # id -> handle owner, for ordered teardown at exit
+_closed = False
+
+
+def _register(obj, rank):
+    obj._rank = rank
+    _live[id(obj)] = obj
+
+
+@atexit.register
+def _teardown():
+    """Free live handles before the CUDA runtime goes away: RK states first,
+    then operators, filled H-matrices and control blocks."""
+    global _closed
+    for rank in (0, 1, 2, 3):
+        for obj in list(_live.values()):
+            if getattr(obj, "_rank", -1) == rank:
+                obj.close()
+    _closed = True
 
 
 def lib():
@@ -117,6 +144,7 @@ class Ctl:
         self.h = C.c_void_p()
         _check(lib().hbi_init(int(nd), C.byref(self.h)), "hbi_init")
         self.nd = nd
+        _register(self, 3)
 
     @property
     def param(self):
@@ -134,10 +162,13 @@ class Ctl:
         _check(lib().hbi_get_lod(self.h, a.ctypes.data_as(_ip)), "hbi_get_lod")
         return a
 
-    def __del__(self):
-        if getattr(self, "h", None) and _lib is not None:
+    def close(self):
+        if getattr(self, "h", None) and _lib is not None and not _closed:
             _lib.hbi_finalize(self.h)
-            self.h = None
+        self.h = None
+
+    def __del__(self):
+        self.close()
 
 
 class LeafMtxp:
@@ -148,6 +179,7 @@ class LeafMtxp:
         coord = geom.coord().ravel(order="F")
         _check(lib().hbi_generate(C.byref(self.h), C.byref(geom.bemv), ctl.h, _p(coord), C.c_double(ztol)),
                "hbi_generate")
+        _register(self, 2)
 
     def leaves(self):
         n, km = C.c_int(), C.c_int()
@@ -164,10 +196,13 @@ class LeafMtxp:
         _check(lib().hbi_get_body(self.h, off.ctypes.data_as(_i64p), _p(body)), "hbi_get_body")
         return off, body[:int(off[-1])]
 
-    def __del__(self):
-        if getattr(self, "h", None) and _lib is not None:
+    def close(self):
+        if getattr(self, "h", None) and _lib is not None and not _closed:
             _lib.hbi_free_leafmtxp(self.h)
-            self.h = None
+        self.h = None
+
+    def __del__(self):
+        self.close()
 
 
 class LHp:
@@ -179,6 +214,7 @@ class LHp:
         self.ctl, self.h, self.storage = ctl, C.c_void_p(), storage
         _check(lib().hbi_construct_lh(C.byref(self.h), lf.h, ctl.h, int(storage)), "hbi_construct_lh")
         self.n = ctl.nd
+        _register(self, 1)
 
     def matvec(self, u):
         """HACApK_adot_lattice_hyp: au = H u (cluster order, host arrays)."""
@@ -187,15 +223,28 @@ class LHp:
         _check(lib().hbi_adot_lattice_hyp(_p(au), self.h, self.ctl.h, None, _p(u)), "hbi_adot_lattice_hyp")
         return au
 
+    def matvec_dev(self, d_au, d_u, stream=0, phase=0):
+        """Product on device pointers (ints), enqueued on `stream`."""
+        _check(lib().hbi_adot_lattice_hyp_phase_dev(C.c_void_p(d_au), self.h, C.c_void_p(d_u), C.c_void_p(stream),
+                                                    int(phase)), "hbi_adot_lattice_hyp_phase_dev")
+
+    def phase_bytes(self):
+        p1, p2 = C.c_double(), C.c_double()
+        _check(lib().hbi_lh_phase_bytes(self.h, C.byref(p1), C.byref(p2)), "hbi_lh_phase_bytes")
+        return p1.value, p2.value
+
     def info(self):
         fe, sb, ab = C.c_int64(), C.c_int64(), C.c_double()
         _check(lib().hbi_lh_info(self.h, C.byref(fe), C.byref(sb), C.byref(ab)), "hbi_lh_info")
         return {"factor_elems": fe.value, "store_bytes": sb.value, "alg_bytes": ab.value}
 
-    def __del__(self):
-        if getattr(self, "h", None) and _lib is not None:
+    def close(self):
+        if getattr(self, "h", None) and _lib is not None and not _closed:
             _lib.hbi_free_lh(self.h)
-            self.h = None
+        self.h = None
+
+    def __del__(self):
+        self.close()
 
 
 # ---- HACApK-named functions (the drop-in surface) -----------------------
@@ -266,6 +315,7 @@ class RK:
         _check(lib().hbi_rk_create(C.byref(self.h), C.byref(p), lh_s.h, lh_n.h if lh_n is not None else None),
                "hbi_rk_create")
         self.n, self.lh = n, (lh_s, lh_n)
+        _register(self, 0)
 
     def set_state(self, y):
         y = np.ascontiguousarray(y, dtype=np.float64)
@@ -288,6 +338,12 @@ class RK:
         _check(lib().hbi_rkck(self.h, C.c_double(h), C.c_double(eps), _p(yo), _p(ye), C.byref(em)), "hbi_rkck")
         return yo, ye, em.value
 
+    def rkck_into(self, h, eps, yout, yerr):
+        """rkck writing into caller-provided (e.g. pinned) float64 arrays."""
+        em = C.c_double()
+        _check(lib().hbi_rkck(self.h, C.c_double(h), C.c_double(eps), _p(yout), _p(yerr), C.byref(em)), "hbi_rkck")
+        return em.value
+
     def rkqs(self, x, htry, eps, dtmax=1e10):
         xx, hd, hn, em, nr = C.c_double(x), C.c_double(), C.c_double(), C.c_double(), C.c_int()
         _check(lib().hbi_rkqs(self.h, C.byref(xx), C.c_double(htry), C.c_double(eps), C.c_double(dtmax),
@@ -298,7 +354,20 @@ class RK:
     def launches_per_attempt(self):
         return lib().hbi_rk_launches_per_attempt(self.h)
 
-    def __del__(self):
-        if getattr(self, "h", None) and _lib is not None:
+    @property
+    def stream(self):
+        """cudaStream_t (as int) the handle enqueues on."""
+        lib().hbi_rk_stream.restype = C.c_void_p
+        return lib().hbi_rk_stream(self.h) or 0
+
+    def attempt_async(self, h, eps):
+        """Enqueue one Cash-Karp attempt; no host synchronisation."""
+        _check(lib().hbi_rk_attempt_async(self.h, C.c_double(h), C.c_double(eps)), "hbi_rk_attempt_async")
+
+    def close(self):
+        if getattr(self, "h", None) and _lib is not None and not _closed:
             _lib.hbi_rk_free(self.h)
-            self.h = None
+        self.h = None
+
+    def __del__(self):
+        self.close()

@@ -164,9 +164,6 @@ struct hbi_ctl_s {
   bool have_tree = false;
   Structure S;
   int* d_lod = nullptr;
-  bool have_chains = false;
-  ChainPlan chains;
-  int32_t *d_row_fc = nullptr, *d_chain_ptr = nullptr, *d_chain_leaf = nullptr;
 };
 
 struct hbi_leafmtxp_s {
@@ -190,6 +187,7 @@ struct hbi_lhp_s {
   void* d_z = nullptr;
   LeafDescDev* d_desc = nullptr;
   double *d_x = nullptr, *d_y = nullptr;
+  int32_t *d_row_fc = nullptr, *d_chain_ptr = nullptr, *d_chain_leaf = nullptr;
   MatDev md{};
   ChainDev cd{};
   std::vector<Leaf> leaves;
@@ -199,6 +197,11 @@ struct hbi_lhp_s {
 
 extern "C" const char* hbi_last_error(void) { return g_err.c_str(); }
 extern "C" int hbi_version(void) { return 10000; }
+
+extern "C" int hbi_set_device(int device) {
+  CK(cudaSetDevice(device));
+  return HBI_OK;
+}
 
 extern "C" int hbi_init(int nd, hbi_ctl** out) {
   if (!out || nd < 1) return fail(HBI_ERR_ARG, "hbi_init: nd<1 or null handle");
@@ -228,7 +231,6 @@ extern "C" int hbi_param_get(const hbi_ctl* c, double* p) {
 extern "C" int hbi_finalize(hbi_ctl* c) {
   if (!c) return HBI_OK;
   dfree(c->d_lod);
-  dfree(c->d_row_fc); dfree(c->d_chain_ptr); dfree(c->d_chain_leaf);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return HBI_OK;
@@ -374,7 +376,6 @@ extern "C" int hbi_generate(hbi_leafmtxp** out, const hbi_bemv* bv, hbi_ctl* c, 
   if (c->param[20] < 2) c->param[20] = 3;  // HACApK_chk_st_ctl
   if (build_structure(c->nd, coord, c->param, c->S) != 0) return fail(HBI_ERR_ARG, "structure");
   c->have_tree = true;
-  c->have_chains = false;
   dfree(c->d_lod);
   CK(upload(&c->d_lod, c->S.lod, c->stream));
   DevGeom G;
@@ -527,28 +528,24 @@ extern "C" int hbi_entry_ij(const hbi_bemv* bv, int n, const int* i, const int* 
 }
 
 // ---------------------------------------------------------- construct
-static int ensure_chains(hbi_ctl* c) {
-  if (c->have_chains) return HBI_OK;
-  plan_chains(c->nd, c->S.leaves, c->chains);
-  dfree(c->d_row_fc); dfree(c->d_chain_ptr); dfree(c->d_chain_leaf);
-  CK(upload(&c->d_row_fc, c->chains.row_fc, c->stream));
-  CK(upload(&c->d_chain_ptr, c->chains.chain_ptr, c->stream));
-  CK(upload(&c->d_chain_leaf, c->chains.chain_leaf, c->stream));
-  c->have_chains = true;
-  return HBI_OK;
-}
-
 extern "C" int hbi_construct_lh(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* c, int storage) {
   if (!out || !lf || !c) return fail(HBI_ERR_ARG, "hbi_construct_lh: null");
   if (storage < 0 || storage > 2) return fail(HBI_ERR_ARG, "storage must be HBI_STORE_F64/F32/BF16");
   if (lf->ctl != c || !c->have_tree) return fail(HBI_ERR_STATE, "construct_LH needs the ctl used by generate");
-  int rc = ensure_chains(c);
-  if (rc) return rc;
   hbi_lhp* h = new hbi_lhp_s();
   h->ctl = c;
   h->n = c->nd;
   h->storage = storage;
   h->leaves = lf->leaves;
+  {
+    // row chains of this operator (owned by it, so a later generate on the
+    // same control block cannot invalidate them)
+    ChainPlan cp;
+    plan_chains(c->nd, lf->leaves, cp);
+    CK(upload(&h->d_row_fc, cp.row_fc, c->stream));
+    CK(upload(&h->d_chain_ptr, cp.chain_ptr, c->stream));
+    CK(upload(&h->d_chain_leaf, cp.chain_leaf, c->stream));
+  }
   const int esz = storage == ST_F64 ? 8 : storage == ST_F32 ? 4 : 2;
   const int chunk_rows = getenv("HBI_P1_CHUNK") ? atoi(getenv("HBI_P1_CHUNK")) : 2048;
   plan_matrix(lf->leaves, 16 / esz, chunk_rows, 8, h->plan);
@@ -620,7 +617,7 @@ extern "C" int hbi_construct_lh(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* 
   h->md.z = h->d_z;
   h->md.desc = h->d_desc;
   h->md.scale = 1.0;
-  h->cd = ChainDev{c->nd, c->d_row_fc, c->d_chain_ptr, c->d_chain_leaf};
+  h->cd = ChainDev{c->nd, h->d_row_fc, h->d_chain_ptr, h->d_chain_leaf};
   h->alg_bytes = (double)P.factor_elems * esz + (double)h->n * 8 * 2;
   *out = h;
   return HBI_OK;
@@ -630,6 +627,7 @@ extern "C" int hbi_free_lh(hbi_lhp* h) {
   if (!h) return HBI_OK;
   if (h->d_store) cudaFree(h->d_store);
   dfree(h->d_p1); dfree(h->d_lr); dfree(h->d_cnt); dfree(h->d_desc); dfree(h->d_x); dfree(h->d_y);
+  dfree(h->d_row_fc); dfree(h->d_chain_ptr); dfree(h->d_chain_leaf);
   if (h->d_part) cudaFree(h->d_part);
   if (h->d_z) cudaFree(h->d_z);
   delete h;
@@ -644,13 +642,34 @@ extern "C" int hbi_lh_info(const hbi_lhp* h, int64_t* fe, int64_t* sb, double* a
   return HBI_OK;
 }
 
-extern "C" int hbi_adot_lattice_hyp_dev(double* d_au, hbi_lhp* h, const double* d_u, void* stream) {
-  if (!h || !d_au || !d_u) return fail(HBI_ERR_ARG, "hbi_adot_lattice_hyp_dev: null");
+extern "C" int hbi_adot_lattice_hyp_phase_dev(double* d_au, hbi_lhp* h, const double* d_u, void* stream, int phase) {
+  if (!h || !d_u || (phase != 1 && !d_au) || phase < 0 || phase > 2)
+    return fail(HBI_ERR_ARG, "hbi_adot_lattice_hyp_phase_dev: bad arguments");
   cudaStream_t st = stream ? (cudaStream_t)stream : h->ctl->stream;
-  launch_phase1(&h->md, 1, d_u, h->ctl->sm_count, st);
-  double* ys[2] = {d_au, nullptr};
-  launch_phase2_plain(&h->md, 1, h->cd, d_u, ys, st);
+  if (phase != 2) launch_phase1(&h->md, 1, d_u, h->ctl->sm_count, st);
+  if (phase != 1) {
+    double* ys[2] = {d_au, nullptr};
+    launch_phase2_plain(&h->md, 1, h->cd, d_u, ys, st);
+  }
   CK(cudaGetLastError());
+  return HBI_OK;
+}
+
+extern "C" int hbi_adot_lattice_hyp_dev(double* d_au, hbi_lhp* h, const double* d_u, void* stream) {
+  return hbi_adot_lattice_hyp_phase_dev(d_au, h, d_u, stream, 0);
+}
+
+extern "C" int hbi_lh_phase_bytes(const hbi_lhp* h, double* p1, double* p2) {
+  if (!h) return fail(HBI_ERR_ARG, "null");
+  const int esz = h->storage == ST_F64 ? 8 : h->storage == ST_F32 ? 4 : 2;
+  double v = 0, rest = 0;
+  for (const Leaf& L : h->leaves) {
+    if (L.ltmtx == 1) { v += (double)L.kt * L.ndt; rest += (double)L.kt * L.ndl; }
+    else rest += (double)L.ndl * L.ndt;
+  }
+  // phase 1 reads V and x; phase 2 reads U, dense blocks and x, writes y
+  if (p1) *p1 = v * esz + (double)h->n * 8;
+  if (p2) *p2 = rest * esz + (double)h->n * 8 * 2;
   return HBI_OK;
 }
 
@@ -676,6 +695,11 @@ struct hbi_rk_s {
   MatDev mats[2];
   std::vector<double*> allocs;
   double* h_ctl = nullptr;  // pinned: h, eps, emax, huge index
+  static constexpr int kSlots = 64;
+  double* h_ring = nullptr;  // pinned (h, eps) slots
+  cudaEvent_t slot_ev[kSlots] = {};
+  int slot_used[kSlots] = {};
+  int slot = 0;
   cudaStream_t st = nullptr;
   cudaGraphExec_t gexec = nullptr;
   int launches = 0;
@@ -716,7 +740,12 @@ extern "C" int hbi_rk_create(hbi_rk** out, const hbi_rsf_params* p, hbi_lhp* ls,
   }
   hbi_rk* r = new hbi_rk_s();
   r->ls = ls; r->ln = ln; r->n = p->ncell; r->nmat = ln ? 2 : 1;
-  r->st = ls->ctl->stream;
+  // the RK handle issues all its work on a stream of its own, so its
+  // lifetime does not depend on the control blocks of the operators
+  if (cudaStreamCreateWithFlags(&r->st, cudaStreamNonBlocking) != cudaSuccess) {
+    delete r;
+    return fail(HBI_ERR_CUDA, "RK stream");
+  }
   const int n = r->n;
   auto mk = [&](double** d, size_t cnt) -> int {
     if (dalloc(d, cnt) != cudaSuccess) return 1;
@@ -740,10 +769,12 @@ extern "C" int hbi_rk_create(hbi_rk** out, const hbi_rsf_params* p, hbi_lhp* ls,
   bad |= mk(&R.y, 3 * n); bad |= mk(&R.ys, 3 * n); bad |= mk(&R.vs, n); bad |= mk(&R.x0, n);
   bad |= mk(&R.xb[0], n); bad |= mk(&R.xb[1], n); bad |= mk(&R.K, 18 * (size_t)n);
   bad |= mk(&R.yout, 3 * n); bad |= mk(&R.yerr, 3 * n); bad |= mk(&R.ebuf, 3 * n); bad |= mk(&R.ctl, 4);
-  if (bad || cudaMallocHost(&r->h_ctl, 4 * sizeof(double)) != cudaSuccess) {
+  if (bad || cudaMallocHost(&r->h_ctl, 4 * sizeof(double)) != cudaSuccess ||
+      cudaMallocHost(&r->h_ring, 2 * hbi_rk_s::kSlots * sizeof(double)) != cudaSuccess) {
     hbi_rk_free(r);
     return fail(HBI_ERR_NOMEM, "RK state allocation");
   }
+  for (int s = 0; s < hbi_rk_s::kSlots; s++) cudaEventCreateWithFlags(&r->slot_ev[s], cudaEventDisableTiming);
   r->mats[0] = ls->md; r->mats[0].scale = p->scale_s;
   if (ln) { r->mats[1] = ln->md; r->mats[1].scale = p->scale_n; }
   double B[15], C[6], DC[6];
@@ -756,9 +787,14 @@ extern "C" int hbi_rk_create(hbi_rk** out, const hbi_rsf_params* p, hbi_lhp* ls,
 
 extern "C" int hbi_rk_free(hbi_rk* r) {
   if (!r) return HBI_OK;
+  if (r->st) cudaStreamSynchronize(r->st);
   if (r->gexec) cudaGraphExecDestroy(r->gexec);
   for (double* p : r->allocs) cudaFree(p);
   if (r->h_ctl) cudaFreeHost(r->h_ctl);
+  if (r->h_ring) cudaFreeHost(r->h_ring);
+  for (int s = 0; s < hbi_rk_s::kSlots; s++)
+    if (r->slot_ev[s]) cudaEventDestroy(r->slot_ev[s]);
+  if (r->st) cudaStreamDestroy(r->st);
   delete r;
   return HBI_OK;
 }
@@ -791,11 +827,19 @@ static void enqueue_attempt(hbi_rk* r, cudaStream_t st) {
   }
 }
 
-static int run_attempt(hbi_rk* r, double h, double eps, double* errmax) {
+static int launch_attempt(hbi_rk* r, double h, double eps) {
   cudaStream_t st = r->st;
-  r->h_ctl[0] = h;
-  r->h_ctl[1] = eps;
-  CK(cudaMemcpyAsync(r->R.ctl, r->h_ctl, 2 * sizeof(double), cudaMemcpyHostToDevice, st));
+  // (h, eps) travel through a ring of pinned slots; a slot is rewritten only
+  // after the copy that last read it has completed
+  const int s = r->slot;
+  r->slot = (r->slot + 1) % hbi_rk_s::kSlots;
+  if (r->slot_used[s]) CK(cudaEventSynchronize(r->slot_ev[s]));
+  double* hc = r->h_ring + 2 * s;
+  hc[0] = h;
+  hc[1] = eps;
+  CK(cudaMemcpyAsync(r->R.ctl, hc, 2 * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaEventRecord(r->slot_ev[s], st));
+  r->slot_used[s] = 1;
   if (!r->gexec) {
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -805,6 +849,20 @@ static int run_attempt(hbi_rk* r, double h, double eps, double* errmax) {
     cudaGraphDestroy(g);
   }
   CK(cudaGraphLaunch(r->gexec, st));
+  return HBI_OK;
+}
+
+extern "C" void* hbi_rk_stream(const hbi_rk* r) { return r ? (void*)r->st : nullptr; }
+
+extern "C" int hbi_rk_attempt_async(hbi_rk* r, double h, double eps) {
+  if (!r) return fail(HBI_ERR_ARG, "null");
+  return launch_attempt(r, h, eps);
+}
+
+static int run_attempt(hbi_rk* r, double h, double eps, double* errmax) {
+  cudaStream_t st = r->st;
+  int rc0 = launch_attempt(r, h, eps);
+  if (rc0) return rc0;
   CK(cudaMemcpyAsync(r->h_ctl + 2, r->R.ctl + 2, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   double e = r->h_ctl[2];

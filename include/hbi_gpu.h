@@ -63,6 +63,8 @@ typedef struct hbi_rk_s hbi_rk;             /* RK45 state of the derivs/rkck/rkq
 
 const char* hbi_last_error(void);
 int hbi_version(void);
+/* select the CUDA device that subsequent hbi_init calls on this thread bind */
+int hbi_set_device(int device);
 
 /* HACApK_init (m_HACApK_base.f90:246-345): control block with the default
  * param(1:100) of a one-rank run (param(43)=1).  Binds the current device. */
@@ -108,6 +110,13 @@ int hbi_adot_lattice_hyp(double* au, hbi_lhp* st_LHp, hbi_ctl* st_ctl, double* w
 /* same product on device arrays, enqueued on `stream` (cudaStream_t, NULL =
  * the handle's stream); no synchronisation */
 int hbi_adot_lattice_hyp_dev(double* d_au, hbi_lhp* st_LHp, const double* d_u, void* stream);
+
+/* one phase of the product on device arrays: phase 1 forms z = V^T u for the
+ * low-rank leaves, phase 2 forms au from U z and the dense leaves (phase 2
+ * reads the z of the last phase 1); phase 0 runs both.  For kernel timing. */
+int hbi_adot_lattice_hyp_phase_dev(double* d_au, hbi_lhp* st_LHp, const double* d_u, void* stream, int phase);
+/* algorithmic bytes of each phase (factor bytes + vector bytes) */
+int hbi_lh_phase_bytes(const hbi_lhp* lh, double* phase1, double* phase2);
 
 /* HACApK_entry_ij (m_HACApK_calc_entry_ij.f90:24-90) evaluated on the GPU for
  * n (i,j) pairs, 1-based global ids. */
@@ -155,6 +164,11 @@ int hbi_rkqs(hbi_rk* rk, double* x, double htry, double eps, double dtmax, doubl
              double* hnext, double* errmax, int* nrjct);
 /* number of kernels the handle launches per RK attempt */
 int hbi_rk_launches_per_attempt(const hbi_rk* rk);
+/* the CUDA stream (cudaStream_t) the RK handle enqueues on, for timing events */
+void* hbi_rk_stream(const hbi_rk* rk);
+/* one RK attempt (rkck) enqueued on the handle's stream without any host
+ * synchronisation or copy; the error estimate stays on the device */
+int hbi_rk_attempt_async(hbi_rk* rk, double h, double eps);
 
 #ifdef __cplusplus
 }

@@ -187,9 +187,12 @@ struct hbi_lhp_s {
   void* d_z = nullptr;
   LeafDescDev* d_desc = nullptr;
   double *d_x = nullptr, *d_y = nullptr;
-  int32_t *d_row_fc = nullptr, *d_chain_ptr = nullptr, *d_chain_leaf = nullptr;
+  // row groups (owned by the operator)
+  int32_t *d_gleaf_ptr = nullptr, *d_gleaf = nullptr, *d_grow0 = nullptr, *d_gpoff = nullptr;
+  int32_t *d_row_fc = nullptr, *d_fc_ptr = nullptr, *d_fc_group = nullptr;
+  P2ItemDev* d_p2 = nullptr;
+  void* d_gpart = nullptr;
   MatDev md{};
-  ChainDev cd{};
   std::vector<Leaf> leaves;
   size_t store_bytes = 0;
   double alg_bytes = 0;
@@ -540,11 +543,28 @@ extern "C" int hbi_construct_lh(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* 
   {
     // row chains of this operator (owned by it, so a later generate on the
     // same control block cannot invalidate them)
-    ChainPlan cp;
-    plan_chains(c->nd, lf->leaves, cp);
-    CK(upload(&h->d_row_fc, cp.row_fc, c->stream));
-    CK(upload(&h->d_chain_ptr, cp.chain_ptr, c->stream));
-    CK(upload(&h->d_chain_leaf, cp.chain_leaf, c->stream));
+    GroupPlan gp;
+    plan_groups(c->nd, lf->leaves, gp);
+    std::vector<P2Item> p2;
+    plan_p2_items(lf->leaves, gp, p2);
+    std::vector<P2ItemDev> p2d(p2.size());
+    for (size_t i = 0; i < p2.size(); i++) p2d[i] = P2ItemDev{p2[i].group, p2[i].r0, p2[i].nr, 0};
+    CK(upload(&h->d_gleaf_ptr, gp.gleaf_ptr, c->stream));
+    CK(upload(&h->d_gleaf, gp.gleaf, c->stream));
+    CK(upload(&h->d_grow0, gp.grow0, c->stream));
+    CK(upload(&h->d_gpoff, gp.gpoff, c->stream));
+    CK(upload(&h->d_row_fc, gp.row_fc, c->stream));
+    CK(upload(&h->d_fc_ptr, gp.fc_ptr, c->stream));
+    CK(upload(&h->d_fc_group, gp.fc_group, c->stream));
+    CK(upload(&h->d_p2, p2d, c->stream));
+    const size_t acc_sz = storage == ST_F64 ? 8 : 4;
+    CK(cudaMalloc(&h->d_gpart, std::max<size_t>(gp.plen, 1) * acc_sz));
+    h->md.p2 = h->d_p2;
+    h->md.np2 = (int)p2d.size();
+    h->md.gleaf_ptr = h->d_gleaf_ptr; h->md.gleaf = h->d_gleaf; h->md.grow0 = h->d_grow0; h->md.gpoff = h->d_gpoff;
+    h->md.gpart = h->d_gpart;
+    h->md.row_fc = h->d_row_fc; h->md.fc_ptr = h->d_fc_ptr; h->md.fc_group = h->d_fc_group;
+    h->md.n = c->nd;
   }
   const int esz = storage == ST_F64 ? 8 : storage == ST_F32 ? 4 : 2;
   const int chunk_rows = getenv("HBI_P1_CHUNK") ? atoi(getenv("HBI_P1_CHUNK")) : 2048;
@@ -617,7 +637,6 @@ extern "C" int hbi_construct_lh(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* 
   h->md.z = h->d_z;
   h->md.desc = h->d_desc;
   h->md.scale = 1.0;
-  h->cd = ChainDev{c->nd, h->d_row_fc, h->d_chain_ptr, h->d_chain_leaf};
   h->alg_bytes = (double)P.factor_elems * esz + (double)h->n * 8 * 2;
   *out = h;
   return HBI_OK;
@@ -627,7 +646,9 @@ extern "C" int hbi_free_lh(hbi_lhp* h) {
   if (!h) return HBI_OK;
   if (h->d_store) cudaFree(h->d_store);
   dfree(h->d_p1); dfree(h->d_lr); dfree(h->d_cnt); dfree(h->d_desc); dfree(h->d_x); dfree(h->d_y);
-  dfree(h->d_row_fc); dfree(h->d_chain_ptr); dfree(h->d_chain_leaf);
+  dfree(h->d_gleaf_ptr); dfree(h->d_gleaf); dfree(h->d_grow0); dfree(h->d_gpoff);
+  dfree(h->d_row_fc); dfree(h->d_fc_ptr); dfree(h->d_fc_group); dfree(h->d_p2);
+  if (h->d_gpart) cudaFree(h->d_gpart);
   if (h->d_part) cudaFree(h->d_part);
   if (h->d_z) cudaFree(h->d_z);
   delete h;
@@ -649,7 +670,8 @@ extern "C" int hbi_adot_lattice_hyp_phase_dev(double* d_au, hbi_lhp* h, const do
   if (phase != 2) launch_phase1(&h->md, 1, d_u, h->ctl->sm_count, st);
   if (phase != 1) {
     double* ys[2] = {d_au, nullptr};
-    launch_phase2_plain(&h->md, 1, h->cd, d_u, ys, st);
+    launch_phase2(&h->md, 1, d_u, h->ctl->sm_count, st);
+    launch_phase3_plain(&h->md, 1, ys, st);
   }
   CK(cudaGetLastError());
   return HBI_OK;
@@ -780,7 +802,7 @@ extern "C" int hbi_rk_create(hbi_rk** out, const hbi_rsf_params* p, hbi_lhp* ls,
   double B[15], C[6], DC[6];
   cash_karp(B, C, DC);
   set_tableau(B, C, DC);
-  r->launches = 1 + 6 * (r->nmat + 1);
+  r->launches = 1 + 6 * (2 * r->nmat + 1);
   *out = r;
   return HBI_OK;
 }
@@ -816,14 +838,14 @@ extern "C" int hbi_rk_get_state(hbi_rk* r, double* y) {
 // the six stages of one Cash-Karp attempt (rkck) as a fixed launch sequence
 static void enqueue_attempt(hbi_rk* r, cudaStream_t st) {
   RkDev& R = r->R;
-  const ChainDev& ch = r->ls->cd;
   const int sm = r->ls->ctl->sm_count;
   launch_rk_prepare(R, st);
   for (int s = 0; s < 6; s++) {
     const double* xin = s == 0 ? R.x0 : R.xb[s & 1];
     double* xout = R.xb[(s + 1) & 1];
     launch_phase1(r->mats, r->nmat, xin, sm, st);
-    launch_phase2_rk(r->mats, r->nmat, ch, xin, R, s, xout, st);
+    launch_phase2(r->mats, r->nmat, xin, sm, st);
+    launch_phase3_rk(r->mats, r->nmat, R, s, xout, st);
   }
 }
 

@@ -56,23 +56,28 @@ struct LrInfo {
   int32_t kt, nparts, nitems, poff, zoff, pad;
 };
 
+struct P2ItemDev {
+  int32_t group, r0, nr, pad;
+};
+
 struct MatDev {            // one H-matrix on the device
+  int n;
   const void* store;       // factor store, element type per `storage`
   int storage;
   const P1ItemDev* p1;
   int np1;
   const LrInfo* lr;
   int* lr_cnt;             // arrival counters (self-resetting)
-  void* part;              // partial sums (Acc type)
+  void* part;              // phase-1 partial sums (Acc type)
   void* z;                 // z = V^T x per low-rank leaf (Acc type)
   const LeafDescDev* desc;
+  // row groups (leaves sharing a row range) and their phase-2 items
+  const P2ItemDev* p2;
+  int np2;
+  const int32_t *gleaf_ptr, *gleaf, *grow0, *gpoff;
+  void* gpart;             // per-group row partials (Acc type)
+  const int32_t *row_fc, *fc_ptr, *fc_group;
   double scale;            // result multiplier (1/ds0 for 3dph, else 1)
-};
-struct ChainDev {
-  int n;
-  const int32_t* row_fc;
-  const int32_t* chain_ptr;
-  const int32_t* chain_leaf;
 };
 
 // RK (Cash-Karp) stage state on the device; all arrays in cluster order
@@ -92,11 +97,12 @@ struct RkDev {
   double* ctl;     // [0]=h [1]=eps  [2]=emax (as bits) [3]=huge index (as int64)
 };
 
+// phase 1: z = V^T x; phase 2: per-group row partials of U z + A x;
+// phase 3: per-row sum of the group partials (plain, or with the RK epilogue)
 void launch_phase1(const MatDev* mats, int nmat, const double* x, int sm_count, cudaStream_t st);
-void launch_phase2_plain(const MatDev* mats, int nmat, const ChainDev& ch, const double* x, double* const* y,
-                         cudaStream_t st);
-void launch_phase2_rk(const MatDev* mats, int nmat, const ChainDev& ch, const double* x, const RkDev& rk, int stage,
-                      double* xnext, cudaStream_t st);
+void launch_phase2(const MatDev* mats, int nmat, const double* x, int sm_count, cudaStream_t st);
+void launch_phase3_plain(const MatDev* mats, int nmat, double* const* y, cudaStream_t st);
+void launch_phase3_rk(const MatDev* mats, int nmat, const RkDev& rk, int stage, double* xnext, cudaStream_t st);
 void launch_rk_prepare(const RkDev& rk, cudaStream_t st);
 void set_tableau(const double* B15, const double* C6, const double* DC6);
 // dst[dst_off[i] : +len[i]] = src[i][0 : len[i]]

@@ -98,38 +98,83 @@ __global__ void __launch_bounds__(256) p1_kernel(MatDev m, const double* __restr
 }
 
 // ---------------------------------------------------------------- phase 2
+// One warp per (row group, 32-row chunk): lane = row; the warp walks every
+// leaf of the group (identical for all lanes, so no divergence) and streams
+// the leaf's U or A column segments -- 32 consecutive rows per load.
 template <typename T>
-__device__ __forceinline__ typename AccOf<T>::type row_sum(const MatDev& m, const ChainDev& ch, int r,
-                                                          const double* __restrict__ x) {
+__global__ void __launch_bounds__(256) p2_group_kernel(MatDev m, const double* __restrict__ x) {
   typedef typename AccOf<T>::type Acc;
+  const int lane = threadIdx.x & 31;
+  const int warp = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  const int nwarps = (int)((gridDim.x * (int64_t)blockDim.x) >> 5);
   const T* store = (const T*)m.store;
   const Acc* z = (const Acc*)m.z;
-  const int f = __ldg(&ch.row_fc[r]);
-  const int e0 = __ldg(&ch.chain_ptr[f]), e1 = __ldg(&ch.chain_ptr[f + 1]);
-  Acc acc = 0;
-  for (int e = e0; e < e1; e++) {
-    const LeafDescDev L = m.desc[__ldg(&ch.chain_leaf[e])];
-    const int lr = r - L.row0;
-    const T* P = store + L.off + lr;
-    const int cnt = L.kt_or_ndt;
-    if (L.kind == 1) {
-      const Acc* zz = z + L.aux;
-      for (int k = 0; k < cnt; k++) acc += ld_acc(P + (int64_t)k * L.ndl) * zz[k];
-    } else {
-      const double* xx = x + L.aux;
-      for (int t = 0; t < cnt; t++) acc += ld_acc(P + (int64_t)t * L.ndl) * (Acc)__ldg(&xx[t]);
+  Acc* gpart = (Acc*)m.gpart;
+  for (int it = warp; it < m.np2; it += nwarps) {
+    const P2ItemDev I = m.p2[it];
+    const int g = I.group;
+    const int lr = I.r0 + lane;
+    const bool act = lane < I.nr;
+    const int e0 = __ldg(&m.gleaf_ptr[g]), e1 = __ldg(&m.gleaf_ptr[g + 1]);
+    Acc acc = 0;
+    for (int e = e0; e < e1; e++) {
+      const LeafDescDev L = m.desc[__ldg(&m.gleaf[e])];
+      const int cnt = L.kt_or_ndt;
+      const int64_t ld = L.ndl;
+      const T* P = store + L.off + (act ? lr : 0);
+      if (L.kind == 1) {
+        const Acc* zz = z + L.aux;
+        int k = 0;
+        for (; k + 4 <= cnt; k += 4) {
+          const Acc u0 = ld_acc(P + k * ld), u1 = ld_acc(P + (k + 1) * ld), u2 = ld_acc(P + (k + 2) * ld),
+                    u3 = ld_acc(P + (k + 3) * ld);
+          acc += u0 * zz[k];
+          acc += u1 * zz[k + 1];
+          acc += u2 * zz[k + 2];
+          acc += u3 * zz[k + 3];
+        }
+        for (; k < cnt; k++) acc += ld_acc(P + k * ld) * zz[k];
+      } else {
+        const double* xx = x + L.aux;
+        int t = 0;
+        for (; t + 4 <= cnt; t += 4) {
+          const Acc a0 = ld_acc(P + t * ld), a1 = ld_acc(P + (t + 1) * ld), a2 = ld_acc(P + (t + 2) * ld),
+                    a3 = ld_acc(P + (t + 3) * ld);
+          acc += a0 * (Acc)__ldg(&xx[t]);
+          acc += a1 * (Acc)__ldg(&xx[t + 1]);
+          acc += a2 * (Acc)__ldg(&xx[t + 2]);
+          acc += a3 * (Acc)__ldg(&xx[t + 3]);
+        }
+        for (; t < cnt; t++) acc += ld_acc(P + t * ld) * (Acc)__ldg(&xx[t]);
+      }
     }
+    if (act) gpart[__ldg(&m.gpoff[g]) + lr] = acc;
   }
-  return acc;
 }
 
-template <typename T>
-__global__ void __launch_bounds__(128) p2_plain_kernel(MatDev m0, MatDev m1, int nmat, ChainDev ch,
-                                                       const double* __restrict__ x, double* y0, double* y1) {
+// phase 3: y(r) = scale * sum over the groups covering row r, coarse to fine
+template <typename Acc>
+__device__ __forceinline__ double group_sum(const MatDev& m, int r) {
+  const Acc* gp = (const Acc*)m.gpart;
+  const int f = __ldg(&m.row_fc[r]);
+  const int e0 = __ldg(&m.fc_ptr[f]), e1 = __ldg(&m.fc_ptr[f + 1]);
+  Acc s = 0;
+  for (int e = e0; e < e1; e++) {
+    const int g = __ldg(&m.fc_group[e]);
+    s += __ldcg(&gp[__ldg(&m.gpoff[g]) + r - __ldg(&m.grow0[g])]);
+  }
+  return (double)s * m.scale;
+}
+
+__device__ __forceinline__ double row_value(const MatDev& m, int r) {
+  return m.storage == ST_F64 ? group_sum<double>(m, r) : group_sum<float>(m, r);
+}
+
+__global__ void __launch_bounds__(256) p3_plain_kernel(MatDev m0, MatDev m1, int nmat, double* y0, double* y1) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= ch.n) return;
-  y0[r] = (double)row_sum<T>(m0, ch, r, x) * m0.scale;
-  if (nmat == 2) y1[r] = (double)row_sum<T>(m1, ch, r, x) * m1.scale;
+  if (r >= m0.n) return;
+  y0[r] = row_value(m0, r);
+  if (nmat == 2) y1[r] = row_value(m1, r);
 }
 
 // deriv (main_LH.f90:2165-2244): aging (0) and slip (1) laws
@@ -163,15 +208,13 @@ __device__ __forceinline__ double slip_rate(double vref, double psi, double tau,
   return 2 * vref * exp(-psi / a) * sinh(tau / sig / a);
 }
 
-template <typename T>
-__global__ void __launch_bounds__(128) p2_rk_kernel(MatDev m0, MatDev m1, ChainDev ch, const double* __restrict__ x,
-                                                    RkDev R, int s, double* __restrict__ xnext) {
+__global__ void __launch_bounds__(128) p3_rk_kernel(MatDev m0, MatDev m1, RkDev R, int s, double* __restrict__ xnext) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   double emax = -1.0;
   long long hidx = -1;
-  if (r < ch.n) {
-    const double gs = (double)row_sum<T>(m0, ch, r, x) * m0.scale + R.taudot[r];
-    const double gn = (R.nmat == 2 ? (double)row_sum<T>(m1, ch, r, x) * m1.scale : 0.0) + R.sigdot[r];
+  if (r < R.n) {
+    const double gs = row_value(m0, r) + R.taudot[r];
+    const double gn = (R.nmat == 2 ? row_value(m1, r) : 0.0) + R.sigdot[r];
     const int n3 = 3 * R.n;
     const double psi = R.ys[3 * r], tau = R.ys[3 * r + 1], sig = R.ys[3 * r + 2];
     double k[3];
@@ -306,23 +349,25 @@ void launch_phase1(const MatDev* mats, int nmat, const double* x, int sm, cudaSt
   }
 }
 
-void launch_phase2_plain(const MatDev* mats, int nmat, const ChainDev& ch, const double* x, double* const* y,
-                         cudaStream_t st) {
-  const int blocks = (ch.n + 127) / 128;
-  const MatDev& m1 = nmat == 2 ? mats[1] : mats[0];
-  double* y1 = nmat == 2 ? y[1] : nullptr;
-  if (mats[0].storage == ST_F64) p2_plain_kernel<double><<<blocks, 128, 0, st>>>(mats[0], m1, nmat, ch, x, y[0], y1);
-  else if (mats[0].storage == ST_F32) p2_plain_kernel<float><<<blocks, 128, 0, st>>>(mats[0], m1, nmat, ch, x, y[0], y1);
-  else p2_plain_kernel<__nv_bfloat16><<<blocks, 128, 0, st>>>(mats[0], m1, nmat, ch, x, y[0], y1);
+void launch_phase2(const MatDev* mats, int nmat, const double* x, int sm, cudaStream_t st) {
+  for (int i = 0; i < nmat; i++) {
+    const MatDev& m = mats[i];
+    if (m.np2 == 0) continue;
+    const int blocks = p1_blocks(sm, m.np2);
+    if (m.storage == ST_F64) p2_group_kernel<double><<<blocks, 256, 0, st>>>(m, x);
+    else if (m.storage == ST_F32) p2_group_kernel<float><<<blocks, 256, 0, st>>>(m, x);
+    else p2_group_kernel<__nv_bfloat16><<<blocks, 256, 0, st>>>(m, x);
+  }
 }
 
-void launch_phase2_rk(const MatDev* mats, int nmat, const ChainDev& ch, const double* x, const RkDev& rk, int stage,
-                      double* xnext, cudaStream_t st) {
-  const int blocks = (ch.n + 127) / 128;
+void launch_phase3_plain(const MatDev* mats, int nmat, double* const* y, cudaStream_t st) {
   const MatDev& m1 = nmat == 2 ? mats[1] : mats[0];
-  if (mats[0].storage == ST_F64) p2_rk_kernel<double><<<blocks, 128, 0, st>>>(mats[0], m1, ch, x, rk, stage, xnext);
-  else if (mats[0].storage == ST_F32) p2_rk_kernel<float><<<blocks, 128, 0, st>>>(mats[0], m1, ch, x, rk, stage, xnext);
-  else p2_rk_kernel<__nv_bfloat16><<<blocks, 128, 0, st>>>(mats[0], m1, ch, x, rk, stage, xnext);
+  p3_plain_kernel<<<(mats[0].n + 255) / 256, 256, 0, st>>>(mats[0], m1, nmat, y[0], nmat == 2 ? y[1] : nullptr);
+}
+
+void launch_phase3_rk(const MatDev* mats, int nmat, const RkDev& rk, int stage, double* xnext, cudaStream_t st) {
+  const MatDev& m1 = nmat == 2 ? mats[1] : mats[0];
+  p3_rk_kernel<<<(rk.n + 127) / 128, 128, 0, st>>>(mats[0], m1, rk, stage, xnext);
 }
 
 void launch_rk_prepare(const RkDev& rk, cudaStream_t st) {

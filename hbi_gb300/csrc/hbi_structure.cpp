@@ -257,6 +257,71 @@ void plan_matrix(const std::vector<Leaf>& leaves, int align, int chunk_rows, int
   });
 }
 
+void plan_groups(int n, const std::vector<Leaf>& leaves, GroupPlan& gp) {
+  // groups ordered by (row0 ascending, ndl descending): coarse before fine
+  std::vector<std::pair<std::pair<int, int>, int>> key;
+  key.reserve(leaves.size());
+  for (int i = 0; i < (int)leaves.size(); i++) key.push_back({{leaves[i].nstrtl - 1, -leaves[i].ndl}, i});
+  std::stable_sort(key.begin(), key.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+  gp.gleaf_ptr.assign(1, 0);
+  gp.gleaf.clear(); gp.grow0.clear(); gp.gndl.clear(); gp.gpoff.clear();
+  int64_t poff = 0;
+  for (size_t k = 0; k < key.size(); k++) {
+    if (k == 0 || key[k].first != key[k - 1].first) {
+      if (k) gp.gleaf_ptr.push_back((int32_t)gp.gleaf.size());
+      gp.grow0.push_back(key[k].first.first);
+      gp.gndl.push_back(-key[k].first.second);
+      gp.gpoff.push_back((int32_t)poff);
+      poff += -key[k].first.second;
+    }
+    gp.gleaf.push_back(key[k].second);
+  }
+  gp.gleaf_ptr.push_back((int32_t)gp.gleaf.size());
+  gp.plen = poff;
+  // fine ranges: elementary intervals of all group boundaries
+  std::vector<int> bnd{0, n};
+  for (size_t g = 0; g < gp.grow0.size(); g++) {
+    bnd.push_back(gp.grow0[g]);
+    bnd.push_back(gp.grow0[g] + gp.gndl[g]);
+  }
+  std::sort(bnd.begin(), bnd.end());
+  bnd.erase(std::unique(bnd.begin(), bnd.end()), bnd.end());
+  const int nf = (int)bnd.size() - 1;
+  gp.row_fc.assign(n, 0);
+  for (int f = 0; f < nf; f++)
+    for (int r = bnd[f]; r < bnd[f + 1]; r++) gp.row_fc[r] = f;
+  std::vector<std::vector<int32_t>> cov(nf);
+  for (size_t g = 0; g < gp.grow0.size(); g++) {
+    int f0 = gp.row_fc[gp.grow0[g]], f1 = gp.row_fc[gp.grow0[g] + gp.gndl[g] - 1];
+    for (int f = f0; f <= f1; f++) cov[f].push_back((int32_t)g);
+  }
+  gp.fc_ptr.assign(1, 0);
+  gp.fc_group.clear();
+  for (int f = 0; f < nf; f++) {
+    for (int32_t g : cov[f]) gp.fc_group.push_back(g);
+    gp.fc_ptr.push_back((int32_t)gp.fc_group.size());
+  }
+}
+
+void plan_p2_items(const std::vector<Leaf>& leaves, const GroupPlan& gp, std::vector<P2Item>& items) {
+  const int ng = (int)gp.grow0.size();
+  std::vector<std::pair<int64_t, P2Item>> v;
+  for (int g = 0; g < ng; g++) {
+    int64_t cols = 0;
+    for (int e = gp.gleaf_ptr[g]; e < gp.gleaf_ptr[g + 1]; e++) {
+      const Leaf& L = leaves[gp.gleaf[e]];
+      cols += L.ltmtx == 1 ? L.kt : L.ndt;
+    }
+    for (int r0 = 0; r0 < gp.gndl[g]; r0 += 32) {
+      P2Item it{g, r0, std::min(32, gp.gndl[g] - r0), 0};
+      v.push_back({cols * it.nr, it});
+    }
+  }
+  std::stable_sort(v.begin(), v.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+  items.resize(v.size());
+  for (size_t i = 0; i < v.size(); i++) items[i] = v[i].second;
+}
+
 void plan_chains(int n, const std::vector<Leaf>& leaves, ChainPlan& cp) {
   std::vector<int> bnd;
   bnd.reserve(2 * leaves.size() + 2);

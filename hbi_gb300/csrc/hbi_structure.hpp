@@ -82,4 +82,23 @@ void plan_matrix(const std::vector<Leaf>& leaves, int align, int p1_chunk_rows, 
                  MatPlan& mp);
 void plan_chains(int n, const std::vector<Leaf>& leaves, ChainPlan& cp);
 
+// Row groups: the leaves that share one row range (nstrtl, ndl).  Phase 2
+// gives a warp one 32-row chunk of a group and all of the group's leaves; the
+// per-row sum over the (at most tree-depth) groups that cover a row follows.
+struct P2Item {
+  int32_t group, r0, nr, pad;
+};
+struct GroupPlan {
+  std::vector<int32_t> gleaf_ptr, gleaf;  // group -> its leaves, in leaf order
+  std::vector<int32_t> grow0, gndl;       // 0-based first row, rows
+  std::vector<int32_t> gpoff;             // offset of the group's partials
+  int64_t plen = 0;                       // sum of gndl
+  std::vector<int32_t> row_fc;            // row -> fine range
+  std::vector<int32_t> fc_ptr, fc_group;  // fine range -> covering groups, coarse to fine
+};
+void plan_groups(int n, const std::vector<Leaf>& leaves, GroupPlan& gp);
+// items of 32-row chunks, ordered by decreasing cost (bytes) for the static
+// warp schedule; cost uses kt, so the order is per matrix
+void plan_p2_items(const std::vector<Leaf>& leaves, const GroupPlan& gp, std::vector<P2Item>& items);
+
 }  // namespace hbi

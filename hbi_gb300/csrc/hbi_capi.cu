@@ -546,7 +546,7 @@ extern "C" int hbi_construct_lh(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* 
     GroupPlan gp;
     plan_groups(c->nd, lf->leaves, gp);
     std::vector<P2Item> p2;
-    plan_p2_items(lf->leaves, gp, p2);
+    plan_p2_items(lf->leaves, gp, 16 / (storage == ST_F64 ? 8 : storage == ST_F32 ? 4 : 2), p2);
     std::vector<P2ItemDev> p2d(p2.size());
     for (size_t i = 0; i < p2.size(); i++) p2d[i] = P2ItemDev{p2[i].group, p2[i].r0, p2[i].nr, 0};
     CK(upload(&h->d_gleaf_ptr, gp.gleaf_ptr, c->stream));
@@ -567,8 +567,9 @@ extern "C" int hbi_construct_lh(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* 
     h->md.n = c->nd;
   }
   const int esz = storage == ST_F64 ? 8 : storage == ST_F32 ? 4 : 2;
-  const int chunk_rows = getenv("HBI_P1_CHUNK") ? atoi(getenv("HBI_P1_CHUNK")) : 2048;
-  plan_matrix(lf->leaves, 16 / esz, chunk_rows, 8, h->plan);
+  // phase-1 items of about 8192 factor elements, up to 32 columns each
+  const int chunk_elems = getenv("HBI_P1_CHUNK") ? atoi(getenv("HBI_P1_CHUNK")) : 8192;
+  plan_matrix(lf->leaves, 16 / esz, chunk_elems, h->plan);
   MatPlan& P = h->plan;
   const int nl = (int)lf->leaves.size();
   // factor store in the requested precision

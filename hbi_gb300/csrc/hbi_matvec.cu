@@ -2,18 +2,20 @@
 // rate-and-state / Cash-Karp stage epilogue.
 //
 // Replaces HACApK_adot_lattice_hyp + HACApK_adot_body_lfmtx_hyp_contiguous
-// (m_HACApK_solve.f90:220-337, 2108-2164).  Two kernels per product:
-//   phase 1  z_l = V_l^T x for every low-rank leaf: one warp per (leaf, row
-//            chunk, column group) item; leaves split over several chunks are
-//            summed by the last-arriving warp in a fixed order;
-//   phase 2  one thread per row walks the leaves covering its row (coarse to
-//            fine) and accumulates U_l z_l and A_l x; the sum order per row is
-//            fixed, so the product is deterministic without atomics.
-// Factors are stored column-major (U, V: ndl/ndt x kt; dense A: ndl x ndt) in
-// FP64, FP32 or BF16; FP32/BF16 storage accumulates in FP32.
-// Phase 2 optionally runs the RK stage epilogue (derivs/deriv/rkck of
-// main_LH.f90:2053-2244, 2472-2554) for its row, so a Cash-Karp attempt is
-// 6 x (phase 1, phase 2) launches.
+// (m_HACApK_solve.f90:220-337, 2108-2164).  Three kernels per product:
+//   phase 1  z_l = V_l^T x for every low-rank leaf (one warp per leaf row
+//            chunk; leaves split over several chunks are summed by the
+//            last-arriving warp in a fixed order);
+//   phase 2  per row group (the leaves sharing one row range) and chunk of
+//            rows: sum of U_l z_l and A_l x over the group's leaves;
+//   phase 3  per row: sum of the partials of the groups covering the row,
+//            coarse to fine -- plain, or fused with the rate-and-state / RK
+//            stage epilogue (derivs/deriv/rkck, main_LH.f90:2053-2244,
+//            2472-2554).
+// Every sum has a fixed order, so the product is deterministic without atomics.
+// Factors are column-major (V: ndt x kt, U: ndl x kt, dense A: ndl x ndt), each
+// column zero-padded to 16 bytes, in FP64, FP32 or BF16; FP32/BF16 storage
+// accumulates in FP32.  All factor reads are 16-byte vector loads.
 #include <cuda_bf16.h>
 
 #include "hbi_kernels.cuh"
@@ -37,10 +39,39 @@ __device__ __forceinline__ double ld_acc(const double* p) { return __ldg(p); }
 __device__ __forceinline__ float ld_acc(const float* p) { return __ldg(p); }
 __device__ __forceinline__ float ld_acc(const __nv_bfloat16* p) { return __bfloat162float(__ldg(p)); }
 
+// ---------------------------------------------------------------- vectors
+// 16-byte loads: 4 floats, 2 doubles or 8 bf16 (widened to float)
+__device__ __forceinline__ void ldv(const float* p, float* o) {
+  const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+  o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+}
+__device__ __forceinline__ void ldv(const double* p, double* o) {
+  const double2 v = __ldg(reinterpret_cast<const double2*>(p));
+  o[0] = v.x; o[1] = v.y;
+}
+__device__ __forceinline__ void ldv(const __nv_bfloat16* p, float* o) {
+  const uint4 v = __ldg(reinterpret_cast<const uint4*>(p));
+  const unsigned w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    o[2 * i] = __uint_as_float(w[i] << 16);
+    o[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
+  }
+}
+// smallest power of two >= n, as a shift (n in 1..32)
+__device__ __forceinline__ int log2ceil32(int n) { return n <= 1 ? 0 : 32 - __clz(n - 1); }
+
 // ---------------------------------------------------------------- phase 1
-template <typename T, int KG>
+// z_l = V_l^T x.  V is column-major, each column padded to a multiple of VEC
+// rows.  A warp task covers rows [t0, t0+nt) of every column of one leaf.
+// The lanes form CS = 32/LW column slots of LW lanes; lane j of a slot reads
+// rows [j*VEC, j*VEC+VEC) of its column with one 16-byte load, so a warp
+// instruction moves CS column segments at once and four such columns are in
+// flight per lane.  Each column's sum is reduced over the LW lanes of its slot.
+template <typename T>
 __global__ void __launch_bounds__(256) p1_kernel(MatDev m, const double* __restrict__ x) {
   typedef typename AccOf<T>::type Acc;
+  constexpr int VEC = 16 / sizeof(T);
   const int lane = threadIdx.x & 31;
   const int warp = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
   const int nwarps = (int)((gridDim.x * (int64_t)blockDim.x) >> 5);
@@ -49,37 +80,45 @@ __global__ void __launch_bounds__(256) p1_kernel(MatDev m, const double* __restr
   Acc* z = (Acc*)m.z;
   for (int it = warp; it < m.np1; it += nwarps) {
     const P1ItemDev I = m.p1[it];
-    Acc acc[KG];
-#pragma unroll
-    for (int kk = 0; kk < KG; kk++) acc[kk] = 0;
+    const int nq = (I.nt + VEC - 1) / VEC;
+    const int lw = log2ceil32(min(nq, 32));
+    const int LW = 1 << lw, CS = 32 >> lw;
+    const int slot = lane >> lw, j = lane & (LW - 1);
     const T* V = store + I.voff;
-    if (I.nk == KG) {
-      for (int t = lane; t < I.nt; t += 32) {
-        const Acc xv = (Acc)__ldg(&x[I.x0 + t]);
+    const int64_t ld = I.ldv;
+    const LrInfo L = m.lr[I.lr];
+    Acc* dst = L.nparts == 1 ? z : part;
+    for (int kb = 0; kb < I.nk; kb += 4 * CS) {
+      Acc s[4] = {0, 0, 0, 0};
+      for (int q = j; q < nq; q += LW) {
+        const int t = q * VEC;
+        Acc xv[VEC], a[4][VEC];
+        // all loads of the step first; columns past nk re-read column 0 and
+        // are dropped at the write
 #pragma unroll
-        for (int kk = 0; kk < KG; kk++) acc[kk] += ld_acc(&V[(int64_t)kk * I.ldv + t]) * xv;
+        for (int u = 0; u < 4; u++) {
+          const int k = kb + u * CS + slot;
+          ldv(V + (k < I.nk ? k : 0) * ld + t, a[u]);
+        }
+#pragma unroll
+        for (int v = 0; v < VEC; v++) xv[v] = (t + v < I.nt) ? (Acc)__ldg(&x[I.x0 + t + v]) : Acc(0);
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+#pragma unroll
+          for (int v = 0; v < VEC; v++) s[u] += a[u][v] * xv[v];
       }
-    } else {
-      for (int t = lane; t < I.nt; t += 32) {
-        const Acc xv = (Acc)__ldg(&x[I.x0 + t]);
 #pragma unroll
-        for (int kk = 0; kk < KG; kk++)
-          if (kk < I.nk) acc[kk] += ld_acc(&V[(int64_t)kk * I.ldv + t]) * xv;
+      for (int u = 0; u < 4; u++)
+        for (int o = 1; o < LW; o <<= 1) s[u] += __shfl_xor_sync(0xffffffffu, s[u], o);
+      if (j == 0) {
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int k = kb + u * CS + slot;
+          if (k < I.nk) dst[I.pout + k] = s[u];
+        }
       }
     }
-#pragma unroll
-    for (int kk = 0; kk < KG; kk++)
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) acc[kk] += __shfl_xor_sync(0xffffffffu, acc[kk], o);
-    Acc mine = 0;
-#pragma unroll
-    for (int kk = 0; kk < KG; kk++)
-      if (lane == kk) mine = acc[kk];
-    const LrInfo L = m.lr[I.lr];
-    if (L.nparts == 1) {
-      if (lane < I.nk) z[I.pout + lane] = mine;
-    } else {
-      if (lane < I.nk) part[I.pout + lane] = mine;
+    if (L.nparts > 1) {
       __threadfence();
       int last = 0;
       if (lane == 0) last = (atomicAdd(&m.lr_cnt[I.lr], 1) == L.nitems - 1);
@@ -98,12 +137,17 @@ __global__ void __launch_bounds__(256) p1_kernel(MatDev m, const double* __restr
 }
 
 // ---------------------------------------------------------------- phase 2
-// One warp per (row group, 32-row chunk): lane = row; the warp walks every
-// leaf of the group (identical for all lanes, so no divergence) and streams
-// the leaf's U or A column segments -- 32 consecutive rows per load.
+// One warp per (row group, chunk of up to 32*VEC rows).  Lane j of column
+// slot `slot` owns rows [j*VEC, j*VEC+VEC) of the chunk; slots take different
+// columns (k) of the same leaf, and the group's leaves are walked in order
+// with their descriptors fetched 32 at a time and broadcast by shuffles.  The
+// slots' partial row sums are combined at the end.  All lanes run the same
+// loop trip counts, so the shuffles are convergent.
 template <typename T>
-__global__ void __launch_bounds__(256) p2_group_kernel(MatDev m, const double* __restrict__ x) {
+__global__ void __launch_bounds__(256, 2) p2_group_kernel(MatDev m, const double* __restrict__ x) {
   typedef typename AccOf<T>::type Acc;
+  constexpr int VEC = 16 / sizeof(T);
+  constexpr int UNR = VEC >= 8 ? 2 : 4;
   const int lane = threadIdx.x & 31;
   const int warp = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
   const int nwarps = (int)((gridDim.x * (int64_t)blockDim.x) >> 5);
@@ -113,42 +157,64 @@ __global__ void __launch_bounds__(256) p2_group_kernel(MatDev m, const double* _
   for (int it = warp; it < m.np2; it += nwarps) {
     const P2ItemDev I = m.p2[it];
     const int g = I.group;
-    const int lr = I.r0 + lane;
-    const bool act = lane < I.nr;
+    const int nq = (I.nr + VEC - 1) / VEC;
+    const int lw = log2ceil32(min(nq, 32));
+    const int LW = 1 << lw, CS = 32 >> lw;
+    const int slot = lane >> lw, j = lane & (LW - 1);
+    const bool act = j < nq;
+    const int rr = I.r0 + j * VEC;
+    Acc acc[VEC];
+#pragma unroll
+    for (int v = 0; v < VEC; v++) acc[v] = 0;
     const int e0 = __ldg(&m.gleaf_ptr[g]), e1 = __ldg(&m.gleaf_ptr[g + 1]);
-    Acc acc = 0;
-    for (int e = e0; e < e1; e++) {
-      const LeafDescDev L = m.desc[__ldg(&m.gleaf[e])];
-      const int cnt = L.kt_or_ndt;
-      const int64_t ld = L.ndl;
-      const T* P = store + L.off + (act ? lr : 0);
-      if (L.kind == 1) {
-        const Acc* zz = z + L.aux;
-        int k = 0;
-        for (; k + 4 <= cnt; k += 4) {
-          const Acc u0 = ld_acc(P + k * ld), u1 = ld_acc(P + (k + 1) * ld), u2 = ld_acc(P + (k + 2) * ld),
-                    u3 = ld_acc(P + (k + 3) * ld);
-          acc += u0 * zz[k];
-          acc += u1 * zz[k + 1];
-          acc += u2 * zz[k + 2];
-          acc += u3 * zz[k + 3];
+    for (int base = e0; base < e1; base += 32) {
+      const int nl = min(32, e1 - base);
+      long long my_off = 0;
+      int my_ld = 0, my_kind = 0, my_cnt = 0, my_aux = 0;
+      if (lane < nl) {
+        const LeafDescDev* d = m.desc + __ldg(&m.gleaf[base + lane]);
+        my_off = __ldg(&d->off);
+        my_ld = __ldg(&d->ndl);
+        my_kind = __ldg(&d->kind);
+        my_cnt = __ldg(&d->kt_or_ndt);
+        my_aux = __ldg(&d->aux);
+      }
+      for (int jl = 0; jl < nl; jl++) {
+        const long long off = __shfl_sync(0xffffffffu, my_off, jl);
+        const int64_t ld = __shfl_sync(0xffffffffu, my_ld, jl);
+        const int kind = __shfl_sync(0xffffffffu, my_kind, jl);
+        const int cnt = __shfl_sync(0xffffffffu, my_cnt, jl);
+        const int aux = __shfl_sync(0xffffffffu, my_aux, jl);
+        const T* P = store + off + (act ? rr : 0);
+        for (int kb = 0; kb < cnt; kb += UNR * CS) {
+          // issue every load of the unrolled step before the first FMA;
+          // out-of-range columns read column 0 and are multiplied by zero
+          Acc a[UNR][VEC], mu[UNR];
+#pragma unroll
+          for (int u = 0; u < UNR; u++) {
+            const int k = kb + u * CS + slot;
+            const bool ok = act && k < cnt;
+            const int kk = ok ? k : 0;
+            ldv(P + kk * ld, a[u]);
+            if (kind == 1) mu[u] = ok ? z[aux + kk] : Acc(0);
+            else mu[u] = ok ? (Acc)__ldg(&x[aux + kk]) : Acc(0);
+          }
+#pragma unroll
+          for (int u = 0; u < UNR; u++)
+#pragma unroll
+            for (int v = 0; v < VEC; v++) acc[v] += a[u][v] * mu[u];
         }
-        for (; k < cnt; k++) acc += ld_acc(P + k * ld) * zz[k];
-      } else {
-        const double* xx = x + L.aux;
-        int t = 0;
-        for (; t + 4 <= cnt; t += 4) {
-          const Acc a0 = ld_acc(P + t * ld), a1 = ld_acc(P + (t + 1) * ld), a2 = ld_acc(P + (t + 2) * ld),
-                    a3 = ld_acc(P + (t + 3) * ld);
-          acc += a0 * (Acc)__ldg(&xx[t]);
-          acc += a1 * (Acc)__ldg(&xx[t + 1]);
-          acc += a2 * (Acc)__ldg(&xx[t + 2]);
-          acc += a3 * (Acc)__ldg(&xx[t + 3]);
-        }
-        for (; t < cnt; t++) acc += ld_acc(P + t * ld) * (Acc)__ldg(&xx[t]);
       }
     }
-    if (act) gpart[__ldg(&m.gpoff[g]) + lr] = acc;
+#pragma unroll
+    for (int v = 0; v < VEC; v++)
+      for (int o = LW; o < 32; o <<= 1) acc[v] += __shfl_xor_sync(0xffffffffu, acc[v], o);
+    if (slot == 0 && act) {
+      const int gp = __ldg(&m.gpoff[g]);
+#pragma unroll
+      for (int v = 0; v < VEC; v++)
+        if (rr + v < I.r0 + I.nr) gpart[gp + rr + v] = acc[v];
+    }
   }
 }
 
@@ -311,34 +377,59 @@ template <typename T>
 __global__ void store_convert_kernel(const double* __restrict__ src, int nleaf, const int64_t* src_off,
                                      const int64_t* dst_off, const int32_t* kind, const int32_t* rows,
                                      const int32_t* cols, const int32_t* kts, T* dst) {
+  // columns padded to multiples of VEC rows (16 bytes); the store is zeroed
+  // beforehand, so pad rows stay zero
+  constexpr int VEC = 16 / sizeof(T);
   for (int lf = blockIdx.x; lf < nleaf; lf += gridDim.x) {
     const double* s = src + src_off[lf];
     T* d = dst + dst_off[lf];
     const int ndl = rows[lf], ndt = cols[lf];
+    const int64_t ndlp = (ndl + VEC - 1) / VEC * VEC;
     if (kind[lf] == 1) {
-      const int64_t ne = (int64_t)kts[lf] * (ndl + ndt);
-      for (int64_t e = threadIdx.x; e < ne; e += blockDim.x) d[e] = cvt<T>(s[e]);
+      // [V: ndtp x kt][U: ndlp x kt], column-major, from [V: ndt x kt][U: ndl x kt]
+      const int kt = kts[lf];
+      const int64_t ndtp = (ndt + VEC - 1) / VEC * VEC;
+      const int64_t nv = (int64_t)kt * ndt, nu = (int64_t)kt * ndl;
+      for (int64_t e = threadIdx.x; e < nv; e += blockDim.x) {
+        const int64_t k = e / ndt, t = e % ndt;
+        d[k * ndtp + t] = cvt<T>(s[e]);
+      }
+      T* du = d + ndtp * kt;
+      for (int64_t e = threadIdx.x; e < nu; e += blockDim.x) {
+        const int64_t k = e / ndl, i = e % ndl;
+        du[k * ndlp + i] = cvt<T>(s[nv + e]);
+      }
     } else {
+      // A(il, it) column-major with leading dimension ndlp, from a1(ndt, ndl)
       const int64_t ne = (int64_t)ndl * ndt;
       for (int64_t e = threadIdx.x; e < ne; e += blockDim.x) {
-        const int il = (int)(e % ndl), it = (int)(e / ndl);  // dst (il,it), column-major
-        d[e] = cvt<T>(s[(int64_t)il * ndt + it]);
+        const int64_t it = e / ndl, il = e % ndl;
+        d[it * ndlp + il] = cvt<T>(s[il * ndt + it]);
       }
     }
   }
 }
 
 // ------------------------------------------------------------- launchers
-static int p1_blocks(int sm, int nitems) {
-  int b = sm * 8;
-  int need = (nitems + 7) / 8;
-  return need < b ? (need > 0 ? need : 1) : b;
+// persistent grid: as many 256-thread blocks as are resident at once (one
+// wave), never more than the items need
+template <typename K>
+static int grid_for(K kernel, int sm, int nitems) {
+  static int per_sm = 0;  // one cache per kernel instantiation
+  if (per_sm == 0) {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, 256, 0) != cudaSuccess || nb < 1) nb = 4;
+    per_sm = nb;
+  }
+  const int full = per_sm * sm;
+  const int need = (nitems + 7) / 8;
+  return need < full ? (need > 0 ? need : 1) : full;
 }
 
 template <typename T>
 static void p1_launch_t(const MatDev& m, const double* x, int sm, cudaStream_t st) {
   if (m.np1 == 0) return;
-  p1_kernel<T, 8><<<p1_blocks(sm, m.np1), 256, 0, st>>>(m, x);
+  p1_kernel<T><<<grid_for(p1_kernel<T>, sm, m.np1), 256, 0, st>>>(m, x);
 }
 
 void launch_phase1(const MatDev* mats, int nmat, const double* x, int sm, cudaStream_t st) {
@@ -353,10 +444,12 @@ void launch_phase2(const MatDev* mats, int nmat, const double* x, int sm, cudaSt
   for (int i = 0; i < nmat; i++) {
     const MatDev& m = mats[i];
     if (m.np2 == 0) continue;
-    const int blocks = p1_blocks(sm, m.np2);
-    if (m.storage == ST_F64) p2_group_kernel<double><<<blocks, 256, 0, st>>>(m, x);
-    else if (m.storage == ST_F32) p2_group_kernel<float><<<blocks, 256, 0, st>>>(m, x);
-    else p2_group_kernel<__nv_bfloat16><<<blocks, 256, 0, st>>>(m, x);
+    if (m.storage == ST_F64)
+      p2_group_kernel<double><<<grid_for(p2_group_kernel<double>, sm, m.np2), 256, 0, st>>>(m, x);
+    else if (m.storage == ST_F32)
+      p2_group_kernel<float><<<grid_for(p2_group_kernel<float>, sm, m.np2), 256, 0, st>>>(m, x);
+    else
+      p2_group_kernel<__nv_bfloat16><<<grid_for(p2_group_kernel<__nv_bfloat16>, sm, m.np2), 256, 0, st>>>(m, x);
   }
 }
 

@@ -195,63 +195,69 @@ int build_structure(int n, const double* coord, const double* param_in, Structur
 
 static int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
 
-void plan_matrix(const std::vector<Leaf>& leaves, int align, int chunk_rows, int kgroup, MatPlan& mp) {
+void plan_matrix(const std::vector<Leaf>& leaves, int vec, int item_elems, MatPlan& mp) {
+  // Every column of V (ndt rows), U (ndl rows) and dense A (ndl rows) is
+  // padded with zeros to a multiple of `vec` rows (vec elements = 16 bytes),
+  // so each column, and each block, starts on a 16-byte boundary and can be
+  // read with 16-byte vector loads.
   const int nl = (int)leaves.size();
   mp.leaf_off.assign(nl, 0);
   mp.p1.clear(); mp.lr_leaf.clear(); mp.lr_zoff.clear(); mp.lr_nparts.clear(); mp.lr_poff.clear();
   mp.desc.assign(nl, LeafDesc{});
   int64_t off = 0, z = 0, pz = 0, fe = 0;
+  const int quantum = 32 * vec;  // rows one warp covers with one vector load per lane
   for (int i = 0; i < nl; i++) {
     const Leaf& L = leaves[i];
-    off = round_up(off, align);
+    off = round_up(off, vec);
     mp.leaf_off[i] = off;
     LeafDesc& d = mp.desc[i];
+    const int ndlp = (int)round_up(L.ndl, vec);
     d.row0 = L.nstrtl - 1;
-    d.ndl = L.ndl;
+    d.ndl = ndlp;  // leading dimension of U / A
     d.kind = L.ltmtx;
     if (L.ltmtx == 1) {
+      const int ndtp = (int)round_up(L.ndt, vec);
       int lr = (int)mp.lr_leaf.size();
-      int nparts = (L.ndt + chunk_rows - 1) / chunk_rows;
+      // rows per phase-1 task: about item_elems elements, a multiple of quantum
+      int chunk = (int)std::max<int64_t>(quantum, (item_elems / std::max(L.kt, 1)) / quantum * quantum);
+      int nparts = (ndtp + chunk - 1) / chunk;
       mp.lr_leaf.push_back(i);
       mp.lr_nparts.push_back(nparts);
       mp.lr_zoff.push_back((int32_t)z);
       mp.lr_poff.push_back((int32_t)pz);
       for (int p = 0; p < nparts; p++) {
-        int t0 = p * chunk_rows;
-        int nt = std::min(chunk_rows, L.ndt - t0);
-        for (int k0 = 0; k0 < L.kt; k0 += kgroup) {
-          P1Item it;
-          it.voff = off + (int64_t)k0 * L.ndt + t0;
-          it.ldv = L.ndt;
-          it.nt = nt;
-          it.x0 = L.nstrtt - 1 + t0;
-          it.k0 = k0;
-          it.nk = std::min(kgroup, L.kt - k0);
-          it.leaf = lr;
-          it.part = p;
-          mp.p1.push_back(it);
-        }
+        int t0 = p * chunk;
+        P1Item it;
+        it.voff = off + t0;
+        it.ldv = ndtp;
+        it.nt = std::min(chunk, L.ndt - t0);
+        it.x0 = L.nstrtt - 1 + t0;
+        it.k0 = 0;
+        it.nk = L.kt;
+        it.leaf = lr;
+        it.part = p;
+        mp.p1.push_back(it);
       }
-      d.off = off + (int64_t)L.ndt * L.kt;  // U block follows V
+      d.off = off + (int64_t)ndtp * L.kt;  // U block follows V
       d.kt_or_ndt = L.kt;
       d.aux = (int32_t)z;
       z += L.kt;
       pz += (int64_t)L.kt * nparts;
-      off += (int64_t)L.kt * (L.ndl + L.ndt);
+      off += (int64_t)L.kt * (ndlp + ndtp);
       fe += (int64_t)L.kt * (L.ndl + L.ndt);
     } else {
       d.off = off;
       d.kt_or_ndt = L.ndt;
       d.aux = L.nstrtt - 1;
-      off += (int64_t)L.ndl * L.ndt;
+      off += (int64_t)ndlp * L.ndt;
       fe += (int64_t)L.ndl * L.ndt;
     }
   }
-  mp.store_elems = round_up(off, align);
+  mp.store_elems = round_up(off, vec);
   mp.zlen = z;
   mp.plen = pz;
   mp.factor_elems = fe;
-  // big items first so the static warp schedule ends evenly
+  // big tasks first so the static warp schedule ends evenly
   std::stable_sort(mp.p1.begin(), mp.p1.end(), [](const P1Item& a, const P1Item& b) {
     return (int64_t)a.nt * a.nk > (int64_t)b.nt * b.nk;
   });
@@ -303,8 +309,9 @@ void plan_groups(int n, const std::vector<Leaf>& leaves, GroupPlan& gp) {
   }
 }
 
-void plan_p2_items(const std::vector<Leaf>& leaves, const GroupPlan& gp, std::vector<P2Item>& items) {
+void plan_p2_items(const std::vector<Leaf>& leaves, const GroupPlan& gp, int vec, std::vector<P2Item>& items) {
   const int ng = (int)gp.grow0.size();
+  const int quantum = 32 * vec;  // rows of one task: 32 lanes x one vector each
   std::vector<std::pair<int64_t, P2Item>> v;
   for (int g = 0; g < ng; g++) {
     int64_t cols = 0;
@@ -312,8 +319,8 @@ void plan_p2_items(const std::vector<Leaf>& leaves, const GroupPlan& gp, std::ve
       const Leaf& L = leaves[gp.gleaf[e]];
       cols += L.ltmtx == 1 ? L.kt : L.ndt;
     }
-    for (int r0 = 0; r0 < gp.gndl[g]; r0 += 32) {
-      P2Item it{g, r0, std::min(32, gp.gndl[g] - r0), 0};
+    for (int r0 = 0; r0 < gp.gndl[g]; r0 += quantum) {
+      P2Item it{g, r0, std::min(quantum, gp.gndl[g] - r0), 0};
       v.push_back({cols * it.nr, it});
     }
   }

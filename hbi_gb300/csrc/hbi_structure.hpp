@@ -39,7 +39,7 @@ int build_structure(int n, const double* coord, const double* param, Structure& 
 // one thread per row walking the leaves that cover the row) chains.
 struct P1Item {            // one warp task
   int64_t voff;            // element offset of V(t0, k0) in the factor store
-  int32_t ldv;             // leading dimension of V (ndt)
+  int32_t ldv;             // row stride of the transposed V (kt)
   int32_t nt;              // rows in this chunk
   int32_t x0;              // 0-based column of x for row t0
   int32_t k0, nk;          // column range of V
@@ -78,8 +78,9 @@ struct ChainPlan {                   // shared by matrices with the same leaf li
 };
 
 // align: element alignment of each leaf block in the factor store
-void plan_matrix(const std::vector<Leaf>& leaves, int align, int p1_chunk_rows, int p1_kgroup,
-                 MatPlan& mp);
+// vec: elements per 16-byte vector of the storage type; columns are padded to
+// multiples of vec rows.  item_elems: target size of a phase-1 task.
+void plan_matrix(const std::vector<Leaf>& leaves, int vec, int item_elems, MatPlan& mp);
 void plan_chains(int n, const std::vector<Leaf>& leaves, ChainPlan& cp);
 
 // Row groups: the leaves that share one row range (nstrtl, ndl).  Phase 2
@@ -99,6 +100,6 @@ struct GroupPlan {
 void plan_groups(int n, const std::vector<Leaf>& leaves, GroupPlan& gp);
 // items of 32-row chunks, ordered by decreasing cost (bytes) for the static
 // warp schedule; cost uses kt, so the order is per matrix
-void plan_p2_items(const std::vector<Leaf>& leaves, const GroupPlan& gp, std::vector<P2Item>& items);
+void plan_p2_items(const std::vector<Leaf>& leaves, const GroupPlan& gp, int vec, std::vector<P2Item>& items);
 
 }  // namespace hbi

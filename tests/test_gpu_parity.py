@@ -147,7 +147,14 @@ def test_matvec_mixed(built, kind, store, tol):
     y = lm.matvec(u)
     assert np.linalg.norm(y - ref) <= tol * np.linalg.norm(ref)
     info = lm.info()
-    assert info["store_bytes"] <= info["factor_elems"] * (4 if store == "f32" else 2) * 1.05 + 4096
+    # the store holds exactly the factors with every column zero-padded to 16 bytes
+    esz = 4 if store == "f32" else 2
+    vec = 16 // esz
+    pad = lambda r: (r + vec - 1) // vec * vec
+    lv = B["lf"].leaves()
+    elems = sum(kt * (pad(ndl) + pad(ndt)) if lt == 1 else pad(ndl) * ndt for lt, kt, _, ndl, _, ndt in lv)
+    assert elems * esz <= info["store_bytes"] <= (elems + vec * len(lv)) * esz + 64
+    assert info["factor_elems"] == sum(kt * (ndl + ndt) if lt == 1 else ndl * ndt for lt, kt, _, ndl, _, ndt in lv)
 
 
 def _rsf_setup(B, oracle, two_mats, evlaw=0):

@@ -35,7 +35,7 @@ EXPORTS = [
     "hbi_get_leaves", "hbi_get_body", "hbi_lh_info", "hbi_rk_create", "hbi_rk_free", "hbi_rk_set_state",
     "hbi_rk_get_state", "hbi_derivs", "hbi_rkck", "hbi_rkqs", "hbi_rk_launches_per_attempt",
     "hbi_cluster_structure", "hbi_rk_stream", "hbi_rk_attempt_async", "hbi_set_device",
-    "hbi_adot_lattice_hyp_phase_dev", "hbi_lh_phase_bytes",
+    "hbi_adot_lattice_hyp_phase_dev", "hbi_lh_phase_bytes", "hbi_adot_lattice_hyp_noalloc",
 ]
 
 

@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -196,6 +197,7 @@ struct hbi_lhp_s {
   std::vector<Leaf> leaves;
   size_t store_bytes = 0;
   double alg_bytes = 0;
+  int64_t gplen = 0;  // row-group partials (elements)
 };
 
 extern "C" const char* hbi_last_error(void) { return g_err.c_str(); }
@@ -558,6 +560,7 @@ extern "C" int hbi_construct_lh(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* 
     CK(upload(&h->d_fc_group, gp.fc_group, c->stream));
     CK(upload(&h->d_p2, p2d, c->stream));
     const size_t acc_sz = storage == ST_F64 ? 8 : 4;
+    h->gplen = gp.plen;
     CK(cudaMalloc(&h->d_gpart, std::max<size_t>(gp.plen, 1) * acc_sz));
     h->md.p2 = h->d_p2;
     h->md.np2 = (int)p2d.size();
@@ -680,6 +683,56 @@ extern "C" int hbi_adot_lattice_hyp_phase_dev(double* d_au, hbi_lhp* h, const do
 
 extern "C" int hbi_adot_lattice_hyp_dev(double* d_au, hbi_lhp* h, const double* d_u, void* stream) {
   return hbi_adot_lattice_hyp_phase_dev(d_au, h, d_u, stream, 0);
+}
+
+// ----------------------------------------------------- allocation-free product
+// The scratch of hbi_adot_lattice_hyp_noalloc: one array in the library's
+// device image.  Host code may not use g_noalloc_scratch as an address (on the
+// host it names a shadow variable); its device address comes from
+// cudaGetSymbolAddress, once per device.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[HBI_NOALLOC_SCRATCH_BYTES];
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_addr[128];
+
+static size_t align256(size_t b) { return (b + 255) / 256 * 256; }
+
+extern "C" int hbi_adot_lattice_hyp_noalloc(double* d_au, hbi_lhp* h, const double* d_u, void* stream) {
+  if (!h || !d_au || !d_u) return fail(HBI_ERR_ARG, "hbi_adot_lattice_hyp_noalloc: null argument");
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 128) return fail(HBI_ERR_LIMIT, "hbi_adot_lattice_hyp_noalloc: device %d out of range", dev);
+  void* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) CK(cudaGetSymbolAddress(&g_noalloc_addr[dev], g_noalloc_scratch));
+    base = g_noalloc_addr[dev];
+  }
+  // layout: [arrival counters][z][phase-1 partials][row-group partials]
+  const size_t acc = h->storage == ST_F64 ? 8 : 4;
+  const size_t nlr = h->plan.lr_leaf.size();
+  const size_t b_cnt = align256(std::max<size_t>(nlr, 1) * sizeof(int));
+  const size_t b_z = align256(std::max<int64_t>(h->plan.zlen, 1) * acc);
+  const size_t b_part = align256(std::max<int64_t>(h->plan.plen, 1) * acc);
+  const size_t b_gp = align256(std::max<int64_t>(h->gplen, 1) * acc);
+  const size_t need = b_cnt + b_z + b_part + b_gp;
+  if (need > HBI_NOALLOC_SCRATCH_BYTES)
+    return fail(HBI_ERR_LIMIT, "hbi_adot_lattice_hyp_noalloc: operator needs %zu bytes of scratch, the limit is %u",
+                need, (unsigned)HBI_NOALLOC_SCRATCH_BYTES);
+  unsigned char* p = (unsigned char*)base;
+  MatDev md = h->md;
+  md.lr_cnt = (int*)p;
+  md.z = p + b_cnt;
+  md.part = p + b_cnt + b_z;
+  md.gpart = p + b_cnt + b_z + b_part;
+  cudaStream_t st = stream ? (cudaStream_t)stream : h->ctl->stream;
+  // the counters must start at zero; everything else is written before it is read
+  CK(cudaMemsetAsync(md.lr_cnt, 0, nlr * sizeof(int), st));
+  double* ys[2] = {d_au, nullptr};
+  launch_phase1(&md, 1, d_u, h->ctl->sm_count, st);
+  launch_phase2(&md, 1, d_u, h->ctl->sm_count, st);
+  launch_phase3_plain(&md, 1, ys, st);
+  CK(cudaGetLastError());
+  return HBI_OK;
 }
 
 extern "C" int hbi_lh_phase_bytes(const hbi_lhp* h, double* p1, double* p2) {

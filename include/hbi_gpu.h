@@ -111,6 +111,24 @@ int hbi_adot_lattice_hyp(double* au, hbi_lhp* st_LHp, hbi_ctl* st_ctl, double* w
  * the handle's stream); no synchronisation */
 int hbi_adot_lattice_hyp_dev(double* d_au, hbi_lhp* st_LHp, const double* d_u, void* stream);
 
+/* The product of hbi_adot_lattice_hyp_dev without any device allocation.
+ * No counterpart in the reference (HACApK allocates its scratch per call).
+ * For callers that cannot allocate device memory at the point of the call:
+ * a host program whose device memory is owned by another allocator or held
+ * under a fixed budget, or a time loop that must not reach cudaMalloc, which
+ * can synchronise the whole device.  The per-call scratch (phase-1 sums, the
+ * z vectors, the row-group partials and arrival counters) lives in one
+ * file-scope device array of HBI_NOALLOC_SCRATCH_BYTES (16 MiB) inside the
+ * library, which every GPU that loads the library holds until the process
+ * exits.  Operators whose scratch exceeds that return HBI_ERR_LIMIT.  The
+ * first call on a device looks up the array's device address (one-time
+ * set-up, no allocation); make that first call before any stream capture.
+ * All calls share the array and it keeps the previous call's contents (the
+ * counters are cleared on every call), so calls that overlap on the GPU --
+ * on different streams, or from different threads -- race; serialise them. */
+#define HBI_NOALLOC_SCRATCH_BYTES (16u << 20)
+int hbi_adot_lattice_hyp_noalloc(double* d_au, hbi_lhp* st_LHp, const double* d_u, void* stream);
+
 /* one phase of the product on device arrays: phase 1 forms z = V^T u for the
  * low-rank leaves, phase 2 forms au from U z and the dense leaves (phase 2
  * reads the z of the last phase 1); phase 0 runs both.  For kernel timing. */

@@ -856,7 +856,7 @@ extern "C" int hbi_rk_create(hbi_rk** out, const hbi_rsf_params* p, hbi_lhp* ls,
   double B[15], C[6], DC[6];
   cash_karp(B, C, DC);
   set_tableau(B, C, DC);
-  r->launches = 1 + 6 * (2 * r->nmat + 1);
+  r->launches = 1 + 6 * 3;  // prepare + per stage: phase 1, phase 2 (both matrices), phase 3
   *out = r;
   return HBI_OK;
 }

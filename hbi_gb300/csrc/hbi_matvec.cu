@@ -18,6 +18,9 @@
 // accumulates in FP32.  All factor reads are 16-byte vector loads.
 #include <cuda_bf16.h>
 
+#include <map>
+#include <mutex>
+
 #include "hbi_kernels.cuh"
 
 namespace hbi {
@@ -69,24 +72,29 @@ __device__ __forceinline__ int log2ceil32(int n) { return n <= 1 ? 0 : 32 - __cl
 // instruction moves CS column segments at once and four such columns are in
 // flight per lane.  Each column's sum is reduced over the LW lanes of its slot.
 template <typename T>
-__global__ void __launch_bounds__(256) p1_kernel(MatDev m, const double* __restrict__ x) {
+__global__ void __launch_bounds__(256) p1_kernel(MatDev m0, MatDev m1, int nmat, const double* __restrict__ x) {
   typedef typename AccOf<T>::type Acc;
   constexpr int VEC = 16 / sizeof(T);
   const int lane = threadIdx.x & 31;
   const int warp = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
   const int nwarps = (int)((gridDim.x * (int64_t)blockDim.x) >> 5);
-  const T* store = (const T*)m.store;
-  Acc* part = (Acc*)m.part;
-  Acc* z = (Acc*)m.z;
-  for (int it = warp; it < m.np1; it += nwarps) {
-    const P1ItemDev I = m.p1[it];
+  // the tasks of both H-matrices (shear, normal) in one grid: m0's, then m1's
+  const int n0 = m0.np1, ntot = nmat == 2 ? n0 + m1.np1 : n0;
+  for (int it = warp; it < ntot; it += nwarps) {
+    const bool sec = it >= n0;
+    const T* store = (const T*)(sec ? m1.store : m0.store);
+    Acc* part = (Acc*)(sec ? m1.part : m0.part);
+    Acc* z = (Acc*)(sec ? m1.z : m0.z);
+    const LrInfo* lrt = sec ? m1.lr : m0.lr;
+    int* cnt = sec ? m1.lr_cnt : m0.lr_cnt;
+    const P1ItemDev I = (sec ? m1.p1 : m0.p1)[sec ? it - n0 : it];
     const int nq = (I.nt + VEC - 1) / VEC;
     const int lw = log2ceil32(min(nq, 32));
     const int LW = 1 << lw, CS = 32 >> lw;
     const int slot = lane >> lw, j = lane & (LW - 1);
     const T* V = store + I.voff;
     const int64_t ld = I.ldv;
-    const LrInfo L = m.lr[I.lr];
+    const LrInfo L = lrt[I.lr];
     Acc* dst = L.nparts == 1 ? z : part;
     for (int kb = 0; kb < I.nk; kb += 4 * CS) {
       Acc s[4] = {0, 0, 0, 0};
@@ -121,7 +129,7 @@ __global__ void __launch_bounds__(256) p1_kernel(MatDev m, const double* __restr
     if (L.nparts > 1) {
       __threadfence();
       int last = 0;
-      if (lane == 0) last = (atomicAdd(&m.lr_cnt[I.lr], 1) == L.nitems - 1);
+      if (lane == 0) last = (atomicAdd(&cnt[I.lr], 1) == L.nitems - 1);
       last = __shfl_sync(0xffffffffu, last, 0);
       if (last) {
         __threadfence();
@@ -130,7 +138,7 @@ __global__ void __launch_bounds__(256) p1_kernel(MatDev m, const double* __restr
           for (int p = 0; p < L.nparts; p++) s += __ldcg(&part[L.poff + p * L.kt + k]);
           z[L.zoff + k] = s;
         }
-        if (lane == 0) m.lr_cnt[I.lr] = 0;
+        if (lane == 0) cnt[I.lr] = 0;
       }
     }
   }
@@ -144,18 +152,25 @@ __global__ void __launch_bounds__(256) p1_kernel(MatDev m, const double* __restr
 // slots' partial row sums are combined at the end.  All lanes run the same
 // loop trip counts, so the shuffles are convergent.
 template <typename T>
-__global__ void __launch_bounds__(256, 2) p2_group_kernel(MatDev m, const double* __restrict__ x) {
+__global__ void __launch_bounds__(256, 3) p2_group_kernel(MatDev m0, MatDev m1, int nmat,
+                                                          const double* __restrict__ x) {
   typedef typename AccOf<T>::type Acc;
   constexpr int VEC = 16 / sizeof(T);
   constexpr int UNR = VEC >= 8 ? 2 : 4;
   const int lane = threadIdx.x & 31;
   const int warp = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
   const int nwarps = (int)((gridDim.x * (int64_t)blockDim.x) >> 5);
-  const T* store = (const T*)m.store;
-  const Acc* z = (const Acc*)m.z;
-  Acc* gpart = (Acc*)m.gpart;
-  for (int it = warp; it < m.np2; it += nwarps) {
-    const P2ItemDev I = m.p2[it];
+  const int n0 = m0.np2, ntot = nmat == 2 ? n0 + m1.np2 : n0;
+  for (int it = warp; it < ntot; it += nwarps) {
+    const bool sec = it >= n0;
+    const int32_t* gleaf_ptr = sec ? m1.gleaf_ptr : m0.gleaf_ptr;
+    const int32_t* gleaf = sec ? m1.gleaf : m0.gleaf;
+    const LeafDescDev* desc = sec ? m1.desc : m0.desc;
+    const int32_t* gpoff = sec ? m1.gpoff : m0.gpoff;
+    const T* store = (const T*)(sec ? m1.store : m0.store);
+    const Acc* z = (const Acc*)(sec ? m1.z : m0.z);
+    Acc* gpart = (Acc*)(sec ? m1.gpart : m0.gpart);
+    const P2ItemDev I = (sec ? m1.p2 : m0.p2)[sec ? it - n0 : it];
     const int g = I.group;
     const int nq = (I.nr + VEC - 1) / VEC;
     const int lw = log2ceil32(min(nq, 32));
@@ -166,13 +181,13 @@ __global__ void __launch_bounds__(256, 2) p2_group_kernel(MatDev m, const double
     Acc acc[VEC];
 #pragma unroll
     for (int v = 0; v < VEC; v++) acc[v] = 0;
-    const int e0 = __ldg(&m.gleaf_ptr[g]), e1 = __ldg(&m.gleaf_ptr[g + 1]);
+    const int e0 = __ldg(&gleaf_ptr[g]), e1 = __ldg(&gleaf_ptr[g + 1]);
     for (int base = e0; base < e1; base += 32) {
       const int nl = min(32, e1 - base);
       long long my_off = 0;
       int my_ld = 0, my_kind = 0, my_cnt = 0, my_aux = 0;
       if (lane < nl) {
-        const LeafDescDev* d = m.desc + __ldg(&m.gleaf[base + lane]);
+        const LeafDescDev* d = desc + __ldg(&gleaf[base + lane]);
         my_off = __ldg(&d->off);
         my_ld = __ldg(&d->ndl);
         my_kind = __ldg(&d->kind);
@@ -210,7 +225,7 @@ __global__ void __launch_bounds__(256, 2) p2_group_kernel(MatDev m, const double
     for (int v = 0; v < VEC; v++)
       for (int o = LW; o < 32; o <<= 1) acc[v] += __shfl_xor_sync(0xffffffffu, acc[v], o);
     if (slot == 0 && act) {
-      const int gp = __ldg(&m.gpoff[g]);
+      const int gp = __ldg(&gpoff[g]);
 #pragma unroll
       for (int v = 0; v < VEC; v++)
         if (rr + v < I.r0 + I.nr) gpart[gp + rr + v] = acc[v];
@@ -415,42 +430,50 @@ __global__ void store_convert_kernel(const double* __restrict__ src, int nleaf, 
 // wave), never more than the items need
 template <typename K>
 static int grid_for(K kernel, int sm, int nitems) {
-  static int per_sm = 0;  // one cache per kernel instantiation
-  if (per_sm == 0) {
-    int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, 256, 0) != cudaSuccess || nb < 1) nb = 4;
-    per_sm = nb;
+  // resident blocks per SM, cached per kernel (function address)
+  static std::mutex mu;
+  static std::map<const void*, int> cache;
+  int per_sm;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find((const void*)kernel);
+    if (it == cache.end()) {
+      int nb = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, 256, 0) != cudaSuccess || nb < 1) nb = 2;
+      it = cache.emplace((const void*)kernel, nb).first;
+    }
+    per_sm = it->second;
   }
   const int full = per_sm * sm;
   const int need = (nitems + 7) / 8;
   return need < full ? (need > 0 ? need : 1) : full;
 }
 
-template <typename T>
-static void p1_launch_t(const MatDev& m, const double* x, int sm, cudaStream_t st) {
-  if (m.np1 == 0) return;
-  p1_kernel<T><<<grid_for(p1_kernel<T>, sm, m.np1), 256, 0, st>>>(m, x);
-}
-
+// both H-matrices of a stage in one grid per phase (same storage type)
 void launch_phase1(const MatDev* mats, int nmat, const double* x, int sm, cudaStream_t st) {
-  for (int i = 0; i < nmat; i++) {
-    if (mats[i].storage == ST_F64) p1_launch_t<double>(mats[i], x, sm, st);
-    else if (mats[i].storage == ST_F32) p1_launch_t<float>(mats[i], x, sm, st);
-    else p1_launch_t<__nv_bfloat16>(mats[i], x, sm, st);
-  }
+  const MatDev& m0 = mats[0];
+  const MatDev& m1 = nmat == 2 ? mats[1] : mats[0];
+  const int n = m0.np1 + (nmat == 2 ? m1.np1 : 0);
+  if (n == 0) return;
+  if (m0.storage == ST_F64)
+    p1_kernel<double><<<grid_for(p1_kernel<double>, sm, n), 256, 0, st>>>(m0, m1, nmat, x);
+  else if (m0.storage == ST_F32)
+    p1_kernel<float><<<grid_for(p1_kernel<float>, sm, n), 256, 0, st>>>(m0, m1, nmat, x);
+  else
+    p1_kernel<__nv_bfloat16><<<grid_for(p1_kernel<__nv_bfloat16>, sm, n), 256, 0, st>>>(m0, m1, nmat, x);
 }
 
 void launch_phase2(const MatDev* mats, int nmat, const double* x, int sm, cudaStream_t st) {
-  for (int i = 0; i < nmat; i++) {
-    const MatDev& m = mats[i];
-    if (m.np2 == 0) continue;
-    if (m.storage == ST_F64)
-      p2_group_kernel<double><<<grid_for(p2_group_kernel<double>, sm, m.np2), 256, 0, st>>>(m, x);
-    else if (m.storage == ST_F32)
-      p2_group_kernel<float><<<grid_for(p2_group_kernel<float>, sm, m.np2), 256, 0, st>>>(m, x);
-    else
-      p2_group_kernel<__nv_bfloat16><<<grid_for(p2_group_kernel<__nv_bfloat16>, sm, m.np2), 256, 0, st>>>(m, x);
-  }
+  const MatDev& m0 = mats[0];
+  const MatDev& m1 = nmat == 2 ? mats[1] : mats[0];
+  const int n = m0.np2 + (nmat == 2 ? m1.np2 : 0);
+  if (n == 0) return;
+  if (m0.storage == ST_F64)
+    p2_group_kernel<double><<<grid_for(p2_group_kernel<double>, sm, n), 256, 0, st>>>(m0, m1, nmat, x);
+  else if (m0.storage == ST_F32)
+    p2_group_kernel<float><<<grid_for(p2_group_kernel<float>, sm, n), 256, 0, st>>>(m0, m1, nmat, x);
+  else
+    p2_group_kernel<__nv_bfloat16><<<grid_for(p2_group_kernel<__nv_bfloat16>, sm, n), 256, 0, st>>>(m0, m1, nmat, x);
 }
 
 void launch_phase3_plain(const MatDev* mats, int nmat, double* const* y, cudaStream_t st) {

@@ -36,6 +36,8 @@ EXPORTS = [
     "hbi_rk_get_state", "hbi_derivs", "hbi_rkck", "hbi_rkqs", "hbi_rk_launches_per_attempt",
     "hbi_cluster_structure", "hbi_rk_stream", "hbi_rk_attempt_async", "hbi_set_device",
     "hbi_adot_lattice_hyp_phase_dev", "hbi_lh_phase_bytes", "hbi_adot_lattice_hyp_noalloc",
+    "hbi_cycle_create", "hbi_cycle_run", "hbi_cycle_fields", "hbi_cycle_events", "hbi_cycle_trace",
+    "hbi_cycle_free", "hbi_cycle_set_proposer", "hbi_cycle_proposer_size",
 ]
 
 
@@ -57,6 +59,34 @@ class Bemv(C.Structure):
                                       "ev12", "ev13", "ev21", "ev22", "ev23", "ev31", "ev32", "ev33")])
 
 
+class CycleParams(C.Structure):
+    """hbi_cycle_params: the time-loop controls of main_LH.f90 (:133-160, :330-332)."""
+    _fields_ = ([(f, C.c_double) for f in ("eps_r", "dtinit", "dtmax", "tmax", "velth", "velmax", "velmin",
+                                           "dtout_inter", "dtout_co", "rigid")]
+                + [("nstep", C.c_longlong), ("interval", C.c_longlong), ("number", C.c_int), ("inflight", C.c_int),
+                   ("pad0", C.c_int), ("pad1", C.c_int), ("outdir", C.c_char_p)])
+
+
+class CycleStatus(C.Structure):
+    _fields_ = ([("k", C.c_longlong), ("attempts", C.c_longlong), ("rejected", C.c_longlong)]
+                + [(f, C.c_double) for f in ("x", "hnext", "errmax", "dtdid", "mvel", "meanslip", "meanmu",
+                                             "maxnorm", "minnorm")]
+                + [(f, C.c_int) for f in ("nrjct", "events", "slipping", "stop")]
+                + [("wall_s", C.c_double)])
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class Event(C.Structure):
+    _fields_ = [("id", C.c_int), ("hypoloc", C.c_int), ("k", C.c_longlong), ("onset", C.c_double),
+                ("end", C.c_double), ("moment", C.c_double), ("mw", C.c_double)]
+
+
+STOP_NAMES = {0: "none", 1: "tmax", 2: "velmax", 3: "velmin", 4: "klimit", 5: "underflow", 6: "tlimit"}
+YEAR = 365 * 24 * 3600.0
+
+
 class RsfParams(C.Structure):
     _fields_ = ([("ncell", C.c_int), ("evlaw", C.c_int), ("backslip", C.c_int), ("limitsigma", C.c_int),
                  ("vref", C.c_double), ("minsig", C.c_double), ("maxsig", C.c_double),
@@ -76,10 +106,10 @@ def _register(obj, rank):
 
 @atexit.register
 def _teardown():
-    """Free live handles before the CUDA runtime goes away: RK states first,
-    then operators, filled H-matrices and control blocks."""
+    """Free live handles before the CUDA runtime goes away: time loops first,
+    then RK states, operators, filled H-matrices and control blocks."""
     global _closed
-    for rank in (0, 1, 2, 3):
+    for rank in (0, 1, 2, 3, 4):
         for obj in list(_live.values()):
             if getattr(obj, "_rank", -1) == rank:
                 obj.close()
@@ -144,7 +174,7 @@ class Ctl:
         self.h = C.c_void_p()
         _check(lib().hbi_init(int(nd), C.byref(self.h)), "hbi_init")
         self.nd = nd
-        _register(self, 3)
+        _register(self, 4)
 
     @property
     def param(self):
@@ -179,7 +209,7 @@ class LeafMtxp:
         coord = geom.coord().ravel(order="F")
         _check(lib().hbi_generate(C.byref(self.h), C.byref(geom.bemv), ctl.h, _p(coord), C.c_double(ztol)),
                "hbi_generate")
-        _register(self, 2)
+        _register(self, 3)
 
     def leaves(self):
         n, km = C.c_int(), C.c_int()
@@ -214,7 +244,7 @@ class LHp:
         self.ctl, self.h, self.storage = ctl, C.c_void_p(), storage
         _check(lib().hbi_construct_lh(C.byref(self.h), lf.h, ctl.h, int(storage)), "hbi_construct_lh")
         self.n = ctl.nd
-        _register(self, 1)
+        _register(self, 2)
 
     def matvec(self, u):
         """HACApK_adot_lattice_hyp: au = H u (cluster order, host arrays)."""
@@ -315,7 +345,7 @@ class RK:
         _check(lib().hbi_rk_create(C.byref(self.h), C.byref(p), lh_s.h, lh_n.h if lh_n is not None else None),
                "hbi_rk_create")
         self.n, self.lh = n, (lh_s, lh_n)
-        _register(self, 0)
+        _register(self, 1)
 
     def set_state(self, y):
         y = np.ascontiguousarray(y, dtype=np.float64)
@@ -371,3 +401,85 @@ class RK:
 
     def __del__(self):
         self.close()
+
+
+class Cycle:
+    """The time loop of main_LH.f90 (:1217-1438) on the device: rkqs, slip
+    update, monitors, events, field output and stop controls.
+
+    Reference defaults (main_LH.f90:133-160): velth=1e-2 and vref=1e-6 are
+    default-real literals there, so they are widened from float32 here too.
+    """
+
+    def __init__(self, rk, vel, ds, eps_r=1e-4, dtinit=1.0, dtmax=1e10, tmax_yr=1e4,
+                 velth=float(np.float32(1e-2)), velmax=1e7, velmin=1e-20, dtout_yr=1.0, dtout_co=1000.0,
+                 rigid=32.04, nstep=1000000, interval=0, number=0, outdir=None, inflight=4):
+        p = CycleParams()
+        p.eps_r, p.dtinit, p.dtmax, p.tmax = eps_r, dtinit, dtmax, tmax_yr * YEAR
+        p.velth, p.velmax, p.velmin = velth, velmax, velmin
+        p.dtout_inter, p.dtout_co, p.rigid = dtout_yr * YEAR, dtout_co, rigid
+        p.nstep, p.interval, p.number, p.inflight = nstep, interval, number, inflight
+        self._outdir = outdir.encode() if outdir else None
+        p.outdir = self._outdir
+        vel = np.ascontiguousarray(vel, dtype=np.float64)
+        ds = np.ascontiguousarray(ds, dtype=np.float64)
+        self.h = C.c_void_p()
+        _check(lib().hbi_cycle_create(C.byref(self.h), rk.h, _p(vel), _p(ds), C.byref(p)), "hbi_cycle_create")
+        self.rk, self.n = rk, rk.n
+        _register(self, 0)
+
+    def run(self, k_limit=0, t_limit=0.0):
+        """Run until a stop control, k == k_limit (>0) or x == t_limit (>0, s)."""
+        st = CycleStatus()
+        _check(lib().hbi_cycle_run(self.h, C.c_longlong(int(k_limit)), C.c_double(t_limit), C.byref(st)),
+               "hbi_cycle_run")
+        d = st.as_dict()
+        d["stop_name"] = STOP_NAMES.get(d["stop"], "?")
+        return d
+
+    def fields(self):
+        vel, slip = np.zeros(self.n), np.zeros(self.n)
+        _check(lib().hbi_cycle_fields(self.h, _p(vel), _p(slip)), "hbi_cycle_fields")
+        return vel, slip
+
+    def events(self):
+        cnt = C.c_int()
+        _check(lib().hbi_cycle_events(self.h, None, 0, C.byref(cnt)), "hbi_cycle_events")
+        arr = (Event * max(1, cnt.value))()
+        _check(lib().hbi_cycle_events(self.h, arr, cnt.value, C.byref(cnt)), "hbi_cycle_events")
+        return [{f: getattr(arr[i], f) for f, _ in Event._fields_} for i in range(cnt.value)]
+
+    def trace(self):
+        """Per attempt: k, x, h, errmax, accepted, mvel, hnext, nrjct."""
+        cnt = C.c_longlong()
+        _check(lib().hbi_cycle_trace(self.h, None, 0, C.byref(cnt)), "hbi_cycle_trace")
+        out = np.zeros((cnt.value, 8))
+        if cnt.value:
+            _check(lib().hbi_cycle_trace(self.h, _p(out), cnt.value, C.byref(cnt)), "hbi_cycle_trace")
+        return out
+
+    def set_proposer(self, w):
+        """Learned step-size proposer weights (float32 vector), or None to turn it off."""
+        if w is None:
+            _check(lib().hbi_cycle_set_proposer(self.h, None), "hbi_cycle_set_proposer")
+            return
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        nin, hid, nf = proposer_size()
+        if w.size != nf:
+            raise ValueError(f"proposer weights: {w.size} floats, expected {nf}")
+        _check(lib().hbi_cycle_set_proposer(self.h, w.ctypes.data_as(C.POINTER(C.c_float))), "hbi_cycle_set_proposer")
+
+    def close(self):
+        if getattr(self, "h", None) and _lib is not None and not _closed:
+            _lib.hbi_cycle_free(self.h)
+        self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+def proposer_size():
+    """(inputs, hidden width, floats in the weight vector) of the step-size proposer."""
+    a, b, c = C.c_int(), C.c_int(), C.c_int()
+    _check(lib().hbi_cycle_proposer_size(C.byref(a), C.byref(b), C.byref(c)), "hbi_cycle_proposer_size")
+    return a.value, b.value, c.value

@@ -877,6 +877,21 @@ extern "C" int hbi_rk_free(hbi_rk* r) {
 
 extern "C" int hbi_rk_launches_per_attempt(const hbi_rk* r) { return r ? r->launches : 0; }
 
+namespace hbi {
+// for the device-resident time loop (hbi_cycle.cu)
+int rk_view(hbi_rk* r, RkView* v) {
+  if (!r || !v) return fail(HBI_ERR_ARG, "null");
+  v->R = r->R;
+  v->mats[0] = r->mats[0];
+  v->mats[1] = r->mats[r->nmat == 2 ? 1 : 0];
+  v->nmat = r->nmat;
+  v->n = r->n;
+  v->sm = r->ls->ctl->sm_count;
+  return HBI_OK;
+}
+int set_error(int code, const char* msg) { return fail(code, "%s", msg); }
+}  // namespace hbi
+
 extern "C" int hbi_rk_set_state(hbi_rk* r, const double* y) {
   if (!r || !y) return fail(HBI_ERR_ARG, "null");
   CK(cudaMemcpy(r->R.y, y, sizeof(double) * 3 * r->n, cudaMemcpyHostToDevice));

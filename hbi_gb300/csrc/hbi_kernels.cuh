@@ -78,6 +78,7 @@ struct MatDev {            // one H-matrix on the device
   void* gpart;             // per-group row partials (Acc type)
   const int32_t *row_fc, *fc_ptr, *fc_group;
   double scale;            // result multiplier (1/ds0 for 3dph, else 1)
+  const int* skip;         // when non-null and nonzero, phases 1-2 do nothing
 };
 
 // RK (Cash-Karp) stage state on the device; all arrays in cluster order
@@ -95,6 +96,16 @@ struct RkDev {
   double* yerr;    // embedded error (3n)
   double* ebuf;    // |yerr/yout|/eps per component (3n)
   double* ctl;     // [0]=h [1]=eps  [2]=emax (as bits) [3]=huge index (as int64)
+  // time-loop flags (null outside the device-resident loop): [0] halted,
+  // [1] halted or retrying, [2] retrying the same state (stage 1 is reused)
+  const int* flags;
+};
+
+// host view of an RK handle, for the device-resident time loop (hbi_cycle.cu)
+struct RkView {
+  RkDev R;
+  MatDev mats[2];
+  int nmat, n, sm;
 };
 
 // phase 1: z = V^T x; phase 2: per-group row partials of U z + A x;

@@ -75,6 +75,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) p1_kernel(MatDev m0, MatDev m1, int nmat, const double* __restrict__ x) {
   typedef typename AccOf<T>::type Acc;
   constexpr int VEC = 16 / sizeof(T);
+  if (m0.skip && __ldcg(m0.skip)) return;
   const int lane = threadIdx.x & 31;
   const int warp = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
   const int nwarps = (int)((gridDim.x * (int64_t)blockDim.x) >> 5);
@@ -157,6 +158,7 @@ __global__ void __launch_bounds__(256, 3) p2_group_kernel(MatDev m0, MatDev m1, 
   typedef typename AccOf<T>::type Acc;
   constexpr int VEC = 16 / sizeof(T);
   constexpr int UNR = VEC >= 8 ? 2 : 4;
+  if (m0.skip && __ldcg(m0.skip)) return;
   const int lane = threadIdx.x & 31;
   const int warp = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
   const int nwarps = (int)((gridDim.x * (int64_t)blockDim.x) >> 5);
@@ -290,18 +292,25 @@ __device__ __forceinline__ double slip_rate(double vref, double psi, double tau,
 }
 
 __global__ void __launch_bounds__(128) p3_rk_kernel(MatDev m0, MatDev m1, RkDev R, int s, double* __restrict__ xnext) {
+  if (R.flags && __ldcg(&R.flags[0])) return;
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   double emax = -1.0;
   long long hidx = -1;
   if (r < R.n) {
-    const double gs = row_value(m0, r) + R.taudot[r];
-    const double gn = (R.nmat == 2 ? row_value(m1, r) : 0.0) + R.sigdot[r];
     const int n3 = 3 * R.n;
-    const double psi = R.ys[3 * r], tau = R.ys[3 * r + 1], sig = R.ys[3 * r + 2];
     double k[3];
-    deriv_dev(R, gs, gn, psi, tau, sig, R.vs[r], R.a[r], R.b[r], R.dc[r], R.f0[r], k);
     double* Ks = R.K + (size_t)s * n3 + 3 * r;
-    Ks[0] = k[0]; Ks[1] = k[1]; Ks[2] = k[2];
+    if (s == 0 && R.flags && __ldcg(&R.flags[2])) {
+      // a retried attempt from the same state: k1 = f(y) is the one the
+      // rejected attempt stored (its phases 1-2 were skipped)
+      k[0] = Ks[0]; k[1] = Ks[1]; k[2] = Ks[2];
+    } else {
+      const double gs = row_value(m0, r) + R.taudot[r];
+      const double gn = (R.nmat == 2 ? row_value(m1, r) : 0.0) + R.sigdot[r];
+      const double psi = R.ys[3 * r], tau = R.ys[3 * r + 1], sig = R.ys[3 * r + 2];
+      deriv_dev(R, gs, gn, psi, tau, sig, R.vs[r], R.a[r], R.b[r], R.dc[r], R.f0[r], k);
+      Ks[0] = k[0]; Ks[1] = k[1]; Ks[2] = k[2];
+    }
     const double h = R.ctl[0];
     const double* K0 = R.K + 3 * r;
     if (s < 5) {
@@ -367,6 +376,7 @@ __global__ void __launch_bounds__(128) p3_rk_kernel(MatDev m0, MatDev m1, RkDev 
 // start of an attempt: stage state = accepted state, its slip rate and the
 // stage-0 matvec input; clear the attempt's error accumulators
 __global__ void rk_prepare_kernel(RkDev R) {
+  if (R.flags && __ldcg(&R.flags[0])) return;
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r == 0) {
     R.ctl[2] = 0.0;

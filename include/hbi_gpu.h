@@ -188,6 +188,82 @@ void* hbi_rk_stream(const hbi_rk* rk);
  * synchronisation or copy; the error estimate stays on the device */
 int hbi_rk_attempt_async(hbi_rk* rk, double h, double eps);
 
+/* ---- time loop on the device (main_LH.f90:1217-1434) ----------------------
+ * The reference's loop `do k=kstart,NSTEP`: rkqs, the per-step update of
+ * slip and slip rate (:1266-1287), the monitors (:1291-1336), event detection
+ * (:1338-1388), field output (:1391-1412) and the stop controls (:1425-1438).
+ * Every decision runs on the GPU; the host enqueues attempts ahead of time and
+ * drains one small record per attempt (plus field snapshots when the loop
+ * writes fields) into the reference's output files:
+ *   monitor<number>.dat, time<number>.dat, event<number>.dat (text) and
+ *   vel/slip/sigma/tau/EQslip<number>.dat (stream binary, cluster order). */
+typedef struct hbi_cycle_s hbi_cycle;
+typedef struct {
+  double eps_r;        /* RK tolerance */
+  double dtinit;       /* first trial step (s) */
+  double dtmax;        /* s */
+  double tmax;         /* s (the reference converts its years at :330) */
+  double velth, velmax, velmin;
+  double dtout_inter;  /* s */
+  double dtout_co;     /* s */
+  double rigid;        /* rigidity of the event magnitude (m_const.f90) */
+  long long nstep;     /* NSTEP */
+  long long interval;  /* field output every `interval` steps; 0 = NSTEP */
+  int number;          /* output file number */
+  int inflight;        /* attempts enqueued ahead of the host, 1..16 */
+  int pad0, pad1;
+  const char* outdir;  /* directory for the output files; NULL = no files */
+} hbi_cycle_params;
+
+#define HBI_STOP_NONE 0
+#define HBI_STOP_TMAX 1      /* x > tmax */
+#define HBI_STOP_VELMAX 2    /* max slip rate > velmax */
+#define HBI_STOP_VELMIN 3    /* max slip rate < velmin */
+#define HBI_STOP_KLIMIT 4    /* k reached the run's step limit (resumable) */
+#define HBI_STOP_UNDERFLOW 5 /* rkqs step size underflow (reference: stop) */
+#define HBI_STOP_TLIMIT 6    /* x reached the run's time limit exactly (resumable) */
+
+typedef struct {
+  long long k, attempts, rejected;
+  double x, hnext, errmax, dtdid;
+  double mvel, meanslip, meanmu, maxnorm, minnorm;
+  int nrjct, events, slipping, stop;
+  double wall_s;       /* host wall time of the run call */
+} hbi_cycle_status;
+
+typedef struct {
+  int id, hypoloc;     /* event number; 1-based cluster-order index of max slip rate at onset */
+  long long k;         /* step at which the event ended */
+  double onset, end;   /* s */
+  double moment;       /* mean slip of the event (m) */
+  double mw;           /* (log10(moment*rigid*sg)+5.9)/1.5 as event*.dat */
+} hbi_event;
+
+/* Starts a loop from the RK handle's current state (hbi_rk_set_state), with
+ * slip rate vel (ncell, cluster order: the reference's `vel` before the loop)
+ * and element areas ds (ncell, cluster order: ds(lodc(i))).  Writes the k=0
+ * outputs.  The RK handle must outlive the loop. */
+int hbi_cycle_create(hbi_cycle** c, hbi_rk* rk, const double* vel, const double* ds, const hbi_cycle_params* p);
+/* Runs until a stop control fires, until k reaches k_limit (<=0: none) or x
+ * reaches t_limit (<=0: none; the last step is shortened to land on it). */
+int hbi_cycle_run(hbi_cycle* c, long long k_limit, double t_limit, hbi_cycle_status* st);
+/* slip and slip rate (ncell, cluster order); the state y via hbi_rk_get_state */
+int hbi_cycle_fields(hbi_cycle* c, double* vel, double* slip);
+/* finished events so far; *count = their number (up to max are copied) */
+int hbi_cycle_events(hbi_cycle* c, hbi_event* ev, int max, int* count);
+/* per attempt: k, x, h, errmax, accepted, mvel, hnext, nrjct (8 doubles each) */
+int hbi_cycle_trace(hbi_cycle* c, double* rec, long long max, long long* count);
+int hbi_cycle_free(hbi_cycle* c);
+/* Learned step-size proposer (no reference counterpart).  After each accepted
+ * step an MLP (nin -> hid -> hid -> 1, tanh) maps the loop's history to
+ * d = log10(h_next / rkqs h_next), clamped to [lo, hi]; the next attempt uses
+ * rkqs's h_next * 10^d.  The rkqs error test still judges every attempt and
+ * its shrink rule still handles every rejection.  w (floats, layout
+ * W1[hid][nin] b1 W2[hid][hid] b2 W3[hid] b3 mean[nin] sd[nin] lo hi) is
+ * copied; NULL turns the proposer off. */
+int hbi_cycle_set_proposer(hbi_cycle* c, const float* w);
+int hbi_cycle_proposer_size(int* nin, int* hid, int* nfloats);
+
 #ifdef __cplusplus
 }
 #endif

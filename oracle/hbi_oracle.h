@@ -131,6 +131,17 @@ double orc_errmax(int len, const double* yerr, const double* ytemp, double eps);
 void orc_step_update(const orc_rsf* p, const double* y, double dtdid, double* psi,
                      double* tau, double* sigma, double* slip, double* vel, double* mu);
 
+/* the time loop of main_LH.f90:1217-1438 (no output files) */
+typedef struct {
+  double eps_r, dtinit, dtmax, tmax, velth, velmax, velmin, dtout_inter, dtout_co;
+  long long interval, nstep;
+} orc_cycle_params;
+#define ORC_CYCLE_REC 12
+#define ORC_CYCLE_EV 6
+int orc_cycle(const orc_rsf* p, const orc_cycle_params* cp, double* y, double* vel, double* slip,
+              const double* ds, long long nsteps, double* rec, long long* nrec, double* ev, int max_ev,
+              int* nev);
+
 /* Cash-Karp tableau as the reference's parameter statements produce it */
 void orc_cashkarp(double* a6, double* b15, double* c6, double* dc6);
 /* rkqs constants: SAFETY, PGROW, PSHRNK, tiny */

@@ -311,6 +311,34 @@ class RSF:
         return psi, tau, sig, slip, vel, mu
 
 
+class CycleParams(C.Structure):
+    _fields_ = ([(f, C.c_double) for f in ("eps_r", "dtinit", "dtmax", "tmax", "velth", "velmax", "velmin",
+                                           "dtout_inter", "dtout_co")]
+                + [("interval", C.c_longlong), ("nstep", C.c_longlong)])
+
+
+def cycle(rsf, y, vel, ds, nsteps, eps_r=1e-4, dtinit=1.0, dtmax=1e10, tmax_yr=1e4,
+          velth=float(np.float32(1e-2)), velmax=1e7, velmin=1e-20, dtout_yr=1.0, dtout_co=1000.0, interval=0,
+          nstep=1000000, max_events=10000):
+    """The time loop of main_LH.f90:1217-1438 (no files).  Returns (stop,
+    records[k, x, hdid, errmax, nrjct, mvel, loc, meanslip, meanmu, maxnorm,
+    minnorm, outfield], events[id, k, onset, moment, hypoloc, x], y, vel, slip)."""
+    year = 365 * 24 * 3600.0
+    cp = CycleParams(eps_r, dtinit, dtmax, tmax_yr * year, velth, velmax, velmin, dtout_yr * year, dtout_co,
+                     interval, nstep)
+    n = rsf.n
+    y = np.array(y, dtype=np.float64)
+    vel = np.array(vel, dtype=np.float64)
+    slip = np.zeros(n)
+    ds = np.ascontiguousarray(ds, dtype=np.float64)
+    rec = np.zeros((nsteps, 12))
+    ev = np.zeros((max_events, 6))
+    nrec, nev = C.c_longlong(), C.c_int()
+    stop = lib().orc_cycle(C.byref(rsf.r), C.byref(cp), _p(y), _p(vel), _p(slip), _p(ds), C.c_longlong(nsteps),
+                           _p(rec), C.byref(nrec), _p(ev), C.c_int(max_events), C.byref(nev))
+    return stop, rec[:nrec.value], ev[:min(nev.value, max_events)], y, vel, slip
+
+
 def mlp_loss_grad(nin, h, params, x, target):
     params = np.ascontiguousarray(params, dtype=np.float32)
     x = np.ascontiguousarray(x, dtype=np.float32)

@@ -315,3 +315,79 @@ double orc_mlp_loss_grad(int nin, int h, int batch, const float* P, const float*
   free(g); free(a1); free(a2); free(d1); free(d2);
   return loss / batch;
 }
+
+/* The time loop of main_LH.f90:1217-1438 without its output files: rkqs, the
+ * step update (:1266-1287), the monitors (:1291-1336), the event list
+ * (:1338-1388) and the stop controls (:1425-1438), for at most nsteps steps.
+ * Per accepted step one record of ORC_CYCLE_REC doubles
+ *   k, x, hdid, errmax, nrjct, mvel, loc (0-based maxloc of |vel|), meanslip,
+ *   meanmu, maxnorm, minnorm, outfield
+ * and per finished event ORC_CYCLE_EV doubles
+ *   eventcount, k, onset_time, moment, hypoloc, x.
+ * Returns the stop code (0 none, 1 tmax, 2 velmax, 3 velmin, 4 step limit,
+ * 5 step size underflow).  y, slip and vel carry the loop state in and out. */
+int orc_cycle(const orc_rsf* p, const orc_cycle_params* cp, double* y, double* vel, double* slip,
+              const double* ds, long long nsteps, double* rec, long long* nrec, double* ev, int max_ev,
+              int* nev) {
+  const int n = p->n;
+  double* psi = (double*)malloc(sizeof(double) * n);
+  double* tau = (double*)malloc(sizeof(double) * n);
+  double* sig = (double*)malloc(sizeof(double) * n);
+  double* mu = (double*)malloc(sizeof(double) * n);
+  double* islip = (double*)calloc(n, sizeof(double));
+  double sg = 0.0;
+  for (int i = 0; i < n; i++) sg += ds[i];
+  double x = 0.0, dtnxt = cp->dtinit, dtout = cp->dtout_inter, tout = dtout, moment0 = 0.0, onset = 0.0;
+  int slipping = 0, eventcount = 0, hypoloc = 0, stop = 0;
+  long long interval = cp->interval > 0 ? cp->interval : cp->nstep;
+  *nrec = 0;
+  *nev = 0;
+  for (long long k = 1; k <= nsteps; k++) {
+    double dtdid, errmax;
+    int nrjct;
+    if (orc_rkqs(p, y, &x, dtnxt, cp->eps_r, cp->dtmax, &dtdid, &dtnxt, &errmax, &nrjct)) {
+      stop = 5;
+      break;
+    }
+    orc_step_update(p, y, dtdid, psi, tau, sig, slip, vel, mu);
+    double mvel = -1.0, maxnorm = -INFINITY, minnorm = INFINITY, meanslip = 0.0, meanmu = 0.0;
+    int loc = 0;
+    for (int i = 0; i < n; i++) {
+      if (fabs(vel[i]) > mvel) { mvel = fabs(vel[i]); loc = i; }
+      if (sig[i] > maxnorm) maxnorm = sig[i];
+      if (sig[i] < minnorm) minnorm = sig[i];
+      meanslip += fabs(slip[i]) * ds[i];
+      meanmu += mu[i] * ds[i];
+    }
+    meanslip /= sg;
+    meanmu /= sg;
+    int outfield = 0;
+    if (!slipping && mvel > cp->velth) {
+      outfield = 1; slipping = 1; dtout = cp->dtout_co; tout = x + dtout; eventcount++;
+      moment0 = meanslip;
+      memcpy(islip, slip, sizeof(double) * n);
+      hypoloc = loc + 1;
+      onset = x;
+    }
+    if (slipping && mvel < 0.5 * cp->velth) {
+      outfield = 1; slipping = 0; dtout = cp->dtout_inter; tout = x + dtout;
+      if (*nev < max_ev) {
+        double* e = ev + (size_t)(*nev) * ORC_CYCLE_EV;
+        e[0] = eventcount; e[1] = (double)k; e[2] = onset; e[3] = meanslip - moment0; e[4] = hypoloc; e[5] = x;
+      }
+      (*nev)++;
+    }
+    if (k % interval == 0) outfield = 1;
+    if (x > tout) { outfield = 1; tout = x + dtout; }
+    double* r = rec + (size_t)(*nrec) * ORC_CYCLE_REC;
+    r[0] = (double)k; r[1] = x; r[2] = dtdid; r[3] = errmax; r[4] = nrjct; r[5] = mvel; r[6] = loc;
+    r[7] = meanslip; r[8] = meanmu; r[9] = maxnorm; r[10] = minnorm; r[11] = outfield;
+    (*nrec)++;
+    if (mvel > cp->velmax) { stop = 2; break; }
+    if (mvel < cp->velmin) { stop = 3; break; }
+    if (x > cp->tmax) { stop = 1; break; }
+    if (k == nsteps) stop = 4;
+  }
+  free(psi); free(tau); free(sig); free(mu); free(islip);
+  return stop;
+}

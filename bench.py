@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", default="step", choices=["step", "matvec"])
+    ap.add_argument("--window-yr", type=float, default=100.0,
+                    help="simulated window of the sim-yr/h comparison (0: skip it)")
     return ap.parse_args()
 
 
@@ -98,6 +100,64 @@ class Clocks:
                 pass
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx or None,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# DRAM bytes (read + write) per launch of the phase kernels on the c2 shear
+# H-matrix, from the ncu capture summarised in
+# profiles/matvec_p1_p2_c2_256x256_f32.md (FP32 store)
+NCU_TRAFFIC = {"f32": {"phase1": 334.6e6, "phase2": 378.1e6}}
+
+
+def run_cycles(args, w, lf_s, lf_n, ctl_s, ctl_n, lodc, y0, p):
+    """sim-yr/h of the time loop over [0, window]: the plain FP64 form (FP64
+    factors, rkqs controller) against the mixed form (--store factors,
+    learned step-size proposer trained on the plain run's own trace), with
+    the relative error of the mixed run's slip field at the window's end and
+    of its event onset times."""
+    import hbi_gb300 as H
+    from hbi_gb300 import proposer
+    ds = w.ds_area[lodc - 1]
+    T = args.window_yr * H.YEAR
+
+    def one(store, wts=None):
+        lh_s = H.LHp(lf_s, ctl_s, store)
+        lh_n = H.LHp(lf_n, ctl_n, store)
+        rk = H.RK(lh_s, lh_n, evlaw=w.evlaw, scale=w.scale, a=p["a"], b=p["b"], dc=p["dc"], f0=p["f0"],
+                  vpl=p["vpl"])
+        rk.set_state(y0)
+        c = H.Cycle(rk, p["vel"], ds, eps_r=1e-6, tmax_yr=w.tmax_yr)
+        if wts is not None:
+            c.set_proposer(wts)
+        st = c.run(t_limit=T)
+        out = dict(st=st, trace=c.trace(), events=c.events(), slip=c.fields()[1])
+        c.close(); rk.close(); lh_s.close(); lh_n.close()
+        return out
+
+    plain = one("f64")
+    X, Tt = proposer.training_set(plain["trace"])
+    t0 = time.perf_counter()
+    wts, hist = proposer.train(X, Tt, epochs=30)
+    t_train = time.perf_counter() - t0
+    mixed = one(args.store, wts)
+    rate = lambda r: r["st"]["x"] / H.YEAR / r["st"]["wall_s"] * 3600.0
+    slip_err = float(np.linalg.norm(mixed["slip"] - plain["slip"]) / np.linalg.norm(plain["slip"]))
+    on_p = [e["onset"] for e in plain["events"]]
+    on_m = [e["onset"] for e in mixed["events"]]
+    onset_err = (max(abs(a - b) / b for a, b in zip(on_m, on_p)) if on_p and len(on_p) == len(on_m) else None)
+    rj = lambda r: r["st"]["rejected"] / max(1, r["st"]["attempts"])
+    return {
+        "unit": "simulated yr/hour", "window_yr": args.window_yr,
+        "plain_fp64": round(rate(plain), 1), "mixed": round(rate(mixed), 1),
+        "ratio": round(rate(mixed) / rate(plain), 3),
+        "mixed_form": f"{args.store} factors + learned step-size proposer (trained on the plain run's trace, "
+                      f"{len(Tt)} samples, {t_train:.1f} s on the GPU)",
+        "plain_form": "f64 factors, rkqs controller, same kernels and device-resident loop",
+        "slip_rel_err_at_window_end": slip_err, "onset_rel_err_max": onset_err,
+        "events": [len(on_p), len(on_m)],
+        "attempts": [plain["st"]["attempts"], mixed["st"]["attempts"]],
+        "rejected_frac": [round(rj(plain), 4), round(rj(mixed), 4)],
+        "wall_s": [round(plain["st"]["wall_s"], 2), round(mixed["st"]["wall_s"], 2)],
+    }
 
 
 def dist_init(args):
@@ -238,6 +298,11 @@ def run_ours(args):
         te = float(tt.item())
     e2e = world * args.steps * bytes_attempt / te / 1e9
 
+    # ---- sim-yr/h: plain FP64 form against the mixed + learned form ----
+    cyc = None
+    if rank == 0 and args.window_yr > 0:
+        cyc = run_cycles(args, w, lf_s, lf_n, ctl_s, ctl_n, lodc, y0, p)
+
     # ---- CPU baseline: the oracle port on the host cores (rank 0, N=1) ----
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -256,7 +321,10 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
             "roofline": {"bound": "hbm", "kernel": f"matvec {dominant}", "achieved": round(ach, 1),
                          "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4), "peak_kind": peak_kind,
-                         "traffic": None, "matvec_gbs_both_phases": round(mv_gbs, 1),
+                         "traffic": NCU_TRAFFIC.get(args.store, {}).get(dominant),
+                         "traffic_source": "ncu dram bytes per launch (profiles/matvec_p1_p2_c2_256x256_f32.md)"
+                                           if args.store in NCU_TRAFFIC else None,
+                         "matvec_gbs_both_phases": round(mv_gbs, 1),
                          "phase1_us": round(t1 * 1e6, 2), "phase2_us": round(t2 * 1e6, 2),
                          "phase1_bytes": b1, "phase2_bytes": b2},
             "e2e": {"value": round(e2e, 2), "unit": "GB/s", "h2d_bytes_per_step": 3 * n * 8,
@@ -269,6 +337,8 @@ def run_ours(args):
         }
         if cpu:
             d["cpu_baseline"] = cpu
+        if cyc:
+            d["sim_yr_per_hour"] = cyc
         out_line(d)
     if world > 1:
         dist.destroy_process_group()

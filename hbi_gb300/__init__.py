@@ -38,6 +38,8 @@ EXPORTS = [
     "hbi_adot_lattice_hyp_phase_dev", "hbi_lh_phase_bytes", "hbi_adot_lattice_hyp_noalloc",
     "hbi_cycle_create", "hbi_cycle_run", "hbi_cycle_fields", "hbi_cycle_events", "hbi_cycle_trace",
     "hbi_cycle_free", "hbi_cycle_set_proposer", "hbi_cycle_proposer_size",
+    "hbi_mlp_create", "hbi_mlp_free", "hbi_mlp_set_params", "hbi_mlp_get_params", "hbi_mlp_loss_grad",
+    "hbi_mlp_train", "hbi_mlp_predict",
 ]
 
 
@@ -483,3 +485,77 @@ def proposer_size():
     a, b, c = C.c_int(), C.c_int(), C.c_int()
     _check(lib().hbi_cycle_proposer_size(C.byref(a), C.byref(b), C.byref(c)), "hbi_cycle_proposer_size")
     return a.value, b.value, c.value
+
+
+_fp = C.POINTER(C.c_float)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class MLP:
+    """nin -> hid -> hid -> 1 MLP trained on the GPU by the library's own
+    forward/backward/Adam kernels (hbi_mlp_*)."""
+
+    def __init__(self, nin, hid, batch_max=4096):
+        self.nin, self.hid = nin, hid
+        self.np = hid * nin + hid + hid * hid + hid + hid + 1
+        self.h = C.c_void_p()
+        _check(lib().hbi_mlp_create(C.byref(self.h), nin, hid, batch_max), "hbi_mlp_create")
+        _register(self, 0)
+
+    def init(self, seed=0):
+        """Glorot-uniform weights, zero biases."""
+        rng = np.random.default_rng(seed)
+        p = np.zeros(self.np, dtype=np.float32)
+        nin, h = self.nin, self.hid
+        o = 0
+        for fan_in, fan_out in ((nin, h), (h, h), (h, 1)):
+            lim = np.sqrt(6.0 / (fan_in + fan_out))
+            p[o:o + fan_in * fan_out] = rng.uniform(-lim, lim, fan_in * fan_out)
+            o += fan_in * fan_out + fan_out
+        self.set_params(p)
+        return p
+
+    def set_params(self, p):
+        p = _f32(p)
+        _check(lib().hbi_mlp_set_params(self.h, p.ctypes.data_as(_fp)), "hbi_mlp_set_params")
+
+    def params(self):
+        p = np.zeros(self.np, dtype=np.float32)
+        _check(lib().hbi_mlp_get_params(self.h, p.ctypes.data_as(_fp)), "hbi_mlp_get_params")
+        return p
+
+    def loss_grad(self, x, t):
+        x, t = _f32(x), _f32(t)
+        g = np.zeros(self.np, dtype=np.float32)
+        out = np.zeros(len(t), dtype=np.float32)
+        loss = C.c_float()
+        _check(lib().hbi_mlp_loss_grad(self.h, x.ctypes.data_as(_fp), t.ctypes.data_as(_fp), len(t),
+                                       g.ctypes.data_as(_fp), C.byref(loss), out.ctypes.data_as(_fp)),
+               "hbi_mlp_loss_grad")
+        return float(loss.value), g, out
+
+    def train(self, x, t, epochs=50, batch=1024, lr=1e-3, seed=0):
+        x, t = _f32(x), _f32(t)
+        hist = np.zeros(epochs, dtype=np.float32)
+        _check(lib().hbi_mlp_train(self.h, x.ctypes.data_as(_fp), t.ctypes.data_as(_fp), C.c_longlong(len(t)),
+                                   epochs, batch, C.c_float(lr), C.c_ulonglong(seed), hist.ctypes.data_as(_fp)),
+               "hbi_mlp_train")
+        return hist
+
+    def predict(self, x):
+        x = _f32(x)
+        out = np.zeros(len(x), dtype=np.float32)
+        _check(lib().hbi_mlp_predict(self.h, x.ctypes.data_as(_fp), C.c_longlong(len(x)), out.ctypes.data_as(_fp)),
+               "hbi_mlp_predict")
+        return out
+
+    def close(self):
+        if getattr(self, "h", None) and _lib is not None and not _closed:
+            _lib.hbi_mlp_free(self.h)
+        self.h = None
+
+    def __del__(self):
+        self.close()

@@ -69,7 +69,10 @@ def c2_3dph(imax=256, jmax=256, ds0=0.2, seed=0, b_in=0.014, dc=0.02):
     a = np.full(n, 0.010)
     b = np.where(inside, np.broadcast_to(b_in, (n,)), 0.006) if np.ndim(b_in) == 0 else np.where(inside, b_in, 0.006)
     dcv = np.broadcast_to(np.asarray(dc, dtype=np.float64), (n,)).copy()
-    params = dict(a=a, b=b, dc=dcv, f0=np.full(n, 0.6), sigma=np.full(n, 50.0), vel=np.full(n, 1e-9),
+    # V = vpl everywhere is a fixed point of the back-slip-loaded system (the
+    # error estimate is zero and rkqs cannot step); seeded 1% noise as in c1
+    vel = 1e-9 * (1.0 + 0.01 * np.random.default_rng(seed).uniform(-1, 1, n))
+    params = dict(a=a, b=b, dc=dcv, f0=np.full(n, 0.6), sigma=np.full(n, 50.0), vel=vel,
                   vpl=np.full(n, 1e-9), taudot=np.zeros(n), sigdot=np.zeros(n))
     g = dict(xcol=xcol, ycol=ycol, zcol=zcol, ang=ang, angd=angd, dsl=np.full(n, ds0), dsd=np.full(n, ds0),
              rake=rake)
@@ -84,8 +87,10 @@ def c3_3dnt(nx=500, nz=200, length=60.0, width=30.0, seed=0, eps_h=1e-4):
     n = tri.shape[0]
     rng = np.random.default_rng(seed + 1)
     ln = lambda m: m * np.exp(0.1 * rng.standard_normal(n))
-    params = dict(a=ln(0.01), b=ln(0.014), dc=ln(0.01), f0=np.full(n, 0.6), sigma=np.full(n, 50.0),
-                  vel=np.full(n, 1e-9), vpl=np.full(n, 1e-9), taudot=np.zeros(n), sigdot=np.zeros(n))
+    a, b, dc = ln(0.01), ln(0.014), ln(0.01)
+    vel = 1e-9 * (1.0 + 0.01 * rng.uniform(-1, 1, n))
+    params = dict(a=a, b=b, dc=dc, f0=np.full(n, 0.6), sigma=np.full(n, 50.0),
+                  vel=vel, vpl=np.full(n, 1e-9), taudot=np.zeros(n), sigdot=np.zeros(n))
     g["rake"] = np.zeros(n)
     return Workload(f"c3_3dnt_{n}", HBI_3DNT, n, g, 2, 1, area, params, eps_h, 100.0)
 

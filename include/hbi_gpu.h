@@ -264,6 +264,24 @@ int hbi_cycle_free(hbi_cycle* c);
 int hbi_cycle_set_proposer(hbi_cycle* c, const float* w);
 int hbi_cycle_proposer_size(int* nin, int* hid, int* nfloats);
 
+/* ---- training of the step-size proposer (no reference counterpart) -------
+ * An MLP nin -> hid -> hid -> 1 (tanh, tanh, linear) trained by mean squared
+ * error with Adam, entirely by this library's kernels (forward, backward,
+ * update).  Parameters are packed W1[hid][nin] b1 W2[hid][hid] b2 W3[hid] b3,
+ * the first part of the proposer's weight vector. */
+typedef struct hbi_mlp_s hbi_mlp;
+int hbi_mlp_create(hbi_mlp** m, int nin, int hid, int batch_max);
+int hbi_mlp_free(hbi_mlp* m);
+int hbi_mlp_set_params(hbi_mlp* m, const float* p);
+int hbi_mlp_get_params(hbi_mlp* m, float* p);
+/* loss = mean((out - t)^2) over x[batch][nin]; grad = d loss / d params */
+int hbi_mlp_loss_grad(hbi_mlp* m, const float* x, const float* t, int batch, float* grad, float* loss,
+                      float* out);
+/* `epochs` passes of Adam over n samples in shuffled minibatches (seeded) */
+int hbi_mlp_train(hbi_mlp* m, const float* x, const float* t, long long n, int epochs, int batch, float lr,
+                  unsigned long long seed, float* loss_per_epoch);
+int hbi_mlp_predict(hbi_mlp* m, const float* x, long long n, float* out);
+
 #ifdef __cplusplus
 }
 #endif

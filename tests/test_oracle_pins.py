@@ -120,3 +120,47 @@ def test_rkqs_relaxes_to_steady_sliding(oracle):
         assert rc == 0
     V = 2 * vref * np.exp(-y[0::3] / a) * np.sinh(y[1::3] / y[2::3] / a)
     assert np.allclose(V, v0, rtol=1e-3), (x, V.min(), V.max())
+
+
+def test_mlp_oracle_gradient_matches_finite_differences(oracle):
+    """The proposer's forward/backward restatement (the checker of the GPU
+    training kernels) against central differences of its own loss."""
+    nin, h, B = 3, 4, 16
+    rng = np.random.default_rng(1)
+    npar = h * nin + h + h * h + h + h + 1
+    p = (0.5 * rng.standard_normal(npar)).astype(np.float32)
+    x = rng.standard_normal((B, nin)).astype(np.float32)
+    t = rng.standard_normal(B).astype(np.float32)
+    loss, g, _ = oracle.mlp_loss_grad(nin, h, p, x, t)
+    step = 1e-2
+    fd = np.zeros(npar)
+    for k in range(npar):
+        pp, pm = p.copy(), p.copy()
+        pp[k] += step
+        pm[k] -= step
+        fd[k] = (oracle.mlp_loss_grad(nin, h, pp, x, t)[0] - oracle.mlp_loss_grad(nin, h, pm, x, t)[0]) / (
+            float(pp[k]) - float(pm[k]))
+    assert np.allclose(g, fd, rtol=2e-2, atol=2e-4)
+
+
+def test_proposer_labels_recover_the_ideal_step():
+    """training_set's label is the step that would have met the target error
+    under Cash-Karp's h**5 error law."""
+    from hbi_gb300 import proposer
+    rng = np.random.default_rng(2)
+    n = 50
+    rows = []
+    hstar = 10.0 ** rng.uniform(1, 3, n)
+    hnext = hstar * 10.0 ** rng.uniform(-0.3, 0.3, n)
+    for k in range(n):
+        # accepted attempt of step k with rkqs proposal hnext[k]; then the
+        # first attempt of step k+1 at h1 = hnext[k] with its error e1
+        rows.append([k + 1, 0.0, hstar[k], 0.5, 1, 1e-9, hnext[k], 0])
+        if k + 1 < n:
+            h1 = hnext[k]
+            e1 = proposer.E_TARGET * (h1 / hstar[k + 1]) ** 5
+            if e1 >= 1.0:
+                rows.append([k + 1, 0.0, h1, e1, 0, 1e-9, 0.0, 0])
+    X, T = proposer.training_set(np.array(rows))
+    assert X.shape[1] == 6 and len(T) == n - 3
+    assert np.allclose(T, np.log10(hstar[3:n] / hnext[2:n - 1]), atol=1e-5)

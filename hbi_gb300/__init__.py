@@ -39,7 +39,7 @@ EXPORTS = [
     "hbi_cycle_create", "hbi_cycle_run", "hbi_cycle_fields", "hbi_cycle_events", "hbi_cycle_trace",
     "hbi_cycle_free", "hbi_cycle_set_proposer", "hbi_cycle_proposer_size",
     "hbi_mlp_create", "hbi_mlp_free", "hbi_mlp_set_params", "hbi_mlp_get_params", "hbi_mlp_loss_grad",
-    "hbi_mlp_train", "hbi_mlp_predict",
+    "hbi_mlp_train", "hbi_mlp_predict", "hbi_plan_emulate",
 ]
 
 
@@ -559,3 +559,18 @@ class MLP:
 
     def __del__(self):
         self.close()
+
+
+def plan_emulate(n, leaves, body, vec, x):
+    """Host walk of the product's work plan (hbi_plan_emulate): y = H x and
+    plan statistics, without a GPU.  leaves: (nleaf, 6) int array
+    {ltmtx, kt, nstrtl, ndl, nstrtt, ndt}; body: HACApK-packed FP64 factors."""
+    lv = np.ascontiguousarray(leaves, dtype=np.int32)
+    body = np.ascontiguousarray(body, dtype=np.float64)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.zeros(n)
+    st = np.zeros(8, dtype=np.int64)
+    _check(lib().hbi_plan_emulate(n, len(lv), lv.ctypes.data_as(_ip), _p(body), vec, _p(x), _p(y),
+                                  st.ctypes.data_as(_i64p)), "hbi_plan_emulate")
+    keys = ("items1", "items2", "vstore", "ustore", "zlen", "plen1", "plen2", "segments")
+    return y, dict(zip(keys, (int(v) for v in st)))

@@ -179,25 +179,21 @@ struct hbi_leafmtxp_s {
 struct hbi_lhp_s {
   hbi_ctl* ctl = nullptr;
   int n = 0, storage = 0;
-  MatPlan plan;
-  void* d_store = nullptr;
-  P1ItemDev* d_p1 = nullptr;
-  LrInfo* d_lr = nullptr;
+  StreamPlan plan;                 // host copy (conversion maps released after upload)
+  void *d_vstore = nullptr, *d_ustore = nullptr;
+  S1ItemDev* d_s1 = nullptr;
+  S2ItemDev* d_s2 = nullptr;
   int* d_cnt = nullptr;
-  void* d_part = nullptr;
-  void* d_z = nullptr;
-  LeafDescDev* d_desc = nullptr;
-  double *d_x = nullptr, *d_y = nullptr;
-  // row groups (owned by the operator)
-  int32_t *d_gleaf_ptr = nullptr, *d_gleaf = nullptr, *d_grow0 = nullptr, *d_gpoff = nullptr;
+  void *d_part = nullptr, *d_z = nullptr, *d_gpart = nullptr;
+  int32_t* d_midx = nullptr;
+  int32_t *d_grow0 = nullptr, *d_gndl = nullptr, *d_gnch = nullptr, *d_gpoff = nullptr;
   int32_t *d_row_fc = nullptr, *d_fc_ptr = nullptr, *d_fc_group = nullptr;
-  P2ItemDev* d_p2 = nullptr;
-  void* d_gpart = nullptr;
+  int* d_err = nullptr;
+  double *d_x = nullptr, *d_y = nullptr;
   MatDev md{};
   std::vector<Leaf> leaves;
   size_t store_bytes = 0;
   double alg_bytes = 0;
-  int64_t gplen = 0;  // row-group partials (elements)
 };
 
 extern "C" const char* hbi_last_error(void) { return g_err.c_str(); }
@@ -542,119 +538,84 @@ extern "C" int hbi_construct_lh(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* 
   h->n = c->nd;
   h->storage = storage;
   h->leaves = lf->leaves;
-  {
-    // row chains of this operator (owned by it, so a later generate on the
-    // same control block cannot invalidate them)
-    GroupPlan gp;
-    plan_groups(c->nd, lf->leaves, gp);
-    std::vector<P2Item> p2;
-    plan_p2_items(lf->leaves, gp, 16 / (storage == ST_F64 ? 8 : storage == ST_F32 ? 4 : 2), p2);
-    std::vector<P2ItemDev> p2d(p2.size());
-    for (size_t i = 0; i < p2.size(); i++) p2d[i] = P2ItemDev{p2[i].group, p2[i].r0, p2[i].nr, 0};
-    CK(upload(&h->d_gleaf_ptr, gp.gleaf_ptr, c->stream));
-    CK(upload(&h->d_gleaf, gp.gleaf, c->stream));
-    CK(upload(&h->d_grow0, gp.grow0, c->stream));
-    CK(upload(&h->d_gpoff, gp.gpoff, c->stream));
-    CK(upload(&h->d_row_fc, gp.row_fc, c->stream));
-    CK(upload(&h->d_fc_ptr, gp.fc_ptr, c->stream));
-    CK(upload(&h->d_fc_group, gp.fc_group, c->stream));
-    CK(upload(&h->d_p2, p2d, c->stream));
-    const size_t acc_sz = storage == ST_F64 ? 8 : 4;
-    h->gplen = gp.plen;
-    CK(cudaMalloc(&h->d_gpart, std::max<size_t>(gp.plen, 1) * acc_sz));
-    h->md.p2 = h->d_p2;
-    h->md.np2 = (int)p2d.size();
-    h->md.gleaf_ptr = h->d_gleaf_ptr; h->md.gleaf = h->d_gleaf; h->md.grow0 = h->d_grow0; h->md.gpoff = h->d_gpoff;
-    h->md.gpart = h->d_gpart;
-    h->md.row_fc = h->d_row_fc; h->md.fc_ptr = h->d_fc_ptr; h->md.fc_group = h->d_fc_group;
-    h->md.n = c->nd;
-  }
   const int esz = storage == ST_F64 ? 8 : storage == ST_F32 ? 4 : 2;
-  // phase-1 items of about 8192 factor elements, up to 32 columns each
-  const int chunk_elems = getenv("HBI_P1_CHUNK") ? atoi(getenv("HBI_P1_CHUNK")) : 8192;
-  plan_matrix(lf->leaves, 16 / esz, chunk_elems, h->plan);
-  MatPlan& P = h->plan;
-  const int nl = (int)lf->leaves.size();
-  // factor store in the requested precision
-  h->store_bytes = (size_t)P.store_elems * esz;
-  CK(cudaMalloc(&h->d_store, std::max<size_t>(h->store_bytes, 16)));
-  CK(cudaMemsetAsync(h->d_store, 0, std::max<size_t>(h->store_bytes, 16), c->stream));
-  {
-    std::vector<int64_t> so(nl), dof(nl);
-    std::vector<int32_t> kind(nl), rows(nl), cols(nl), kts(nl);
-    for (int i = 0; i < nl; i++) {
-      so[i] = lf->off[i]; dof[i] = P.leaf_off[i];
-      kind[i] = lf->leaves[i].ltmtx; rows[i] = lf->leaves[i].ndl; cols[i] = lf->leaves[i].ndt; kts[i] = lf->leaves[i].kt;
-    }
-    int64_t *d_so = nullptr, *d_dof = nullptr;
-    int32_t *d_kind = nullptr, *d_rows = nullptr, *d_cols = nullptr, *d_kts = nullptr;
-    CK(upload(&d_so, so, c->stream)); CK(upload(&d_dof, dof, c->stream));
-    CK(upload(&d_kind, kind, c->stream)); CK(upload(&d_rows, rows, c->stream));
-    CK(upload(&d_cols, cols, c->stream)); CK(upload(&d_kts, kts, c->stream));
-    launch_store_convert(lf->d_body, nullptr, nl, d_so, d_dof, d_kind, d_rows, d_cols, d_kts, h->d_store, storage, c->stream);
-    CK(cudaStreamSynchronize(c->stream));
-    dfree(d_so); dfree(d_dof); dfree(d_kind); dfree(d_rows); dfree(d_cols); dfree(d_kts);
+  const size_t acc = storage == ST_F64 ? 8 : 4;
+  cudaStream_t st = c->stream;
+  // row-tiled stores read by bulk copies (plan_stream)
+  std::vector<int64_t> boff(lf->leaves.size());
+  for (size_t i = 0; i < boff.size(); i++) boff[i] = lf->off[i];
+  StreamPlan& P = h->plan;
+  plan_stream(c->nd, lf->leaves, boff, 16 / esz, P);
+  const size_t vbytes = (size_t)P.vstore * esz, ubytes = (size_t)P.ustore * esz;
+  h->store_bytes = vbytes + ubytes;
+  CK(cudaMalloc(&h->d_vstore, std::max<size_t>(vbytes, 16)));
+  CK(cudaMalloc(&h->d_ustore, std::max<size_t>(ubytes, 16)));
+  CK(cudaMemsetAsync(h->d_vstore, 0, std::max<size_t>(vbytes, 16), st));
+  CK(cudaMemsetAsync(h->d_ustore, 0, std::max<size_t>(ubytes, 16), st));
+  for (int which = 0; which < 2; which++) {
+    std::vector<SegCopy>& map = which == 0 ? P.vcopy : P.ucopy;
+    SegCopyDev* d_map = nullptr;
+    CK(upload(&d_map, map, st));
+    launch_segcopy(lf->d_body, d_map, (int64_t)map.size(), which == 0 ? h->d_vstore : h->d_ustore, storage, st);
+    CK(cudaStreamSynchronize(st));
+    dfree(d_map);
+    std::vector<SegCopy>().swap(map);
   }
-  // phase-1 items and low-rank leaf table
-  const int nlr = (int)P.lr_leaf.size();
-  std::vector<LrInfo> lr(nlr);
-  for (int q = 0; q < nlr; q++) {
-    lr[q].kt = lf->leaves[P.lr_leaf[q]].kt;
-    lr[q].nparts = P.lr_nparts[q];
-    lr[q].nitems = 0;
-    lr[q].poff = P.lr_poff[q];
-    lr[q].zoff = P.lr_zoff[q];
-    lr[q].pad = 0;
-  }
-  std::vector<P1ItemDev> items(P.p1.size());
-  for (size_t t = 0; t < P.p1.size(); t++) {
-    const P1Item& I = P.p1[t];
-    P1ItemDev& d = items[t];
-    d.voff = I.voff; d.ldv = I.ldv; d.nt = I.nt; d.x0 = I.x0; d.k0 = I.k0; d.nk = I.nk; d.lr = I.leaf; d.pad = 0;
-    const LrInfo& L = lr[I.leaf];
-    d.pout = L.nparts == 1 ? L.zoff + I.k0 : L.poff + I.part * L.kt + I.k0;
-    lr[I.leaf].nitems++;
-  }
-  std::vector<LeafDescDev> desc(nl);
-  for (int i = 0; i < nl; i++) {
-    const LeafDesc& s = P.desc[i];
-    desc[i] = LeafDescDev{s.off, s.row0, s.ndl, s.kind, s.kt_or_ndt, s.aux, 0};
-  }
-  const size_t accsz = storage == ST_F64 ? 8 : 4;
-  CK(upload(&h->d_p1, items, c->stream));
-  CK(upload(&h->d_lr, lr, c->stream));
-  CK(upload(&h->d_desc, desc, c->stream));
-  CK(dalloc(&h->d_cnt, nlr));
-  CK(cudaMemset(h->d_cnt, 0, sizeof(int) * std::max(nlr, 1)));
-  CK(cudaMalloc(&h->d_part, std::max<size_t>(P.plen, 1) * accsz));
-  CK(cudaMalloc(&h->d_z, std::max<size_t>(P.zlen, 1) * accsz));
-  CK(cudaMemset(h->d_z, 0, std::max<size_t>(P.zlen, 1) * accsz));
+  CK(cudaGetLastError());
+  const GroupPlan& G = P.gp;
+  CK(upload(&h->d_s1, P.p1, st));
+  CK(upload(&h->d_s2, P.p2, st));
+  CK(upload(&h->d_midx, P.midx, st));
+  CK(upload(&h->d_grow0, G.grow0, st));
+  CK(upload(&h->d_gndl, G.gndl, st));
+  CK(upload(&h->d_gnch, P.gnch, st));
+  CK(upload(&h->d_gpoff, P.gpoff2, st));
+  CK(upload(&h->d_row_fc, G.row_fc, st));
+  CK(upload(&h->d_fc_ptr, G.fc_ptr, st));
+  CK(upload(&h->d_fc_group, G.fc_group, st));
+  CK(dalloc(&h->d_cnt, (size_t)P.ncg));
+  CK(cudaMemset(h->d_cnt, 0, sizeof(int) * std::max<int64_t>(P.ncg, 1)));
+  CK(dalloc(&h->d_err, 1));
+  CK(cudaMemset(h->d_err, 0, sizeof(int)));
+  CK(cudaMalloc(&h->d_part, std::max<size_t>(P.plen1, 1) * acc));
+  CK(cudaMalloc(&h->d_z, std::max<size_t>(P.zlen, 1) * acc));
+  CK(cudaMemset(h->d_z, 0, std::max<size_t>(P.zlen, 1) * acc));
+  CK(cudaMalloc(&h->d_gpart, std::max<size_t>(P.plen2, 1) * acc));
   CK(dalloc(&h->d_x, h->n));
   CK(dalloc(&h->d_y, h->n));
-  h->md.store = h->d_store;
-  h->md.storage = storage;
-  h->md.p1 = h->d_p1;
-  h->md.np1 = (int)items.size();
-  h->md.lr = h->d_lr;
-  h->md.lr_cnt = h->d_cnt;
-  h->md.part = h->d_part;
-  h->md.z = h->d_z;
-  h->md.desc = h->d_desc;
-  h->md.scale = 1.0;
+  MatDev& m = h->md;
+  m.n = c->nd;
+  m.storage = storage;
+  m.vstore = h->d_vstore;
+  m.ustore = h->d_ustore;
+  m.s1 = h->d_s1;
+  m.ns1 = (int)P.p1.size();
+  m.s2 = h->d_s2;
+  m.ns2 = (int)P.p2.size();
+  m.cnt = h->d_cnt;
+  m.part = h->d_part;
+  m.z = h->d_z;
+  m.midx = h->d_midx;
+  m.gpart = h->d_gpart;
+  m.grow0 = h->d_grow0; m.gndl = h->d_gndl; m.gnch = h->d_gnch; m.gpoff = h->d_gpoff;
+  m.row_fc = h->d_row_fc; m.fc_ptr = h->d_fc_ptr; m.fc_group = h->d_fc_group;
+  m.scale = 1.0;
+  m.skip = nullptr;
+  m.err = h->d_err;
   h->alg_bytes = (double)P.factor_elems * esz + (double)h->n * 8 * 2;
+  prepare_stream_kernels();
+  CK(cudaGetLastError());
   *out = h;
   return HBI_OK;
 }
 
 extern "C" int hbi_free_lh(hbi_lhp* h) {
   if (!h) return HBI_OK;
-  if (h->d_store) cudaFree(h->d_store);
-  dfree(h->d_p1); dfree(h->d_lr); dfree(h->d_cnt); dfree(h->d_desc); dfree(h->d_x); dfree(h->d_y);
-  dfree(h->d_gleaf_ptr); dfree(h->d_gleaf); dfree(h->d_grow0); dfree(h->d_gpoff);
-  dfree(h->d_row_fc); dfree(h->d_fc_ptr); dfree(h->d_fc_group); dfree(h->d_p2);
-  if (h->d_gpart) cudaFree(h->d_gpart);
-  if (h->d_part) cudaFree(h->d_part);
-  if (h->d_z) cudaFree(h->d_z);
+  for (void* p : {h->d_vstore, h->d_ustore, (void*)h->d_s1, (void*)h->d_s2, (void*)h->d_cnt, h->d_part, h->d_z,
+                  h->d_gpart, (void*)h->d_midx, (void*)h->d_grow0, (void*)h->d_gndl, (void*)h->d_gnch,
+                  (void*)h->d_gpoff, (void*)h->d_row_fc, (void*)h->d_fc_ptr, (void*)h->d_fc_group, (void*)h->d_err,
+                  (void*)h->d_x, (void*)h->d_y})
+    if (p) cudaFree(p);
   delete h;
   return HBI_OK;
 }
@@ -709,24 +670,24 @@ extern "C" int hbi_adot_lattice_hyp_noalloc(double* d_au, hbi_lhp* h, const doub
   }
   // layout: [arrival counters][z][phase-1 partials][row-group partials]
   const size_t acc = h->storage == ST_F64 ? 8 : 4;
-  const size_t nlr = h->plan.lr_leaf.size();
+  const size_t nlr = (size_t)h->plan.ncg;
   const size_t b_cnt = align256(std::max<size_t>(nlr, 1) * sizeof(int));
   const size_t b_z = align256(std::max<int64_t>(h->plan.zlen, 1) * acc);
-  const size_t b_part = align256(std::max<int64_t>(h->plan.plen, 1) * acc);
-  const size_t b_gp = align256(std::max<int64_t>(h->gplen, 1) * acc);
+  const size_t b_part = align256(std::max<int64_t>(h->plan.plen1, 1) * acc);
+  const size_t b_gp = align256(std::max<int64_t>(h->plan.plen2, 1) * acc);
   const size_t need = b_cnt + b_z + b_part + b_gp;
   if (need > HBI_NOALLOC_SCRATCH_BYTES)
     return fail(HBI_ERR_LIMIT, "hbi_adot_lattice_hyp_noalloc: operator needs %zu bytes of scratch, the limit is %u",
                 need, (unsigned)HBI_NOALLOC_SCRATCH_BYTES);
   unsigned char* p = (unsigned char*)base;
   MatDev md = h->md;
-  md.lr_cnt = (int*)p;
+  md.cnt = (int*)p;
   md.z = p + b_cnt;
   md.part = p + b_cnt + b_z;
   md.gpart = p + b_cnt + b_z + b_part;
   cudaStream_t st = stream ? (cudaStream_t)stream : h->ctl->stream;
   // the counters must start at zero; everything else is written before it is read
-  CK(cudaMemsetAsync(md.lr_cnt, 0, nlr * sizeof(int), st));
+  CK(cudaMemsetAsync(md.cnt, 0, nlr * sizeof(int), st));
   double* ys[2] = {d_au, nullptr};
   launch_phase1(&md, 1, d_u, h->ctl->sm_count, st);
   launch_phase2(&md, 1, d_u, h->ctl->sm_count, st);
@@ -1028,5 +989,101 @@ extern "C" int hbi_rkqs(hbi_rk* r, double* x, double htry, double eps, double dt
   if (errmax) *errmax = e;
   if (nrjct) *nrjct = nr;
   *x = *x + h;
+  return HBI_OK;
+}
+
+// ------------------------------------------------- work-plan self check (host)
+// Runs plan_stream on a leaf list and walks its items exactly as the phase
+// kernels do, in FP64 on the host: y = H x from a HACApK-packed body.  Checks
+// every bound the kernels rely on (regions inside the stores and at most one
+// stage, 16-byte alignment, indices inside z / x / partials).  stats (8):
+// phase-1 items, phase-2 items, V store, U store (elements), z length,
+// phase-1 partials, phase-2 partials, conversion segments.
+extern "C" int hbi_plan_emulate(int n, int nleaf, const int* lv6, const double* body, int vec, const double* x,
+                                double* y, int64_t* stats) {
+  if (n < 1 || nleaf < 1 || !lv6 || !body || !x || !y || (vec != 2 && vec != 4 && vec != 8))
+    return fail(HBI_ERR_ARG, "hbi_plan_emulate: bad arguments");
+  std::vector<Leaf> L(nleaf);
+  std::vector<int64_t> boff(nleaf);
+  int64_t off = 0;
+  for (int i = 0; i < nleaf; i++) {
+    const int* q = lv6 + 6 * i;
+    L[i] = Leaf{q[0], q[1], q[2], q[3], q[4], q[5]};
+    boff[i] = off;
+    off += L[i].ltmtx == 1 ? (int64_t)L[i].kt * (L[i].ndl + L[i].ndt) : (int64_t)L[i].ndl * L[i].ndt;
+  }
+  StreamPlan P;
+  plan_stream(n, L, boff, vec, P);
+  const int esz = 16 / vec;
+  std::vector<double> V(P.vstore, 0.0), U(P.ustore, 0.0);
+  int64_t nseg_conv = 0;
+  for (int w = 0; w < 2; w++) {
+    const std::vector<SegCopy>& map = w ? P.ucopy : P.vcopy;
+    std::vector<double>& dst = w ? U : V;
+    for (const SegCopy& c : map) {
+      if (c.dst < 0 || c.dst + c.len > (int64_t)dst.size() || c.dst % vec) return fail(HBI_ERR_STATE, "copy dst");
+      if (c.src < 0 || c.src + (int64_t)(c.len - 1) * c.stride >= off) return fail(HBI_ERR_STATE, "copy src");
+      for (int r = 0; r < c.len; r++) dst[c.dst + r] = body[c.src + (int64_t)r * c.stride];
+    }
+    nseg_conv += (int64_t)map.size();
+  }
+  std::vector<double> z(std::max<int64_t>(P.zlen, 1), 0.0), part(std::max<int64_t>(P.plen1, 1), 0.0);
+  for (const S1Item& it : P.p1) {
+    if (it.ncols < 1 || it.ntp % vec || it.ntp > 32 * vec || chunk_cols(it.ntp, esz) < 32 ||
+        chunk_cols(it.ntp, esz) > 256 || (int64_t)chunk_cols(it.ntp, esz) * it.ntp * esz > 16384 || it.soff % vec ||
+        it.soff + (int64_t)it.ncols * it.ntp > P.vstore || it.x0 < 0 || it.x0 + it.nt > n || it.nt > it.ntp ||
+        it.z0 < 0 || it.z0 + it.ncols > P.zlen ||
+        (it.ntile > 1 && (it.cg < 0 || it.cg >= P.ncg || it.poff < 0 ||
+                          it.poff + (int64_t)it.ntile * it.ncols > P.plen1)))
+      return fail(HBI_ERR_STATE, "phase-1 item out of bounds");
+    for (int c = 0; c < it.ncols; c++) {
+      double t = 0.0;
+      for (int r = 0; r < it.nt; r++) t += V[it.soff + (int64_t)c * it.ntp + r] * x[it.x0 + r];
+      if (it.ntile == 1) z[it.z0 + c] = t;
+      else part[it.poff + (int64_t)it.tile * it.ncols + c] = t;
+    }
+  }
+  for (const S1Item& it : P.p1)
+    if (it.ntile > 1 && it.tile == 0)
+      for (int c = 0; c < it.ncols; c++) {
+        double t = 0.0;
+        for (int q = 0; q < it.ntile; q++) t += part[it.poff + (int64_t)q * it.ncols + c];
+        z[it.z0 + c] = t;
+      }
+  std::vector<double> gp(std::max<int64_t>(P.plen2, 1), 0.0);
+  for (const S2Item& it : P.p2) {
+    const int cc = chunk_cols(it.ntp, esz);
+    const int64_t last_chunk = (int64_t)(it.ncols - 1) / cc * cc;
+    const int64_t midx_end = it.m0 + last_chunk + ((it.ncols - last_chunk + 3) / 4) * 4;
+    if (it.ncols < 1 || it.ntp % vec || it.ntp > 32 * vec || cc < 32 || cc > 256 || (int64_t)cc * it.ntp * esz > 16384 ||
+        ((cc + 3) / 4) * 16 > 1024 || it.soff % vec ||
+        it.soff + (int64_t)it.ncols * it.ntp > P.ustore || it.nr > it.ntp || it.m0 < 0 || it.m0 % 4 ||
+        midx_end > (int64_t)P.midx.size() || it.pout < 0 || it.pout + it.nr > P.plen2)
+      return fail(HBI_ERR_STATE, "phase-2 item out of bounds");
+    for (int r = 0; r < it.nr; r++) {
+      double t = 0.0;
+      for (int c = 0; c < it.ncols; c++) {
+        const int mi = P.midx[it.m0 + c];
+        if (mi >= P.zlen || -mi - 1 >= n) return fail(HBI_ERR_STATE, "multiplier index");
+        const double mu = mi >= 0 ? z[mi] : x[-mi - 1];
+        t += U[it.soff + (int64_t)c * it.ntp + r] * mu;
+      }
+      gp[it.pout + r] = t;
+    }
+  }
+  const GroupPlan& G = P.gp;
+  for (int r = 0; r < n; r++) {
+    double t = 0.0;
+    const int f = G.row_fc[r];
+    for (int e = G.fc_ptr[f]; e < G.fc_ptr[f + 1]; e++) {
+      const int g = G.fc_group[e];
+      for (int c = 0; c < P.gnch[g]; c++) t += gp[P.gpoff2[g] + (int64_t)c * G.gndl[g] + r - G.grow0[g]];
+    }
+    y[r] = t;
+  }
+  if (stats) {
+    stats[0] = (int64_t)P.p1.size(); stats[1] = (int64_t)P.p2.size(); stats[2] = P.vstore; stats[3] = P.ustore;
+    stats[4] = P.zlen; stats[5] = P.plen1; stats[6] = P.plen2; stats[7] = nseg_conv;
+  }
   return HBI_OK;
 }

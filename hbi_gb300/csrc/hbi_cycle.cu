@@ -276,6 +276,8 @@ __global__ void __launch_bounds__(256) cycle_control_kernel(RkDev R, CycleConst 
       if (!(d == d)) d = 0.0;
       const float* lohi = M.w + proposer_weights(M.nin, M.hid) + 2 * M.nin;
       d = fmin(fmax(d, (double)lohi[0]), (double)lohi[1]);
+      // after a step that needed retries, never propose more than rkqs does
+      if (S->nrjct > 0) d = fmin(d, 0.0);
       S->proposal = d;
       red[0] = fmin(red[0] * exp(d * 2.302585092994046), P.dtmax);
     }

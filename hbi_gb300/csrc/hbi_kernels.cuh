@@ -7,6 +7,7 @@
 #include <cstdint>
 
 #include "hbi_entries.cuh"
+#include "hbi_structure.hpp"
 
 #ifndef HBI_ACA_NT
 #define HBI_ACA_NT 128
@@ -43,42 +44,31 @@ void launch_entries(const DevBemv& b, const int* ii, const int* jj, int n, doubl
 // ---- matvec ----------------------------------------------------------------
 enum { ST_F64 = 0, ST_F32 = 1, ST_BF16 = 2 };
 
-struct P1ItemDev {
-  int64_t voff;
-  int32_t ldv, nt, x0, k0, nk, lr, pout, pad;
-};
-struct LeafDescDev {
-  int64_t off;
-  int32_t row0, ndl, kind, kt_or_ndt, aux, pad;
-};
-// per low-rank leaf, for the multi-chunk reduction of phase 1
-struct LrInfo {
-  int32_t kt, nparts, nitems, poff, zoff, pad;
-};
-
-struct P2ItemDev {
-  int32_t group, r0, nr, pad;
-};
+// work items of the streamed product (plan_stream in hbi_structure.cpp)
+typedef S1Item S1ItemDev;
+typedef S2Item S2ItemDev;
+typedef SegCopy SegCopyDev;
 
 struct MatDev {            // one H-matrix on the device
   int n;
-  const void* store;       // factor store, element type per `storage`
-  int storage;
-  const P1ItemDev* p1;
-  int np1;
-  const LrInfo* lr;
-  int* lr_cnt;             // arrival counters (self-resetting)
-  void* part;              // phase-1 partial sums (Acc type)
-  void* z;                 // z = V^T x per low-rank leaf (Acc type)
-  const LeafDescDev* desc;
-  // row groups (leaves sharing a row range) and their phase-2 items
-  const P2ItemDev* p2;
-  int np2;
-  const int32_t *gleaf_ptr, *gleaf, *grow0, *gpoff;
-  void* gpart;             // per-group row partials (Acc type)
+  int storage;             // element type of the stores (ST_*)
+  const void* vstore;      // phase-1 store: V tiles of the column groups
+  const void* ustore;      // phase-2 store: U / A tiles of the row groups
+  const S1ItemDev* s1;
+  int ns1;
+  const S2ItemDev* s2;
+  int ns2;
+  int* cnt;                // phase-1 column-chunk arrival counters (self-resetting)
+  void* part;              // phase-1 per-tile partial column sums (Acc type)
+  void* z;                 // z = V^T x per low-rank column (Acc type)
+  const int32_t* midx;     // phase-2 column multipliers: z index, or -(x index)-1
+  void* gpart;             // phase-2 partial row sums (Acc type)
+  // phase 3: rows -> covering row groups -> their column chunks
+  const int32_t *grow0, *gndl, *gnch, *gpoff;
   const int32_t *row_fc, *fc_ptr, *fc_group;
   double scale;            // result multiplier (1/ds0 for 3dph, else 1)
   const int* skip;         // when non-null and nonzero, phases 1-2 do nothing
+  int* err;                // set to nonzero when a bulk copy did not arrive in time
 };
 
 // RK (Cash-Karp) stage state on the device; all arrays in cluster order
@@ -110,6 +100,9 @@ struct RkView {
 
 // phase 1: z = V^T x; phase 2: per-group row partials of U z + A x;
 // phase 3: per-row sum of the group partials (plain, or with the RK epilogue)
+void launch_segcopy(const double* body, const SegCopyDev* map, int64_t nmap, void* dst, int storage,
+                    cudaStream_t st);
+void prepare_stream_kernels();
 void launch_phase1(const MatDev* mats, int nmat, const double* x, int sm_count, cudaStream_t st);
 void launch_phase2(const MatDev* mats, int nmat, const double* x, int sm_count, cudaStream_t st);
 void launch_phase3_plain(const MatDev* mats, int nmat, double* const* y, cudaStream_t st);
@@ -119,8 +112,6 @@ void set_tableau(const double* B15, const double* C6, const double* DC6);
 // dst[dst_off[i] : +len[i]] = src[i][0 : len[i]]
 void launch_copy_segments(const double* const* src, const int64_t* dst_off, const int64_t* len, int nseg,
                           double* dst, cudaStream_t st);
-void launch_store_convert(const double* src, const LeafDescDev* desc_src_dense_transpose, int nleaf,
-                          const int64_t* src_off, const int64_t* dst_off, const int32_t* kind, const int32_t* rows,
-                          const int32_t* cols, const int32_t* kts, void* dst, int storage, cudaStream_t st);
+
 
 }  // namespace hbi

@@ -1,0 +1,618 @@
+// hbi_stream.cu -- phases 1 and 2 of the lattice H-matrix-vector product
+// (HACApK_adot_body_lfmtx_hyp_contiguous, m_HACApK_solve.f90:2108-2164) as
+// streams of bulk asynchronous copies.
+//
+// The factor store is laid out in row tiles (hbi_structure.cpp, plan_stream):
+// every work item reads one contiguous region of at most 16 KB -- up to 32
+// column segments of one tile of a column group (phase 1) or of a row group
+// (phase 2).  Each warp of a block owns NS shared-memory stages with one
+// mbarrier each; one lane starts a cp.async.bulk (TMA) copy of an item's
+// region into a free stage while the warp consumes an earlier stage, so the
+// bytes in flight per SM are set by the stages (NW x NS x 16 KB), not by
+// registers.  The small per-item operands (x rows, z / x multipliers) are
+// loaded by the lanes one item ahead of their use.
+//
+// Lanes work on a stage as column slots: a segment of ntp rows is covered by
+// LW = pow2ceil(ntp / VEC) lanes with one 16-byte vector each, and CS = 32/LW
+// slots take different columns.  Phase 1 reduces each column over its LW
+// lanes (z = V^T x, partial per row tile, combined by the last tile of a
+// column chunk); phase 2 accumulates y rows per lane and reduces over the
+// slots once per item.  Every sum has a fixed order: results are
+// deterministic run to run.
+//
+// Waits are bounded: a stage that does not complete within ~1 s of SM clock
+// sets the operator's error word, the warp waits (bounded again) for its other
+// copies and leaves.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdlib>
+#include <mutex>
+
+#include "hbi_kernels.cuh"
+
+namespace hbi {
+
+namespace {
+
+constexpr int kStage = 16384;  // bytes per stage: 32 segments x 512 bytes
+constexpr long long kWaitCycles = 2LL << 30;
+
+template <typename T>
+struct AccT {
+  typedef float type;
+};
+template <>
+struct AccT<double> {
+  typedef double type;
+};
+
+__device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(saddr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// lane 0: wait for the phase `parity` of `bar` for at most kWaitCycles
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity))
+    if (clock64() - t0 > kWaitCycles) return false;
+  return true;
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(saddr(dst)),
+      "l"(src), "r"(bytes), "r"(saddr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+// one 16-byte vector of shared memory as VEC accumulator values
+__device__ __forceinline__ void lds16(const double* p, double* o) {
+  const double2 v = *reinterpret_cast<const double2*>(p);
+  o[0] = v.x;
+  o[1] = v.y;
+}
+__device__ __forceinline__ void lds16(const float* p, float* o) {
+  const float4 v = *reinterpret_cast<const float4*>(p);
+  o[0] = v.x;
+  o[1] = v.y;
+  o[2] = v.z;
+  o[3] = v.w;
+}
+__device__ __forceinline__ void lds16(const __nv_bfloat16* p, float* o) {
+  const uint4 v = *reinterpret_cast<const uint4*>(p);
+  const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    o[2 * i] = __uint_as_float(w[i] << 16);
+    o[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
+  }
+}
+
+__device__ __forceinline__ int log2ceil(int n) { return n <= 1 ? 0 : 32 - __clz(n - 1); }
+
+// shared memory of a block: per warp NS stages of [16 KB data][1 KB column
+// indices], then per warp 256 multipliers, then the stage barriers
+constexpr int kIdx = 1024;
+constexpr int kStageAll = kStage + kIdx;
+template <int NW, int NS>
+struct Ring {
+  unsigned char* buf;  // stage s at buf + s * kStageAll
+  void* mu;            // 256 multipliers (Acc) of the warp
+  uint64_t* bar;
+  __device__ Ring(unsigned char* smem, int warp) {
+    buf = smem + (size_t)warp * NS * kStageAll;
+    mu = smem + (size_t)NW * NS * kStageAll + (size_t)warp * 256 * 8;
+    bar = reinterpret_cast<uint64_t*>(smem + (size_t)NW * NS * kStageAll + (size_t)NW * 256 * 8) + warp * NS;
+  }
+};
+
+// wait for a stage's phase `parity`; all lanes acquire.  Returns false (and
+// records the error) when the copy did not arrive in time.
+__device__ __forceinline__ bool stage_ready(uint64_t* bar, uint32_t parity, int* err) {
+  int ok = 1;
+  if ((threadIdx.x & 31) == 0) ok = mbar_wait_bounded(bar, parity) ? 1 : 0;
+  ok = __shfl_sync(0xffffffffu, ok, 0);
+  if (!ok) {
+    if ((threadIdx.x & 31) == 0 && err) atomicExch(err, 1);
+    return false;
+  }
+  // the phase has completed: these waits return at once
+  while (!mbar_try_wait(bar, parity)) {
+  }
+  return true;
+}
+
+// after a failed wait: let the warp's copies still in flight land (bounded)
+template <int NS>
+__device__ void drain(uint64_t* bar, int c_seq, int p_seq) {
+  if ((threadIdx.x & 31) == 0)
+    for (int q = c_seq; q < p_seq; q++) mbar_wait_bounded(&bar[q % NS], (uint32_t)((q / NS) & 1));
+  __syncwarp();
+}
+
+// as chunk_cols (hbi_structure.hpp): whole columns in 16 KB, multiple of 32, at most 256
+__device__ __forceinline__ int chunk_cols_dev(int ntp, int esz) { return min((kStage / (ntp * esz)) / 32 * 32, 256); }
+
+// arrival count with release (prior writes of the warp, ordered by the
+// __syncwarp before it) and acquire (the partials of the other tiles)
+__device__ __forceinline__ int arrive_acq_rel(int* p) {
+  int old;
+  asm volatile("atom.add.acq_rel.gpu.s32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+  return old;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- phase 1
+// Item = one row tile of a column group over all its columns; streamed in
+// chunks of up to 16 KB.  Column sums of a chunk go to z (one tile) or to the
+// tile's partials; the last tile of the group to finish sums the partials.
+template <typename T, int NW, int NS>
+__global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev m1, int nmat,
+                                                               const double* __restrict__ x) {
+  typedef typename AccT<T>::type Acc;
+  constexpr int VEC = 16 / sizeof(T);
+  constexpr int ESZ = sizeof(T);
+  extern __shared__ __align__(128) unsigned char smem[];
+  if (m0.skip && __ldcg(m0.skip)) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  Ring<NW, NS> R(smem, warp);
+  if (lane == 0) {
+    for (int s = 0; s < NS; s++) mbar_init(&R.bar[s], 1);
+    fence_mbar_init();
+  }
+  __syncwarp();
+  const int gw = blockIdx.x * NW + warp, GW = gridDim.x * NW;
+  const int n0 = m0.ns1, ntot = nmat == 2 ? n0 + m1.ns1 : n0;
+  auto desc = [&](int it) -> S1ItemDev {
+    S1ItemDev d{};
+    if (it < ntot) d = it < n0 ? m0.s1[it] : m1.s1[it - n0];
+    return d;
+  };
+  // producer: walks this warp's items chunk by chunk, NS chunks ahead
+  int p_it = gw, p_c0 = 0, p_seq = 0;
+  S1ItemDev Dp = desc(p_it), Dpn = desc(p_it + GW);
+  auto produce = [&]() {
+    if (p_it >= ntot) return;
+    const int nc = min(chunk_cols_dev(Dp.ntp, ESZ), Dp.ncols - p_c0);
+    const int s = p_seq % NS;
+    if (lane == 0) {
+      const uint32_t bytes = (uint32_t)(nc * Dp.ntp * ESZ);
+      const T* src = (const T*)(p_it < n0 ? m0.vstore : m1.vstore) + Dp.soff + (int64_t)p_c0 * Dp.ntp;
+      fence_proxy_async();
+      mbar_expect_tx(&R.bar[s], bytes);
+      bulk_g2s(R.buf + s * kStageAll, src, bytes, &R.bar[s]);
+    }
+    p_seq++;
+    p_c0 += nc;
+    if (p_c0 >= Dp.ncols) {
+      p_it += GW;
+      p_c0 = 0;
+      Dp = Dpn;
+      Dpn = desc(p_it + GW);
+    }
+  };
+  for (int q = 0; q < NS; q++) produce();
+  // consumer
+  int c_it = gw, c_c0 = 0, c_seq = 0;
+  S1ItemDev Dc = desc(c_it), Dn = desc(c_it + GW), Dnn = desc(c_it + 2 * GW);
+  auto load_x = [&](const S1ItemDev& D, Acc* xv) {
+    const int lw = log2ceil(max(1, D.ntp / VEC));
+    const int j = lane & ((1 << lw) - 1);
+#pragma unroll
+    for (int v = 0; v < VEC; v++) {
+      const int r = j * VEC + v;
+      xv[v] = (D.ncols > 0 && r < D.nt) ? (Acc)__ldg(&x[D.x0 + r]) : Acc(0);
+    }
+  };
+  Acc xc[VEC], xn[VEC];
+  load_x(Dc, xc);
+  load_x(Dn, xn);
+  while (c_it < ntot) {
+    const bool sec = c_it >= n0;
+    const MatDev& M = sec ? m1 : m0;
+    const int s = c_seq % NS;
+    if (!stage_ready(&R.bar[s], (uint32_t)((c_seq / NS) & 1), M.err)) {
+      drain<NS>(R.bar, c_seq, p_seq);
+      return;
+    }
+    const int nc = min(chunk_cols_dev(Dc.ntp, ESZ), Dc.ncols - c_c0);
+    const T* st = (const T*)(R.buf + s * kStageAll);
+    const int nq = Dc.ntp / VEC;
+    const int lw = log2ceil(nq), LW = 1 << lw, CS = 32 >> lw;
+    const int slot = lane >> lw, j = lane & (LW - 1);
+    Acc* z = (Acc*)M.z;
+    Acc* part = (Acc*)M.part;
+    if (LW == 32) {
+      // full-height tiles: 32 columns at a time, reduced by a butterfly
+      // reduce-scatter (31 shuffle-adds per lane for 32 columns); lane L ends
+      // with the sum of column r0 + L
+      for (int r0 = 0; r0 < nc; r0 += 32) {
+        Acc p[32];
+#pragma unroll
+        for (int u = 0; u < 32; u++) {
+          p[u] = 0;
+          if (r0 + u < nc && j < nq) {
+            Acc a[VEC];
+            lds16(st + (r0 + u) * Dc.ntp + j * VEC, a);
+#pragma unroll
+            for (int v = 0; v < VEC; v++) p[u] += a[v] * xc[v];
+          }
+        }
+#pragma unroll
+        for (int lev = 16; lev >= 1; lev >>= 1) {
+          const bool upper = (lane & lev) != 0;
+#pragma unroll
+          for (int i = 0; i < lev; i++) {
+            const Acc send = upper ? p[i] : p[i + lev];
+            const Acc keep = upper ? p[i + lev] : p[i];
+            p[i] = keep + __shfl_xor_sync(0xffffffffu, send, lev);
+          }
+        }
+        if (r0 + lane < nc) {
+          const int col = c_c0 + r0 + lane;
+          if (Dc.ntile == 1) z[Dc.z0 + col] = p[0];
+          else part[Dc.poff + (int64_t)Dc.tile * Dc.ncols + col] = p[0];
+        }
+      }
+    } else
+    // eight columns per slot at a time, so that their lane reductions
+    // (shuffle chains) proceed side by side
+    for (int r0 = 0; r0 < nc; r0 += 8 * CS) {
+      constexpr int UC_ = 8;
+      Acc p[UC_];
+#pragma unroll
+      for (int u = 0; u < UC_; u++) {
+        const int sg = r0 + u * CS + slot;
+        p[u] = 0;
+        if (sg < nc && j < nq) {
+          Acc a[VEC];
+          lds16(st + sg * Dc.ntp + j * VEC, a);
+#pragma unroll
+          for (int v = 0; v < VEC; v++) p[u] += a[v] * xc[v];
+        }
+      }
+      for (int o = 1; o < LW; o <<= 1)
+#pragma unroll
+        for (int u = 0; u < UC_; u++) p[u] += __shfl_xor_sync(0xffffffffu, p[u], o);
+      if (j == 0) {
+#pragma unroll
+        for (int u = 0; u < UC_; u++) {
+          const int sg = r0 + u * CS + slot;
+          if (sg < nc) {
+            const int col = c_c0 + sg;
+            if (Dc.ntile == 1) z[Dc.z0 + col] = p[u];
+            else part[Dc.poff + (int64_t)Dc.tile * Dc.ncols + col] = p[u];
+          }
+        }
+      }
+    }
+    __syncwarp();
+    c_seq++;
+    produce();
+    c_c0 += nc;
+    if (c_c0 < Dc.ncols) continue;
+    // item done: the last row tile of a column group sums the tiles in order
+    if (Dc.ntile > 1) {
+      __syncwarp();
+      int last = 0;
+      if (lane == 0) last = arrive_acq_rel(&M.cnt[Dc.cg]) == Dc.ntile - 1;
+      last = __shfl_sync(0xffffffffu, last, 0);
+      if (last) {
+        __syncwarp();  // lane 0's acquire orders the reads of every lane
+        for (int col = lane; col < Dc.ncols; col += 32) {
+          Acc t = 0;
+          for (int q = 0; q < Dc.ntile; q++) t += __ldcg(&part[Dc.poff + (int64_t)q * Dc.ncols + col]);
+          z[Dc.z0 + col] = t;
+        }
+        if (lane == 0) M.cnt[Dc.cg] = 0;
+      }
+    }
+    c_it += GW;
+    c_c0 = 0;
+    Dc = Dn;
+    Dn = Dnn;
+#pragma unroll
+    for (int v = 0; v < VEC; v++) xc[v] = xn[v];
+    load_x(Dn, xn);
+    Dnn = desc(c_it + 2 * GW);
+  }
+}
+
+// ---------------------------------------------------------------- phase 2
+// Item = one row tile of a row group over all its columns, streamed in chunks
+// of up to 16 KB together with the chunk's multiplier indices; the lanes
+// gather the multipliers (z for low-rank columns, x for dense ones) into
+// shared memory, then accumulate their rows; one reduction over the column
+// slots per item.
+template <typename T, int NW, int NS>
+__global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev m1, int nmat,
+                                                               const double* __restrict__ x) {
+  typedef typename AccT<T>::type Acc;
+  constexpr int VEC = 16 / sizeof(T);
+  constexpr int ESZ = sizeof(T);
+  extern __shared__ __align__(128) unsigned char smem[];
+  if (m0.skip && __ldcg(m0.skip)) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  Ring<NW, NS> R(smem, warp);
+  Acc* musm = (Acc*)R.mu;
+  if (lane == 0) {
+    for (int s = 0; s < NS; s++) mbar_init(&R.bar[s], 1);
+    fence_mbar_init();
+  }
+  __syncwarp();
+  const int gw = blockIdx.x * NW + warp, GW = gridDim.x * NW;
+  const int n0 = m0.ns2, ntot = nmat == 2 ? n0 + m1.ns2 : n0;
+  auto desc = [&](int it) -> S2ItemDev {
+    S2ItemDev d{};
+    if (it < ntot) d = it < n0 ? m0.s2[it] : m1.s2[it - n0];
+    return d;
+  };
+  int p_it = gw, p_c0 = 0, p_seq = 0;
+  S2ItemDev Dp = desc(p_it), Dpn = desc(p_it + GW);
+  auto produce = [&]() {
+    if (p_it >= ntot) return;
+    const int nc = min(chunk_cols_dev(Dp.ntp, ESZ), Dp.ncols - p_c0);
+    const int s = p_seq % NS;
+    if (lane == 0) {
+      const uint32_t bytes = (uint32_t)(nc * Dp.ntp * ESZ);
+      const uint32_t ibytes = (uint32_t)(((nc + 3) / 4) * 16);
+      const MatDev& PM = p_it < n0 ? m0 : m1;
+      const T* src = (const T*)PM.ustore + Dp.soff + (int64_t)p_c0 * Dp.ntp;
+      fence_proxy_async();
+      mbar_expect_tx(&R.bar[s], bytes + ibytes);
+      bulk_g2s(R.buf + s * kStageAll, src, bytes, &R.bar[s]);
+      bulk_g2s(R.buf + s * kStageAll + kStage, PM.midx + Dp.m0 + p_c0, ibytes, &R.bar[s]);
+    }
+    p_seq++;
+    p_c0 += nc;
+    if (p_c0 >= Dp.ncols) {
+      p_it += GW;
+      p_c0 = 0;
+      Dp = Dpn;
+      Dpn = desc(p_it + GW);
+    }
+  };
+  for (int q = 0; q < NS; q++) produce();
+  int c_it = gw, c_c0 = 0, c_seq = 0;
+  S2ItemDev Dc = desc(c_it), Dn = desc(c_it + GW);
+  Acc acc[VEC];
+#pragma unroll
+  for (int v = 0; v < VEC; v++) acc[v] = 0;
+  while (c_it < ntot) {
+    const bool sec = c_it >= n0;
+    const MatDev& M = sec ? m1 : m0;
+    const int s = c_seq % NS;
+    if (!stage_ready(&R.bar[s], (uint32_t)((c_seq / NS) & 1), M.err)) {
+      drain<NS>(R.bar, c_seq, p_seq);
+      return;
+    }
+    const int nc = min(chunk_cols_dev(Dc.ntp, ESZ), Dc.ncols - c_c0);
+    const T* st = (const T*)(R.buf + s * kStageAll);
+    const int32_t* ix = (const int32_t*)(R.buf + s * kStageAll + kStage);
+    // multipliers of the chunk's columns
+    const Acc* zv = (const Acc*)M.z;
+    for (int k = lane; k < nc; k += 32) {
+      const int mi = ix[k];
+      musm[k] = mi >= 0 ? __ldcg(&zv[mi]) : (Acc)__ldg(&x[-mi - 1]);
+    }
+    __syncwarp();
+    const int nq = Dc.ntp / VEC;
+    const int lw = log2ceil(nq), LW = 1 << lw, CS = 32 >> lw;
+    const int slot = lane >> lw, j = lane & (LW - 1);
+    if (j < nq) {
+      // two accumulator sets over alternating columns: independent FMA chains
+      Acc acc2[VEC];
+#pragma unroll
+      for (int v = 0; v < VEC; v++) acc2[v] = 0;
+      int r0 = 0;
+      for (; r0 + 2 * CS <= nc; r0 += 2 * CS) {
+        const int sg = r0 + slot;
+        const Acc mu0 = musm[sg], mu1 = musm[sg + CS];
+        Acc a[VEC], b[VEC];
+        lds16(st + sg * Dc.ntp + j * VEC, a);
+        lds16(st + (sg + CS) * Dc.ntp + j * VEC, b);
+#pragma unroll
+        for (int v = 0; v < VEC; v++) {
+          acc[v] += a[v] * mu0;
+          acc2[v] += b[v] * mu1;
+        }
+      }
+      for (; r0 < nc; r0 += CS) {
+        const int sg = r0 + slot;
+        if (sg < nc) {
+          const Acc mu = musm[sg];
+          Acc a[VEC];
+          lds16(st + sg * Dc.ntp + j * VEC, a);
+#pragma unroll
+          for (int v = 0; v < VEC; v++) acc[v] += a[v] * mu;
+        }
+      }
+#pragma unroll
+      for (int v = 0; v < VEC; v++) acc[v] += acc2[v];
+    }
+    __syncwarp();
+    c_seq++;
+    produce();
+    c_c0 += nc;
+    if (c_c0 < Dc.ncols) continue;
+    // item done: combine the column slots, write the tile's rows
+#pragma unroll
+    for (int v = 0; v < VEC; v++)
+      for (int o = LW; o < 32; o <<= 1) acc[v] += __shfl_xor_sync(0xffffffffu, acc[v], o);
+    if (slot == 0 && j < nq) {
+      Acc* gp = (Acc*)M.gpart + Dc.pout;
+#pragma unroll
+      for (int v = 0; v < VEC; v++)
+        if (j * VEC + v < Dc.nr) gp[j * VEC + v] = acc[v];
+    }
+#pragma unroll
+    for (int v = 0; v < VEC; v++) acc[v] = 0;
+    c_it += GW;
+    c_c0 = 0;
+    Dc = Dn;
+    Dn = desc(c_it + GW);
+  }
+}
+
+// ------------------------------------------------------ store conversion
+// one warp per column segment: dst[r] = (T) body[src + r * stride], r < len
+template <typename T>
+__global__ void segcopy_kernel(const double* __restrict__ body, const SegCopyDev* __restrict__ map, int64_t nmap,
+                               T* __restrict__ dst) {
+  const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = (gridDim.x * (int64_t)blockDim.x) >> 5;
+  for (int64_t q = w; q < nmap; q += nw) {
+    const SegCopyDev c = map[q];
+    for (int r = lane; r < c.len; r += 32) {
+      const double v = body[c.src + (int64_t)r * c.stride];
+      if constexpr (sizeof(T) == 8) dst[c.dst + r] = v;
+      else if constexpr (sizeof(T) == 4) dst[c.dst + r] = (float)v;
+      else dst[c.dst + r] = __double2bfloat16(v);
+    }
+  }
+}
+
+// ------------------------------------------------------------- launchers
+namespace {
+
+// warps per block and stages per warp (one block per SM); the block's
+// shared memory: NW x NS x 17 KB + multipliers + barriers
+template <int NW, int NS>
+constexpr size_t smem_bytes() {
+  return (size_t)NW * NS * kStageAll + (size_t)NW * 256 * 8 + (size_t)NW * NS * 8;
+}
+
+template <typename K>
+void set_smem_once(K kernel, size_t bytes) {
+  static std::mutex mu;
+  static const void* done[64];
+  static int ndone = 0;
+  std::lock_guard<std::mutex> lock(mu);
+  for (int i = 0; i < ndone; i++)
+    if (done[i] == (const void*)kernel) return;
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (ndone < 64) done[ndone++] = (const void*)kernel;
+}
+
+// pipeline shape: 6 warps x 2 stages (default; measured fastest on c2 for
+// all three storage types), 4 x 3 or 3 x 4 -- HBI_STREAM_SHAPE = 1, 0, 2
+int stream_shape() {
+  static int shape = -1;
+  if (shape < 0) {
+    const char* e = getenv("HBI_STREAM_SHAPE");
+    shape = e ? atoi(e) : 1;
+    if (shape < 0 || shape > 2) shape = 1;
+  }
+  return shape;
+}
+
+template <typename T, int NW, int NS>
+void launch_p1_shape(const MatDev& m0, const MatDev& m1, int nmat, const double* x, int sm, int n, cudaStream_t st) {
+  const int need = (n + NW - 1) / NW;
+  const int grid = need < sm ? (need > 0 ? need : 1) : sm;
+  set_smem_once(p1_stream_kernel<T, NW, NS>, smem_bytes<NW, NS>());
+  p1_stream_kernel<T, NW, NS><<<grid, NW * 32, smem_bytes<NW, NS>(), st>>>(m0, m1, nmat, x);
+}
+
+template <typename T, int NW, int NS>
+void launch_p2_shape(const MatDev& m0, const MatDev& m1, int nmat, const double* x, int sm, int n, cudaStream_t st) {
+  const int need = (n + NW - 1) / NW;
+  const int grid = need < sm ? (need > 0 ? need : 1) : sm;
+  set_smem_once(p2_stream_kernel<T, NW, NS>, smem_bytes<NW, NS>());
+  p2_stream_kernel<T, NW, NS><<<grid, NW * 32, smem_bytes<NW, NS>(), st>>>(m0, m1, nmat, x);
+}
+
+template <typename T>
+void launch_p1(const MatDev& m0, const MatDev& m1, int nmat, const double* x, int sm, cudaStream_t st) {
+  const int n = m0.ns1 + (nmat == 2 ? m1.ns1 : 0);
+  if (n == 0) return;
+  switch (stream_shape()) {
+    case 1: launch_p1_shape<T, 6, 2>(m0, m1, nmat, x, sm, n, st); break;
+    case 2: launch_p1_shape<T, 3, 4>(m0, m1, nmat, x, sm, n, st); break;
+    default: launch_p1_shape<T, 4, 3>(m0, m1, nmat, x, sm, n, st);
+  }
+}
+
+template <typename T>
+void launch_p2(const MatDev& m0, const MatDev& m1, int nmat, const double* x, int sm, cudaStream_t st) {
+  const int n = m0.ns2 + (nmat == 2 ? m1.ns2 : 0);
+  if (n == 0) return;
+  switch (stream_shape()) {
+    case 1: launch_p2_shape<T, 6, 2>(m0, m1, nmat, x, sm, n, st); break;
+    case 2: launch_p2_shape<T, 3, 4>(m0, m1, nmat, x, sm, n, st); break;
+    default: launch_p2_shape<T, 4, 3>(m0, m1, nmat, x, sm, n, st);
+  }
+}
+
+template <typename T>
+void prepare_type() {
+  set_smem_once(p1_stream_kernel<T, 4, 3>, smem_bytes<4, 3>());
+  set_smem_once(p1_stream_kernel<T, 6, 2>, smem_bytes<6, 2>());
+  set_smem_once(p1_stream_kernel<T, 3, 4>, smem_bytes<3, 4>());
+  set_smem_once(p2_stream_kernel<T, 4, 3>, smem_bytes<4, 3>());
+  set_smem_once(p2_stream_kernel<T, 6, 2>, smem_bytes<6, 2>());
+  set_smem_once(p2_stream_kernel<T, 3, 4>, smem_bytes<3, 4>());
+}
+
+}  // namespace
+
+// the large shared-memory opt-in of the phase kernels, once per process and
+// before any stream capture
+void prepare_stream_kernels() {
+  prepare_type<double>();
+  prepare_type<float>();
+  prepare_type<__nv_bfloat16>();
+}
+
+// both H-matrices of a stage in one grid per phase (same storage type)
+void launch_phase1(const MatDev* mats, int nmat, const double* x, int sm, cudaStream_t st) {
+  const MatDev& m0 = mats[0];
+  const MatDev& m1 = nmat == 2 ? mats[1] : mats[0];
+  if (m0.storage == ST_F64) launch_p1<double>(m0, m1, nmat, x, sm, st);
+  else if (m0.storage == ST_F32) launch_p1<float>(m0, m1, nmat, x, sm, st);
+  else launch_p1<__nv_bfloat16>(m0, m1, nmat, x, sm, st);
+}
+
+void launch_phase2(const MatDev* mats, int nmat, const double* x, int sm, cudaStream_t st) {
+  const MatDev& m0 = mats[0];
+  const MatDev& m1 = nmat == 2 ? mats[1] : mats[0];
+  if (m0.storage == ST_F64) launch_p2<double>(m0, m1, nmat, x, sm, st);
+  else if (m0.storage == ST_F32) launch_p2<float>(m0, m1, nmat, x, sm, st);
+  else launch_p2<__nv_bfloat16>(m0, m1, nmat, x, sm, st);
+}
+
+void launch_segcopy(const double* body, const SegCopyDev* map, int64_t nmap, void* dst, int storage,
+                    cudaStream_t st) {
+  if (nmap == 0) return;
+  const int blocks = (int)std::min<int64_t>((nmap + 7) / 8, 152 * 16);
+  if (storage == ST_F64) segcopy_kernel<double><<<blocks, 256, 0, st>>>(body, map, nmap, (double*)dst);
+  else if (storage == ST_F32) segcopy_kernel<float><<<blocks, 256, 0, st>>>(body, map, nmap, (float*)dst);
+  else segcopy_kernel<__nv_bfloat16><<<blocks, 256, 0, st>>>(body, map, nmap, (__nv_bfloat16*)dst);
+}
+
+}  // namespace hbi

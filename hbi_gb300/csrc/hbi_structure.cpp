@@ -362,4 +362,138 @@ void plan_chains(int n, const std::vector<Leaf>& leaves, ChainPlan& cp) {
   }
 }
 
+void plan_stream(int n, const std::vector<Leaf>& leaves, const std::vector<int64_t>& body_off, int vec,
+                 StreamPlan& sp) {
+  const int nl = (int)leaves.size();
+  const int tr = 32 * vec;
+  sp = StreamPlan();
+  sp.vec = vec;
+  sp.tr = tr;
+  int64_t fe = 0;
+  for (const Leaf& L : leaves) fe += L.ltmtx == 1 ? (int64_t)L.kt * (L.ndl + L.ndt) : (int64_t)L.ndl * L.ndt;
+  sp.factor_elems = fe;
+  // ---- phase 1: column groups of the low-rank leaves ----
+  std::vector<std::pair<std::pair<int, int>, int>> ck;  // ((col0, -ndt), leaf)
+  for (int i = 0; i < nl; i++)
+    if (leaves[i].ltmtx == 1 && leaves[i].kt > 0) ck.push_back({{leaves[i].nstrtt - 1, -leaves[i].ndt}, i});
+  std::stable_sort(ck.begin(), ck.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+  std::vector<int32_t> leaf_z(nl, -1);
+  int64_t voff = 0, z = 0, poff = 0, ncg = 0;
+  for (size_t a = 0; a < ck.size();) {
+    size_t b = a;
+    while (b < ck.size() && ck[b].first == ck[a].first) b++;
+    const int col0 = ck[a].first.first, ndt = -ck[a].first.second;
+    int ncols = 0;
+    for (size_t e = a; e < b; e++) {
+      leaf_z[ck[e].second] = (int32_t)(z + ncols);
+      ncols += leaves[ck[e].second].kt;
+    }
+    const int ntile = (ndt + tr - 1) / tr;
+    const int64_t poff0 = poff;
+    if (ntile > 1) poff += (int64_t)ntile * ncols;
+    for (int t = 0; t < ntile; t++) {
+      const int nt = std::min(tr, ndt - t * tr);
+      const int ntp = (int)round_up(nt, vec);
+      const int64_t region = voff;
+      int c = 0;
+      for (size_t e = a; e < b; e++) {
+        const int li = ck[e].second;
+        const Leaf& L = leaves[li];
+        for (int k = 0; k < L.kt; k++, c++)
+          sp.vcopy.push_back(SegCopy{region + (int64_t)c * ntp, body_off[li] + (int64_t)k * L.ndt + (int64_t)t * tr,
+                                     nt, 1});
+      }
+      S1Item it{};
+      it.soff = region;
+      it.ncols = ncols;
+      it.ntp = ntp;
+      it.x0 = col0 + t * tr;
+      it.nt = nt;
+      it.z0 = (int32_t)z;
+      it.cg = (int32_t)ncg;
+      it.tile = t;
+      it.ntile = ntile;
+      it.poff = ntile > 1 ? (int32_t)poff0 : -1;
+      sp.p1.push_back(it);
+      voff += (int64_t)ncols * ntp;
+    }
+    ncg++;
+    z += ncols;
+    a = b;
+  }
+  sp.vstore = round_up(voff, vec);
+  sp.zlen = z;
+  sp.plen1 = poff;
+  sp.ncg = ncg;
+  // ---- phase 2: row groups of all leaves ----
+  plan_groups(n, leaves, sp.gp);
+  const GroupPlan& gp = sp.gp;
+  const int ng = (int)gp.grow0.size();
+  sp.gnch.assign(ng, 1);
+  sp.gpoff2.assign(ng, 0);
+  int64_t uoff = 0, p2off = 0;
+  for (int g = 0; g < ng; g++) {
+    const int ndl = gp.gndl[g];
+    while (sp.midx.size() % 4) sp.midx.push_back(0);
+    const int m0 = (int)sp.midx.size();
+    for (int e = gp.gleaf_ptr[g]; e < gp.gleaf_ptr[g + 1]; e++) {
+      const int li = gp.gleaf[e];
+      const Leaf& L = leaves[li];
+      if (L.ltmtx == 1) {
+        for (int k = 0; k < L.kt; k++) sp.midx.push_back(leaf_z[li] + k);
+      } else {
+        for (int k = 0; k < L.ndt; k++) sp.midx.push_back(-(L.nstrtt - 1 + k) - 1);
+      }
+    }
+    const int ncols = (int)sp.midx.size() - m0;
+    sp.gpoff2[g] = (int32_t)p2off;
+    p2off += ndl;
+    if (ncols == 0) {
+      sp.gnch[g] = 0;
+      continue;
+    }
+    const int ntile = (ndl + tr - 1) / tr;
+    for (int t = 0; t < ntile; t++) {
+      const int nr = std::min(tr, ndl - t * tr);
+      const int ntp = (int)round_up(nr, vec);
+      const int64_t region = uoff;
+      int c = 0;
+      for (int e = gp.gleaf_ptr[g]; e < gp.gleaf_ptr[g + 1]; e++) {
+        const int li = gp.gleaf[e];
+        const Leaf& L = leaves[li];
+        if (L.ltmtx == 1) {
+          const int64_t u0 = body_off[li] + (int64_t)L.ndt * L.kt;
+          for (int k = 0; k < L.kt; k++, c++)
+            sp.ucopy.push_back(SegCopy{region + (int64_t)c * ntp, u0 + (int64_t)k * L.ndl + (int64_t)t * tr, nr, 1});
+        } else {
+          // a1(ndt, ndl): element (it, il) at it + il*ndt; column it, rows il
+          for (int k = 0; k < L.ndt; k++, c++)
+            sp.ucopy.push_back(SegCopy{region + (int64_t)c * ntp, body_off[li] + k + (int64_t)t * tr * L.ndt, nr,
+                                       L.ndt});
+        }
+      }
+      S2Item it{};
+      it.soff = region;
+      it.ncols = ncols;
+      it.ntp = ntp;
+      it.nr = nr;
+      it.m0 = m0;
+      it.pout = (int32_t)(sp.gpoff2[g] + t * tr);
+      sp.p2.push_back(it);
+      uoff += (int64_t)ncols * ntp;
+    }
+  }
+  while (sp.midx.size() % 4) sp.midx.push_back(0);
+  sp.midx.resize(sp.midx.size() + 256, 0);  // chunk copies may read a whole chunk's worth past a group
+  sp.ustore = round_up(uoff, vec);
+  sp.plen2 = p2off;
+  // big items first, for the static warp schedule
+  std::stable_sort(sp.p1.begin(), sp.p1.end(), [](const S1Item& a, const S1Item& b) {
+    return (int64_t)a.ncols * a.ntp > (int64_t)b.ncols * b.ntp;
+  });
+  std::stable_sort(sp.p2.begin(), sp.p2.end(), [](const S2Item& a, const S2Item& b) {
+    return (int64_t)a.ncols * a.ntp > (int64_t)b.ncols * b.ntp;
+  });
+}
+
 }  // namespace hbi

@@ -102,4 +102,62 @@ void plan_groups(int n, const std::vector<Leaf>& leaves, GroupPlan& gp);
 // warp schedule; cost uses kt, so the order is per matrix
 void plan_p2_items(const std::vector<Leaf>& leaves, const GroupPlan& gp, int vec, std::vector<P2Item>& items);
 
+// ---- streamed product plan ---------------------------------------------
+// The factor store is re-laid out in row tiles of up to 32*vec rows (one
+// 16-byte vector per lane, 512 bytes per column segment) so that each work
+// item of the product is ONE contiguous region, which the kernels stream into
+// shared memory in chunks of at most 16 KB by bulk asynchronous copies (TMA):
+//   phase 1 (z = V^T x): the low-rank leaves sharing a column cluster form a
+//     column group; item = (column group, row tile) over all its columns;
+//   phase 2 (y = U z + A x): the leaves sharing a row cluster form a row group
+//     (plan_groups); item = (row group, row tile) over all its columns.
+// Within a region, column segments follow the group's leaf order and each
+// leaf's column order; segments are padded with zeros to a multiple of vec.
+// Items are ordered by decreasing size for the static warp schedule.
+struct S1Item {
+  int64_t soff;            // element offset of the region in the V store
+  int32_t ncols, ntp;      // columns, padded rows per column
+  int32_t x0, nt;          // 0-based first row of x, valid rows
+  int32_t z0;              // z index of the first column
+  int32_t cg;              // column group (arrival counter) when ntile > 1
+  int32_t tile, ntile;     // row tile of the column group, tiles of the group
+  int32_t poff;            // phase-1 partials of the group (ntile x ncols)
+  int32_t pad;
+};
+struct S2Item {
+  int64_t soff;            // element offset of the region in the U store
+  int32_t ncols, ntp, nr;  // columns, padded rows, valid rows
+  int32_t m0;              // multiplier index (into midx) of column 0; a multiple of 4
+  int32_t pout;            // partial row sums: gpart[pout .. pout+nr)
+  int32_t pad;
+};
+struct SegCopy {           // conversion of one column segment from the FP64 body
+  int64_t dst, src;        // element offsets (dst in the V or U store)
+  int32_t len, stride;     // valid rows, source element stride between rows
+};
+struct StreamPlan {
+  int vec = 1, tr = 1;
+  std::vector<S1Item> p1;
+  std::vector<S2Item> p2;
+  int64_t vstore = 0, ustore = 0;    // elements
+  int64_t zlen = 0, plen1 = 0, ncg = 0, plen2 = 0;
+  std::vector<int32_t> midx;         // per row-group column: z index, or -(x index)-1; groups padded to 4
+  GroupPlan gp;                      // row groups, fine ranges
+  std::vector<int32_t> gnch;         // partial columns per row group (1)
+  std::vector<int32_t> gpoff2;       // partial offset per row group
+  std::vector<SegCopy> vcopy, ucopy; // conversion maps
+  int64_t factor_elems = 0;
+};
+// columns of one streamed chunk: as many whole columns as fit in 16 KB, a
+// multiple of 32 (ntp * esz <= 512, so at least 32), and at most 256 (the
+// per-warp multiplier and column-index buffers of the phase-2 kernel)
+inline int chunk_cols(int ntp, int esz) {
+  const int c = (16384 / (ntp * esz)) / 32 * 32;
+  return c < 256 ? c : 256;
+}
+// body_off: element offset of each leaf in the HACApK FP64 body (low rank:
+// [V ndt x kt][U ndl x kt] column-major; dense a1(ndt, ndl))
+void plan_stream(int n, const std::vector<Leaf>& leaves, const std::vector<int64_t>& body_off, int vec,
+                 StreamPlan& sp);
+
 }  // namespace hbi

@@ -18,8 +18,8 @@ import numpy as np
 
 from . import MLP, proposer_size
 
-E_TARGET = 0.5
-LO, HI = -1.0, 0.3
+E_TARGET = 0.35
+LO, HI = -1.0, 0.2
 TINY = 1e-30
 
 
@@ -64,14 +64,18 @@ def pack(params, mean, sd, lo=LO, hi=HI):
     return w
 
 
-def train(X, T, epochs=40, batch=1024, lr=2e-3, seed=0):
-    """Fit the proposer on the GPU; returns (weight vector, loss per epoch)."""
+def train(X, T, epochs=40, batch=1024, lr=2e-3, seed=0, min_steps=3000):
+    """Fit the proposer on the GPU; returns (weight vector, loss per epoch).
+    Small traces get smaller batches and more epochs, so that every fit takes
+    at least `min_steps` Adam steps."""
     nin, hid, _ = proposer_size()
+    batch = int(min(batch, max(64, len(T) // 8)))
+    epochs = int(max(epochs, -(-min_steps * batch // max(1, len(T)))))
     mean = X.mean(axis=0)
     sd = X.std(axis=0)
     sd = np.where(sd > 1e-6, sd, 1.0)
     Xs = ((X - mean) / sd).astype(np.float32)
-    m = MLP(nin, hid, batch_max=max(batch, 1024))
+    m = MLP(nin, hid, batch_max=max(batch, 64))
     m.init(seed)
     hist = m.train(Xs, T, epochs=epochs, batch=min(batch, len(T)), lr=lr, seed=seed)
     w = pack(m.params(), mean, sd)

@@ -282,6 +282,17 @@ int hbi_mlp_train(hbi_mlp* m, const float* x, const float* t, long long n, int e
                   unsigned long long seed, float* loss_per_epoch);
 int hbi_mlp_predict(hbi_mlp* m, const float* x, long long n, float* out);
 
+/* Host-only self check of the product's work plan (no GPU, no reference
+ * counterpart): builds the row-tiled stores and work items for a leaf list
+ * leaves6[nleaf][6] = {ltmtx, kt, nstrtl, ndl, nstrtt, ndt} with vec elements
+ * per 16 bytes, checks every bound the kernels rely on, and evaluates y = H x
+ * from the HACApK-packed FP64 body by walking the items as the kernels do.
+ * stats[8]: items of phase 1 and 2, V and U store elements, z length,
+ * phase-1 and phase-2 partials, conversion segments.  HBI_ERR_STATE names the
+ * violated bound. */
+int hbi_plan_emulate(int n, int nleaf, const int* leaves6, const double* body, int vec, const double* x,
+                     double* y, int64_t* stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -71,7 +71,9 @@ def test_gpu_rk_step_matches_golden():
     lh = H.LHp(lf, ctl, "f64")
     ndc, lodc = H.HACApK_gen_lattice_vector(ctl)
     y0, p = wl.initial_state(lodc)
-    assert np.array_equal(y0, G["rk_y0"])
+    # the host's libm (numpy log/sinh) may differ in the last bit between machines
+    assert np.allclose(y0, G["rk_y0"], rtol=1e-13, atol=0)
+    y0 = G["rk_y0"]
     rk = H.RK(lh, None, evlaw=0, a=p["a"], b=p["b"], dc=p["dc"], f0=p["f0"], vpl=p["vpl"])
     rk.set_state(y0)
     yo, ye, _ = rk.rkck(float(G["rk_h"][0]), 1.0)

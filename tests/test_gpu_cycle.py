@@ -12,7 +12,7 @@ earthquake.  Tolerances:
     differences that accumulate over the steps;
   * the first event: onset time within 1e-6 relative, hypocentre equal, mean
     slip within 1e-6 relative (the nucleation amplifies the round-off of the
-    steps before it);
+    steps before it); the mean friction after the event within 1e-5;
   * the loop is deterministic: a run split by a step limit gives the same
     records as one run, bit for bit; a time limit is landed on exactly.
 """
@@ -84,8 +84,8 @@ def test_cycle_follows_oracle_loop(system, oracle_run):
     assert e_g["hypoloc"] == int(e_o[4])
     assert abs(e_g["onset"] - e_o[2]) <= 1e-6 * e_o[2]
     assert abs(e_g["moment"] - e_o[3]) <= 1e-6 * abs(e_o[3])
-    # monitors of the last step
-    assert abs(st["meanmu"] - rec[-1, 8]) <= 1e-6 * abs(rec[-1, 8])
+    # monitors of the last step, after the event has amplified the round-off
+    assert abs(st["meanmu"] - rec[-1, 8]) <= 1e-5 * abs(rec[-1, 8])
     assert st["rejected"] == int(tr[:, 4].size - STEPS)
 
 

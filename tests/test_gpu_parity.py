@@ -259,3 +259,21 @@ def test_rkqs_underflow_is_a_status_not_a_stop(built):
     y[1::3] *= 1 + 1e-3 * np.sin(np.arange(n))
     rk.set_state(y)
     rk.rkqs(0.0, 1.0, 1e-6)
+
+
+@pytest.mark.parametrize("store,tol", [("f64", 1e-12), ("f32", 1e-5), ("bf16", 2e-2)])
+def test_matvec_large_operator(oracle, store, tol):
+    """A 128 x 128 3dph operator (16,384 elements; row groups with hundreds of
+    columns, column groups over many row tiles, chunked streams): the product
+    of the GPU store against the oracle's product of the same FP64 factors."""
+    prob, n, g, w, eps = case("3dph", (128, 128))
+    ctl = H.Ctl(n)
+    lf = H.LeafMtxp(ctl, product_geometry(prob, n, g, w, "s"), eps)
+    off, body = lf.body()
+    Hg = oracle.HMatrix.from_body(n, lf.leaves(), off, body)
+    lh = H.LHp(lf, ctl, store)
+    u = np.random.default_rng(8).standard_normal(n)
+    ref = Hg.matvec(u)
+    y = lh.matvec(u)
+    assert np.linalg.norm(y - ref) <= tol * np.linalg.norm(ref)
+    assert np.array_equal(y, lh.matvec(u))

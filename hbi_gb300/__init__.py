@@ -39,7 +39,7 @@ EXPORTS = [
     "hbi_cycle_create", "hbi_cycle_run", "hbi_cycle_fields", "hbi_cycle_events", "hbi_cycle_trace",
     "hbi_cycle_free", "hbi_cycle_set_proposer", "hbi_cycle_proposer_size",
     "hbi_mlp_create", "hbi_mlp_free", "hbi_mlp_set_params", "hbi_mlp_get_params", "hbi_mlp_loss_grad",
-    "hbi_mlp_train", "hbi_mlp_predict", "hbi_plan_emulate",
+    "hbi_mlp_train", "hbi_mlp_predict", "hbi_plan_emulate", "hbi_umma_probe",
 ]
 
 
@@ -574,3 +574,13 @@ def plan_emulate(n, leaves, body, vec, x):
                                   st.ctypes.data_as(_i64p)), "hbi_plan_emulate")
     keys = ("items1", "items2", "vstore", "ustore", "zlen", "plen1", "plen2", "segments")
     return y, dict(zip(keys, (int(v) for v in st)))
+
+
+def umma_probe(a_bf16_bits, b_bf16_bits, variant=0):
+    """One tcgen05 MMA on the GPU: (128x16) x (64x16)^T from BF16 bit patterns."""
+    a = np.ascontiguousarray(a_bf16_bits, dtype=np.uint16)
+    b = np.ascontiguousarray(b_bf16_bits, dtype=np.uint16)
+    d = np.zeros((128, 64), dtype=np.float32)
+    _check(lib().hbi_umma_probe(a.ctypes.data_as(C.POINTER(C.c_uint16)), b.ctypes.data_as(C.POINTER(C.c_uint16)),
+                                d.ctypes.data_as(_fp), int(variant)), "hbi_umma_probe")
+    return d

@@ -160,7 +160,7 @@ __device__ double proposer_eval(const ProposerDev& M, const float* in, float* sh
 
 // the proposer network: inputs, hidden width; the feature order is shared
 // with the trainer
-#define HBI_PROPOSER_NIN 6
+#define HBI_PROPOSER_NIN 7
 #define HBI_PROPOSER_HID 64
 __host__ __device__ constexpr int proposer_weights(int nin, int hid) {
   return hid * nin + hid + hid * hid + hid + hid + 1;
@@ -168,8 +168,8 @@ __host__ __device__ constexpr int proposer_weights(int nin, int hid) {
 
 // the proposer's features, all known once step k is accepted and before step
 // k+1 is tried: this step's error and the previous one's, the step growth,
-// the slip-rate trend of the last two steps, the rejections of this step and
-// the rkqs growth factor
+// the slip-rate trend of the last two steps, the rejections of this step, the
+// rkqs growth factor and the maximum slip rate
 __host__ __device__ inline void proposer_features(double e, double e_prev, double h, double h_prev, double v1,
                                                   double v2, int nrjct, double hnext, float* f) {
   const double tiny = 1e-30;
@@ -179,6 +179,7 @@ __host__ __device__ inline void proposer_features(double e, double e_prev, doubl
   f[3] = (float)(log10(fmax(v1, tiny)) - log10(fmax(v2, tiny)));
   f[4] = (float)nrjct;
   f[5] = (float)log10(fmax(hnext, tiny) / fmax(h, tiny));
+  f[6] = (float)log10(fmax(v1, tiny));
 }
 
 namespace {

@@ -1,0 +1,84 @@
+// hbi_umma.cuh -- 5th-generation tensor core (tcgen05) primitives in inline
+// PTX: tensor-memory allocation, shared-memory matrix descriptors, the MMA
+// issue, its commit to an mbarrier and tensor-memory loads.
+//
+// Operand layouts are the canonical no-swizzle ("interleaved") layouts of
+// 16-bit elements: the matrix is a grid of 8 x 8 core matrices, each 128
+// contiguous bytes holding 8 rows of 16 bytes; for a K-major operand a row is
+// 8 consecutive K elements of one M (or N) index.  The descriptor's leading
+// byte offset is the distance between core matrices adjacent in K, the stride
+// byte offset between core matrices adjacent in M (or N).
+#pragma once
+#include <cstdint>
+
+namespace hbi {
+namespace umma {
+
+__device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor (SWIZZLE_NONE, descriptor version 1)
+__device__ __forceinline__ uint64_t smem_desc(const void* p, uint32_t lbo, uint32_t sbo) {
+  const uint64_t a = (saddr(p) & 0x3FFFFu) >> 4;
+  return a | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) | ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) |
+         ((uint64_t)1 << 46);
+}
+
+// instruction descriptor of kind::f16: BF16 A and B, FP32 D, both K-major
+__host__ __device__ constexpr uint32_t idesc_bf16_f32(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* smem_dst, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(smem_dst)),
+               "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                         int accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// arrive on an mbarrier when every MMA issued so far by this thread is done
+__device__ __forceinline__ void commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(saddr(bar))
+               : "memory");
+}
+
+// 32 lanes x 32 bits, 16 columns: thread t of the warp gets lane (base + t),
+// columns [col, col+16)
+__device__ __forceinline__ void ld_32x32b_x16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// byte offset of element (row, k) of a K-major operand whose rows are
+// grouped in blocks of 8 (core matrices) with the given LBO / SBO
+__host__ __device__ inline uint32_t kmajor_offset(int row, int k, uint32_t lbo, uint32_t sbo) {
+  return (uint32_t)(k >> 3) * lbo + (uint32_t)(row >> 3) * sbo + (uint32_t)(row & 7) * 16 + (uint32_t)(k & 7) * 2;
+}
+
+}  // namespace umma
+}  // namespace hbi

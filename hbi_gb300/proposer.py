@@ -1,12 +1,15 @@
 """Learned step-size proposer: training data from the solver's own traces,
 training on the GPU (hbi_mlp_* kernels) and packing for the time loop.
 
-After step k is accepted, the time loop feeds the MLP six numbers known at
+After step k is accepted, the time loop feeds the MLP seven numbers known at
 that moment (the features of hbi_cycle.cu's proposer_features): log10 of this
 step's error and of the previous one, the step growth log10(h_k/h_{k-1}), the
 slip-rate trend log10(V_{k-1}/V_{k-2}) of the monitors, the rejections of
-this step, and rkqs's own growth log10(h_next/h_k).  The network answers
-d = log10(h_try / rkqs h_next) for step k+1, clamped to [lo, hi].
+this step, rkqs's own growth log10(h_next/h_k) and log10 V_{k-1}.  The network
+answers d = log10(h_try / rkqs h_next) for step k+1, clamped to [lo, hi].
+With hi = 0 the proposer only ever shortens rkqs's step: it acts where it
+foresees a rejection (the error growing faster than rkqs assumes, as when a
+rupture nucleates) and leaves rkqs's step alone elsewhere.
 
 The training target comes from the trace of a run: the first attempt of step
 k+1 was tried with h1 and gave error e1; Cash-Karp's error scales with h**5,
@@ -18,8 +21,8 @@ import numpy as np
 
 from . import MLP, proposer_size
 
-E_TARGET = 0.35
-LO, HI = -1.0, 0.2
+E_TARGET = 0.5
+LO, HI = -1.0, 0.0
 TINY = 1e-30
 
 
@@ -28,9 +31,9 @@ def _l10(v):
 
 
 def features(e, e_prev, h, h_prev, v1, v2, nrjct, hnext):
-    """The six inputs, as the device computes them (float32)."""
+    """The seven inputs, as the device computes them (float32)."""
     f = np.stack([_l10(e), _l10(e_prev), _l10(h) - _l10(h_prev), _l10(v1) - _l10(v2), np.asarray(nrjct, float),
-                  _l10(hnext) - _l10(h)], axis=-1)
+                  _l10(hnext) - _l10(h), _l10(v1)], axis=-1)
     return f.astype(np.float32)
 
 

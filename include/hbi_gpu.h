@@ -293,6 +293,13 @@ int hbi_mlp_predict(hbi_mlp* m, const float* x, long long n, float* out);
 int hbi_plan_emulate(int n, int nleaf, const int* leaves6, const double* body, int vec, const double* x,
                      double* y, int64_t* stats);
 
+/* Self test of the tensor-core path (no reference counterpart): one
+ * tcgen05 MMA, D[128][64] = A[128][16] * B[64][16]^T with BF16 operands (raw
+ * bit patterns) from canonical K-major shared-memory layouts and FP32
+ * accumulation in tensor memory.  variant 0 uses the descriptor convention of
+ * the ensemble kernels; variant 1 swaps its two stride fields. */
+int hbi_umma_probe(const uint16_t* a, const uint16_t* b, float* d, int variant);
+
 #ifdef __cplusplus
 }
 #endif

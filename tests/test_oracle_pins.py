@@ -152,15 +152,21 @@ def test_proposer_labels_recover_the_ideal_step():
     rows = []
     hstar = 10.0 ** rng.uniform(1, 3, n)
     hnext = hstar * 10.0 ** rng.uniform(-0.3, 0.3, n)
+    # step k+1 is first tried at h1 = hnext[k] (the rkqs proposal of step k)
+    # with error e1 = E_TARGET (h1/hstar)**5; a rejected first try is
+    # followed by an accepted retry at hstar
+    acc = [(hstar[0], proposer.E_TARGET)]
+    for k in range(1, n):
+        h1 = hnext[k - 1]
+        e1 = proposer.E_TARGET * (h1 / hstar[k]) ** 5
+        acc.append((h1, e1) if e1 < 1.0 else (hstar[k], proposer.E_TARGET))
     for k in range(n):
-        # accepted attempt of step k with rkqs proposal hnext[k]; then the
-        # first attempt of step k+1 at h1 = hnext[k] with its error e1
-        rows.append([k + 1, 0.0, hstar[k], 0.5, 1, 1e-9, hnext[k], 0])
-        if k + 1 < n:
-            h1 = hnext[k]
-            e1 = proposer.E_TARGET * (h1 / hstar[k + 1]) ** 5
+        if k > 0:
+            h1 = hnext[k - 1]
+            e1 = proposer.E_TARGET * (h1 / hstar[k]) ** 5
             if e1 >= 1.0:
                 rows.append([k + 1, 0.0, h1, e1, 0, 1e-9, 0.0, 0])
+        rows.append([k + 1, 0.0, acc[k][0], acc[k][1], 1, 1e-9, hnext[k], 0])
     X, T = proposer.training_set(np.array(rows))
-    assert X.shape[1] == 6 and len(T) == n - 3
+    assert X.shape[1] == 7 and len(T) == n - 3
     assert np.allclose(T, np.log10(hstar[3:n] / hnext[2:n - 1]), atol=1e-5)

@@ -851,6 +851,20 @@ int rk_view(hbi_rk* r, RkView* v) {
   return HBI_OK;
 }
 int set_error(int code, const char* msg) { return fail(code, "%s", msg); }
+// for the ensemble (hbi_ens.cu)
+int lhp_view(hbi_lhp* h, LhpView* v) {
+  if (!h || !v) return fail(HBI_ERR_ARG, "null");
+  v->md = h->md;
+  v->n = h->n;
+  v->storage = h->storage;
+  v->zlen = h->plan.zlen;
+  v->plen1 = h->plan.plen1;
+  v->plen2 = h->plan.plen2;
+  v->ncg = h->plan.ncg;
+  v->sm = h->ctl->sm_count;
+  v->leaves = &h->leaves;
+  return HBI_OK;
+}
 }  // namespace hbi
 
 extern "C" int hbi_rk_set_state(hbi_rk* r, const double* y) {

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <vector>
 
 #include "hbi_entries.cuh"
 #include "hbi_structure.hpp"
@@ -89,6 +90,14 @@ struct RkDev {
   // time-loop flags (null outside the device-resident loop): [0] halted,
   // [1] halted or retrying, [2] retrying the same state (stage 1 is reused)
   const int* flags;
+};
+
+// host view of an operator, for the ensemble (hbi_ens.cu)
+struct LhpView {
+  MatDev md;
+  int n, storage, sm;
+  int64_t zlen, plen1, plen2, ncg;
+  const std::vector<Leaf>* leaves;
 };
 
 // host view of an RK handle, for the device-resident time loop (hbi_cycle.cu)

@@ -12,6 +12,7 @@
 #include <cuda_bf16.h>
 
 #include "hbi_kernels.cuh"
+#include "hbi_rsf.cuh"
 
 namespace hbi {
 
@@ -50,37 +51,6 @@ __global__ void __launch_bounds__(256) p3_plain_kernel(MatDev m0, MatDev m1, int
   if (r >= m0.n) return;
   y0[r] = row_value(m0, r);
   if (nmat == 2) y1[r] = row_value(m1, r);
-}
-
-// deriv (main_LH.f90:2165-2244): aging (0) and slip (1) laws
-__device__ __forceinline__ void deriv_dev(const RkDev& R, double sum_gs, double sum_gn, double psi, double tau,
-                                          double sig, double vel, double a, double b, double dc, double f0,
-                                          double* out) {
-  double dsig = sum_gn;
-  if (R.limitsigma) {
-    if (sig < R.minsig) dsig = 0;
-    if (sig > R.maxsig) dsig = 0;
-  }
-  const double vref = R.vref;
-  double dpsi;
-  if (R.evlaw == 0) {
-    dpsi = (b == 0) ? 0.0 : b / dc * vref * exp((f0 - psi) / b) - b * fabs(vel) / dc;
-  } else {
-    const double fss = f0 + (a - b) * log(fabs(vel) / vref);
-    dpsi = -(fabs(vel) / dc * (fabs(tau) / sig - fss));
-  }
-  const double e = exp(-psi / a), ch = cosh(tau / sig / a);
-  const double dvdtau = 2 * vref * e * ch / (a * sig);
-  const double dvdsig = -(2 * vref * e * ch * tau / (a * (sig * sig)));
-  const double dvdpsi = -vel / a;
-  const double t = sum_gs - R.rigid_over_2vs * (dvdpsi * dpsi + dvdsig * dsig);
-  out[0] = dpsi;
-  out[1] = t / (1.0 + R.rigid_over_2vs * dvdtau);
-  out[2] = dsig;
-}
-
-__device__ __forceinline__ double slip_rate(double vref, double psi, double tau, double sig, double a) {
-  return 2 * vref * exp(-psi / a) * sinh(tau / sig / a);
 }
 
 __global__ void __launch_bounds__(128) p3_rk_kernel(MatDev m0, MatDev m1, RkDev R, int s, double* __restrict__ xnext) {

@@ -293,6 +293,32 @@ int hbi_mlp_predict(hbi_mlp* m, const float* x, long long n, float* out);
 int hbi_plan_emulate(int n, int nleaf, const int* leaves6, const double* body, int vec, const double* x,
                      double* y, int64_t* stats);
 
+/* ---- ensemble of simulations sharing one H-matrix pair (no reference
+ * counterpart; configuration c4) -----------------------------------------
+ * `members` rate-and-state systems with per-member friction parameters b
+ * and dc run on the same lh_s / lh_n: every RK stage applies each H-matrix to
+ * all members' slip rates at once (a multi-vector product), and each member
+ * keeps its own FP64 state, step size and rkqs controller (main_LH.f90:
+ * 2270-2370).  Arrays are cluster order with the member index fastest:
+ * y[(3*i + c) * members + m], b[i * members + m].  p supplies a, f0, taudot,
+ * sigdot, vpl (per element) and the law; its b and dc are ignored. */
+typedef struct hbi_ens_s hbi_ens;
+typedef struct {
+  long long attempts;   /* ensemble attempts (each advances every active member) */
+  long long steps;      /* accepted member steps, summed over members */
+  long long rejected;   /* rejected member attempts, summed */
+  int done, failed;     /* members that reached t_limit; members whose step size underflowed */
+  double wall_s;
+} hbi_ens_status;
+int hbi_ens_create(hbi_ens** e, const hbi_rsf_params* p, hbi_lhp* lh_s, hbi_lhp* lh_n, int members,
+                   const double* b, const double* dc);
+int hbi_ens_free(hbi_ens* e);
+/* y (3*ncell*members), vel (ncell*members: the slip rate before the loop) */
+int hbi_ens_set_state(hbi_ens* e, const double* y, const double* vel);
+int hbi_ens_get_state(hbi_ens* e, double* y, double* slip, double* x);
+/* every member from x = 0 to exactly t_limit (s) */
+int hbi_ens_run(hbi_ens* e, double eps_r, double dtinit, double dtmax, double t_limit, hbi_ens_status* st);
+
 /* Self test of the tensor-core path (no reference counterpart): one
  * tcgen05 MMA, D[128][64] = A[128][16] * B[64][16]^T with BF16 operands (raw
  * bit patterns) from canonical K-major shared-memory layouts and FP32

@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--jmax", type=int, default=256)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mode", default="step", choices=["step", "matvec"])
+    ap.add_argument("--mode", default="step", choices=["step", "matvec", "ensemble"])
     ap.add_argument("--window-yr", type=float, default=100.0,
                     help="simulated window of the sim-yr/h comparison (0: skip it)")
     return ap.parse_args()
@@ -214,6 +214,44 @@ def run_matvec_mode(args):
               "phase2_us": round(t2 * 1e6, 2), "phase1_gbs": round(b1 / t1 / 1e9, 1),
               "phase2_gbs": round(b2 / t2 / 1e9, 1), "both_gbs": round((b1 + b2) / (t1 + t2) / 1e9, 1),
               "bytes": b1 + b2})
+
+
+def run_ensemble_mode(args):
+    """Configuration c4: 64 simulations with their own b and dc sharing the c2
+    H-matrices (FP32), every member from steady state to --window-yr; against
+    one member run alone through the single-system loop on the same window."""
+    import hbi_gb300 as H
+    from hbi_gb300 import configs
+    w = workload(args)
+    n = w.nd
+    ctl_s, ctl_n = H.Ctl(n), H.Ctl(n)
+    lf_s = H.LeafMtxp(ctl_s, w.geometry("s"), w.eps_h)
+    lf_n = H.LeafMtxp(ctl_n, w.geometry("n"), w.eps_h)
+    lh_s, lh_n = H.LHp(lf_s, ctl_s, "f32"), H.LHp(lf_n, ctl_n, "f32")
+    ndc, lodc = H.HACApK_gen_lattice_vector(ctl_s)
+    b_in, dc_m = configs.ensemble_params(64, seed=0)
+    y, vel, b, dc, p = configs.ensemble_state(w, lodc, b_in, dc_m)
+    T = args.window_yr * H.YEAR
+    ens = H.Ensemble(lh_s, lh_n, b, dc, evlaw=w.evlaw, scale=w.scale, a=p["a"], f0=p["f0"], vpl=p["vpl"])
+    ens.set_state(y, vel)
+    st = ens.run(T, eps_r=1e-6)
+    ds = w.ds_area[lodc - 1]
+    m = 0
+    rk = H.RK(lh_s, lh_n, evlaw=w.evlaw, scale=w.scale, a=p["a"], b=b[:, m], dc=dc[:, m], f0=p["f0"], vpl=p["vpl"])
+    rk.set_state(y[:, m])
+    cyc = H.Cycle(rk, vel[:, m], ds, eps_r=1e-6)
+    cs = cyc.run(t_limit=T)
+    ye, se, xe = ens.get_state()
+    y1 = rk.get_state()
+    member_yr_h = 64 * args.window_yr / st["wall_s"] * 3600
+    single_yr_h = args.window_yr / cs["wall_s"] * 3600
+    out_line({"mode": "ensemble", "workload": f"c4: 64 members on {w.name}", "members": 64,
+              "window_yr": args.window_yr, "wall_s": round(st["wall_s"], 2), "attempts": st["attempts"],
+              "member_steps": st["steps"], "member_rejected": st["rejected"], "done": st["done"],
+              "ms_per_attempt": round(st["wall_s"] / max(1, st["attempts"]) * 1e3, 3),
+              "member_sim_yr_per_hour": round(member_yr_h, 1),
+              "single_sim_yr_per_hour": round(single_yr_h, 1), "throughput_ratio": round(member_yr_h / single_yr_h, 2),
+              "member0_state_rel_diff": float(np.linalg.norm(ye[:, 0] - y1) / np.linalg.norm(y1))})
 
 
 # --------------------------------------------------------------------- ours
@@ -423,6 +461,8 @@ def main():
         run_reference(args)
     elif args.mode == "matvec":
         run_matvec_mode(args)
+    elif args.mode == "ensemble":
+        run_ensemble_mode(args)
     else:
         run_ours(args)
 

@@ -40,6 +40,7 @@ EXPORTS = [
     "hbi_cycle_free", "hbi_cycle_set_proposer", "hbi_cycle_proposer_size",
     "hbi_mlp_create", "hbi_mlp_free", "hbi_mlp_set_params", "hbi_mlp_get_params", "hbi_mlp_loss_grad",
     "hbi_mlp_train", "hbi_mlp_predict", "hbi_plan_emulate", "hbi_umma_probe",
+    "hbi_ens_create", "hbi_ens_free", "hbi_ens_set_state", "hbi_ens_get_state", "hbi_ens_run",
 ]
 
 
@@ -584,3 +585,66 @@ def umma_probe(a_bf16_bits, b_bf16_bits, variant=0):
     _check(lib().hbi_umma_probe(a.ctypes.data_as(C.POINTER(C.c_uint16)), b.ctypes.data_as(C.POINTER(C.c_uint16)),
                                 d.ctypes.data_as(_fp), int(variant)), "hbi_umma_probe")
     return d
+
+
+class EnsStatus(C.Structure):
+    _fields_ = [("attempts", C.c_longlong), ("steps", C.c_longlong), ("rejected", C.c_longlong),
+                ("done", C.c_int), ("failed", C.c_int), ("wall_s", C.c_double)]
+
+
+class Ensemble:
+    """64 rate-and-state systems with their own b and dc sharing one pair of
+    FP32 H-matrices (hbi_ens_*): one multi-vector product per stage, FP64
+    per-member state and rkqs controllers.  b, dc: (n, 64) arrays in cluster
+    order; other parameters as RK."""
+
+    MEMBERS = 64
+
+    def __init__(self, lh_s, lh_n, b, dc, evlaw=0, backslip=1, limitsigma=1, vref=float(np.float32(1e-6)),
+                 minsig=1.0, maxsig=300.0, scale=1.0, **params):
+        n = lh_s.n
+        self.keep = {}
+        p = RsfParams()
+        p.ncell, p.evlaw, p.backslip, p.limitsigma = n, evlaw, backslip, limitsigma
+        p.vref, p.minsig, p.maxsig, p.scale_s, p.scale_n = vref, minsig, maxsig, scale, scale
+        for k in ("a", "f0", "taudot", "sigdot", "vpl"):
+            a = np.ascontiguousarray(np.broadcast_to(params.get(k, 0.0), (n,)), dtype=np.float64)
+            self.keep[k] = a
+            setattr(p, k, _p(a))
+        zero = np.zeros(n)
+        self.keep["z"] = zero
+        p.b, p.dc = _p(zero), _p(zero)
+        b = np.ascontiguousarray(np.broadcast_to(b, (n, self.MEMBERS)), dtype=np.float64)
+        dc = np.ascontiguousarray(np.broadcast_to(dc, (n, self.MEMBERS)), dtype=np.float64)
+        self.h = C.c_void_p()
+        _check(lib().hbi_ens_create(C.byref(self.h), C.byref(p), lh_s.h, lh_n.h if lh_n is not None else None,
+                                    self.MEMBERS, _p(b), _p(dc)), "hbi_ens_create")
+        self.n, self.lh = n, (lh_s, lh_n)
+        _register(self, 1)
+
+    def set_state(self, y, vel):
+        """y: (3n, 64) [psi, tau, sigma per element], vel: (n, 64)."""
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        vel = np.ascontiguousarray(vel, dtype=np.float64)
+        _check(lib().hbi_ens_set_state(self.h, _p(y), _p(vel)), "hbi_ens_set_state")
+
+    def get_state(self):
+        y = np.zeros((3 * self.n, self.MEMBERS))
+        slip = np.zeros((self.n, self.MEMBERS))
+        x = np.zeros(self.MEMBERS)
+        _check(lib().hbi_ens_get_state(self.h, _p(y), _p(slip), _p(x)), "hbi_ens_get_state")
+        return y, slip, x
+
+    def run(self, t_limit, eps_r=1e-6, dtinit=1.0, dtmax=1e10):
+        st = EnsStatus()
+        _check(lib().hbi_ens_run(self.h, C.c_double(eps_r), C.c_double(dtinit), C.c_double(dtmax),
+                                 C.c_double(t_limit), C.byref(st)), "hbi_ens_run")
+        return {f: getattr(st, f) for f, _ in EnsStatus._fields_}
+
+    def close(self):
+        if getattr(self, "h", None) and _lib is not None and not _closed:
+            _lib.hbi_ens_free(self.h)
+        self.h = None
+
+    def __del__(self):
+        self.close()

@@ -99,3 +99,22 @@ def ensemble_params(M=64, seed=0):
     """c4: per-member b in [0.012, 0.018] and Dc in [5, 30] mm."""
     rng = np.random.default_rng(seed)
     return rng.uniform(0.012, 0.018, M), rng.uniform(0.005, 0.030, M)
+
+
+def ensemble_state(w, lodc, b_in, dc_m):
+    """c4 on a c2 workload: per-member b (b_in inside the velocity-weakening
+    patch, the workload's b outside) and dc, and each member's steady initial
+    state; arrays (n, M) / (3n, M) in cluster order, member index fastest."""
+    idx = lodc - 1
+    p = {k: v[idx] for k, v in w.params.items()}
+    M = len(b_in)
+    inside = p["b"] > 0.01  # the patch carries b_in, the frame 0.006
+    b = np.where(inside[:, None], np.asarray(b_in)[None, :], p["b"][:, None])
+    dc = np.broadcast_to(np.asarray(dc_m)[None, :], (w.nd, M)).copy()
+    a, f0, sig, vel = p["a"][:, None], p["f0"][:, None], p["sigma"][:, None], p["vel"][:, None]
+    psi_ss = f0 - b * np.log(vel / VREF)
+    tau = a * sig * np.arcsinh(vel / (2 * VREF) * np.exp(psi_ss / a))
+    psi = a * np.log(2 * VREF / vel * np.sinh(tau / sig / a))
+    y = np.empty((3 * w.nd, M))
+    y[0::3], y[1::3], y[2::3] = psi, tau, np.broadcast_to(sig, (w.nd, M))
+    return y, np.broadcast_to(vel, (w.nd, M)).copy(), b, dc, p

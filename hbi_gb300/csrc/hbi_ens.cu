@@ -123,6 +123,23 @@ __device__ bool block_wait(uint64_t* b, uint32_t par, int* err, int* sh_ok) {
   return ok != 0;
 }
 
+// after a failed wait: let the block's copies still in flight land (bounded)
+__device__ void drain_e(uint64_t* bar, int c_seq, int p_seq, int xj) {
+  if (threadIdx.x == 0) {
+    for (int q = c_seq; q < p_seq; q++) {
+      const long long t0 = clock64();
+      while (!bar_try(&bar[q & 1], (uint32_t)((q >> 1) & 1)))
+        if (clock64() - t0 > kWait) break;
+    }
+    if (xj >= 0) {
+      const long long t0 = clock64();
+      while (!bar_try(&bar[2 + (xj & 1)], (uint32_t)((xj >> 1) & 1)))
+        if (clock64() - t0 > kWait) break;
+    }
+  }
+  __syncthreads();
+}
+
 __device__ __forceinline__ int ccols(int ntp) { return min((kChunk / (ntp * 4)) / 32 * 32, 256); }
 __device__ __forceinline__ int arrive_acq_rel(int* p) {
   int old;
@@ -186,11 +203,17 @@ __global__ void __launch_bounds__(256, 2) p1e_kernel(EnsMat A, EnsMat B, int nma
   while (c_it < ntot) {
     const EnsMat& M = c_it < n0 ? A : B;
     if (c_c0 == 0) {
-      if (!block_wait(&bar[2 + (j & 1)], (uint32_t)((j >> 1) & 1), M.m.err, &sh_ok)) return;
+      if (!block_wait(&bar[2 + (j & 1)], (uint32_t)((j >> 1) & 1), M.m.err, &sh_ok)) {
+        drain_e(bar, c_seq, p_seq, -1);
+        return;
+      }
       issue_x(c_it + G, j + 1);
     }
     const int s = c_seq & 1;
-    if (!block_wait(&bar[s], (uint32_t)((c_seq >> 1) & 1), M.m.err, &sh_ok)) return;
+    if (!block_wait(&bar[s], (uint32_t)((c_seq >> 1) & 1), M.m.err, &sh_ok)) {
+      drain_e(bar, c_seq, p_seq, c_it + G < ntot ? j + 1 : -1);
+      return;
+    }
     const int nc = min(ccols(Dc.ntp), Dc.ncols - c_c0);
     const float* V = (const float*)cs[s];
     const float* xt = xs[j & 1];
@@ -319,7 +342,10 @@ __global__ void __launch_bounds__(256, 2) p2e_kernel(EnsMat A, EnsMat B, int nma
   while (c_it < ntot) {
     const EnsMat& M = c_it < n0 ? A : B;
     const int s = c_seq & 1;
-    if (!block_wait(&bar[s], (uint32_t)((c_seq >> 1) & 1), M.m.err, &sh_ok)) return;
+    if (!block_wait(&bar[s], (uint32_t)((c_seq >> 1) & 1), M.m.err, &sh_ok)) {
+      drain_e(bar, c_seq, p_seq, -1);
+      return;
+    }
     const int nc = min(cc2(Dc.ntp), Dc.ncols - c_c0);
     // warps: RB row blocks of 16 rows x CSUB column subsets
     const int nrb = (Dc.ntp + 15) / 16;
@@ -805,7 +831,7 @@ extern "C" int hbi_ens_run(hbi_ens* e, double eps_r, double dtinit, double dtmax
     attempts += batch;
     if (cudaStreamSynchronize(e->st) != cudaSuccess) return efail(HBI_ERR_CUDA, "hbi_ens_run: execution");
     if (*(volatile int*)e->hnd >= EM) break;
-    if (attempts >= (1LL << 21)) break;  // members still running are reported as not done
+    if (attempts >= (1LL << 17)) break;  // members still running are reported as not done
   }
   const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   std::vector<int> fl(EM), dn(EM);

@@ -40,7 +40,8 @@ __device__ __forceinline__ bool mbar_try_wait_u(uint64_t* bar, uint32_t parity) 
 constexpr int kProbeOperandBytes = 65536;  // each operand region, zeroed
 
 // variant 0: LBO = K-direction core-matrix stride, SBO = M/N-direction stride;
-// variant 1: the two swapped (same data layout)
+// variant 1: the two swapped (same data layout); variant 2: as 0 with M = 64
+// (A's first 64 rows), D read back from all 128 lanes
 __global__ void __launch_bounds__(128) umma_probe_kernel(const uint16_t* __restrict__ A,
                                                          const uint16_t* __restrict__ B, float* __restrict__ D,
                                                          int variant, int* status) {
@@ -68,14 +69,14 @@ __global__ void __launch_bounds__(128) umma_probe_kernel(const uint16_t* __restr
   const uint32_t tbase = *tslot;
   if (tid == 0) {
     uint64_t da, db;
-    if (variant == 0) {
+    if (variant != 1) {
       da = umma::smem_desc(sA, lboA, sboA);
       db = umma::smem_desc(sB, lboB, sboB);
     } else {
       da = umma::smem_desc(sA, sboA, lboA);
       db = umma::smem_desc(sB, sboB, lboB);
     }
-    umma::mma_bf16(tbase, da, db, umma::idesc_bf16_f32(128, 64), 0);
+    umma::mma_bf16(tbase, da, db, umma::idesc_bf16_f32(variant == 2 ? 64 : 128, 64), 0);
     umma::commit(bar);
   }
   // bounded wait for the MMA (about a second of SM clock)
@@ -109,7 +110,7 @@ __global__ void __launch_bounds__(128) umma_probe_kernel(const uint16_t* __restr
 
 extern "C" int hbi_umma_probe(const uint16_t* a, const uint16_t* b, float* d, int variant) {
   using namespace hbi;
-  if (!a || !b || !d || variant < 0 || variant > 1) return set_error(HBI_ERR_ARG, "hbi_umma_probe: bad arguments");
+  if (!a || !b || !d || variant < 0 || variant > 2) return set_error(HBI_ERR_ARG, "hbi_umma_probe: bad arguments");
   uint16_t *da = nullptr, *db = nullptr;
   float* dd = nullptr;
   int* ds = nullptr;

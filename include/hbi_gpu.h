@@ -323,7 +323,8 @@ int hbi_ens_run(hbi_ens* e, double eps_r, double dtinit, double dtmax, double t_
  * tcgen05 MMA, D[128][64] = A[128][16] * B[64][16]^T with BF16 operands (raw
  * bit patterns) from canonical K-major shared-memory layouts and FP32
  * accumulation in tensor memory.  variant 0 uses the descriptor convention of
- * the ensemble kernels; variant 1 swaps its two stride fields. */
+ * the ensemble kernels; variant 1 swaps its two stride fields; variant 2 is an
+ * M = 64 MMA (rows 0-63 of a), d holding all 128 tensor-memory lanes. */
 int hbi_umma_probe(const uint16_t* a, const uint16_t* b, float* d, int variant);
 
 #ifdef __cplusplus

@@ -1,0 +1,56 @@
+"""The ensemble (hbi_ens_*): 64 systems with their own b and dc on one pair
+of FP32 H-matrices, against each member run alone through the single-system
+time loop on the same operators.
+
+Tolerance: the multi-vector product sums in another order than the
+single-vector one (FP32 partial sums, ~1e-7 per product); over one
+interseismic year the members' states agree within 1e-6 relative and their
+slip within 1e-4."""
+import numpy as np
+import pytest
+
+import hbi_gb300 as H
+from hbi_gb300 import configs
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def setup():
+    w = configs.c2_3dph(32, 16)
+    n = w.nd
+    ctl_s, ctl_n = H.Ctl(n), H.Ctl(n)
+    lf_s = H.LeafMtxp(ctl_s, w.geometry("s"), w.eps_h)
+    lf_n = H.LeafMtxp(ctl_n, w.geometry("n"), w.eps_h)
+    lh_s, lh_n = H.LHp(lf_s, ctl_s, "f32"), H.LHp(lf_n, ctl_n, "f32")
+    ndc, lodc = H.HACApK_gen_lattice_vector(ctl_s)
+    b_in, dc_m = configs.ensemble_params(64, seed=3)
+    y, vel, b, dc, p = configs.ensemble_state(w, lodc, b_in, dc_m)
+    return dict(w=w, n=n, lh=(lh_s, lh_n), y=y, vel=vel, b=b, dc=dc, p=p, lodc=lodc,
+                keep=(ctl_s, ctl_n, lf_s, lf_n))
+
+
+def test_ensemble_members_match_single_runs(setup):
+    S = setup
+    w, p = S["w"], S["p"]
+    T = 1.0 * H.YEAR
+    ens = H.Ensemble(*S["lh"], S["b"], S["dc"], evlaw=w.evlaw, scale=w.scale, a=p["a"], f0=p["f0"], vpl=p["vpl"])
+    ens.set_state(S["y"], S["vel"])
+    st = ens.run(T, eps_r=1e-6)
+    assert st["done"] == 64 and st["failed"] == 0
+    ye, se, xe = ens.get_state()
+    assert np.all(xe == T)
+    ds = w.ds_area[S["lodc"] - 1]
+    for m in (0, 17, 63):
+        rk = H.RK(*S["lh"], evlaw=w.evlaw, scale=w.scale, a=p["a"], b=S["b"][:, m], dc=S["dc"][:, m], f0=p["f0"],
+                  vpl=p["vpl"])
+        rk.set_state(S["y"][:, m])
+        cyc = H.Cycle(rk, S["vel"][:, m], ds, eps_r=1e-6)
+        cs = cyc.run(t_limit=T)
+        assert cs["x"] == T
+        y1 = rk.get_state()
+        _, s1 = cyc.fields()
+        assert np.linalg.norm(ye[:, m] - y1) <= 1e-6 * np.linalg.norm(y1), m
+        assert np.linalg.norm(se[:, m] - s1) <= 1e-4 * np.linalg.norm(s1), m
+        cyc.close()
+        rk.close()

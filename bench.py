@@ -232,16 +232,23 @@ def run_ensemble_mode(args):
     b_in, dc_m = configs.ensemble_params(64, seed=0)
     y, vel, b, dc, p = configs.ensemble_state(w, lodc, b_in, dc_m)
     T = args.window_yr * H.YEAR
-    ens = H.Ensemble(lh_s, lh_n, b, dc, evlaw=w.evlaw, scale=w.scale, a=p["a"], f0=p["f0"], vpl=p["vpl"])
-    ens.set_state(y, vel)
-    st = ens.run(T, eps_r=1e-6)
+    res = {}
+    for product in ("cuda-cores", "tcgen05"):
+        ens = H.Ensemble(lh_s, lh_n, b, dc, evlaw=w.evlaw, scale=w.scale, a=p["a"], f0=p["f0"], vpl=p["vpl"])
+        if product == "tcgen05":
+            ens.use_tensor_cores(lf_s, lf_n)
+        ens.set_state(y, vel)
+        st = ens.run(T, eps_r=1e-6)
+        ye, se, xe = ens.get_state()
+        res[product] = (st, ye)
+        ens.close()
+    st, ye = res["tcgen05"]
     ds = w.ds_area[lodc - 1]
     m = 0
     rk = H.RK(lh_s, lh_n, evlaw=w.evlaw, scale=w.scale, a=p["a"], b=b[:, m], dc=dc[:, m], f0=p["f0"], vpl=p["vpl"])
     rk.set_state(y[:, m])
     cyc = H.Cycle(rk, vel[:, m], ds, eps_r=1e-6)
     cs = cyc.run(t_limit=T)
-    ye, se, xe = ens.get_state()
     y1 = rk.get_state()
     member_yr_h = 64 * args.window_yr / st["wall_s"] * 3600
     single_yr_h = args.window_yr / cs["wall_s"] * 3600
@@ -251,7 +258,10 @@ def run_ensemble_mode(args):
               "ms_per_attempt": round(st["wall_s"] / max(1, st["attempts"]) * 1e3, 3),
               "member_sim_yr_per_hour": round(member_yr_h, 1),
               "single_sim_yr_per_hour": round(single_yr_h, 1), "throughput_ratio": round(member_yr_h / single_yr_h, 2),
-              "member0_state_rel_diff": float(np.linalg.norm(ye[:, 0] - y1) / np.linalg.norm(y1))})
+              "member0_state_rel_diff": float(np.linalg.norm(ye[:, 0] - y1) / np.linalg.norm(y1)),
+              "product": "tcgen05 (BF16 hi+lo, FP32 accumulation in tensor memory)",
+              "cuda_core_product_ms_per_attempt": round(res["cuda-cores"][0]["wall_s"] /
+                                                        max(1, res["cuda-cores"][0]["attempts"]) * 1e3, 3)})
 
 
 # --------------------------------------------------------------------- ours

@@ -41,6 +41,7 @@ EXPORTS = [
     "hbi_mlp_create", "hbi_mlp_free", "hbi_mlp_set_params", "hbi_mlp_get_params", "hbi_mlp_loss_grad",
     "hbi_mlp_train", "hbi_mlp_predict", "hbi_plan_emulate", "hbi_umma_probe",
     "hbi_ens_create", "hbi_ens_free", "hbi_ens_set_state", "hbi_ens_get_state", "hbi_ens_run",
+    "hbi_tc_plan_emulate", "hbi_ens_use_tensor_cores",
 ]
 
 
@@ -635,6 +636,13 @@ class Ensemble:
         _check(lib().hbi_ens_get_state(self.h, _p(y), _p(slip), _p(x)), "hbi_ens_get_state")
         return y, slip, x
 
+    def use_tensor_cores(self, lf_s, lf_n=None):
+        """Switch the multi-vector product to the tcgen05 kernels (FP64
+        factors of the LeafMtxp handles, stored as BF16 hi + lo)."""
+        _check(lib().hbi_ens_use_tensor_cores(self.h, lf_s.h, lf_n.h if lf_n is not None else None),
+               "hbi_ens_use_tensor_cores")
+        self.lf = (lf_s, lf_n)
+
     def run(self, t_limit, eps_r=1e-6, dtinit=1.0, dtmax=1e10):
         st = EnsStatus()
         _check(lib().hbi_ens_run(self.h, C.c_double(eps_r), C.c_double(dtinit), C.c_double(dtmax),
@@ -648,3 +656,15 @@ class Ensemble:
 
     def __del__(self):
         self.close()
+
+
+def tc_plan_emulate(n, leaves, body, x):
+    """Host walk of the ensemble's tensor-core plan (hbi_tc_plan_emulate)."""
+    lv = np.ascontiguousarray(leaves, dtype=np.int32)
+    body = np.ascontiguousarray(body, dtype=np.float64)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.zeros(n)
+    st = np.zeros(4, dtype=np.int64)
+    _check(lib().hbi_tc_plan_emulate(n, len(lv), lv.ctypes.data_as(_ip), _p(body), _p(x), _p(y),
+                                     st.ctypes.data_as(_i64p)), "hbi_tc_plan_emulate")
+    return y, dict(zip(("items1", "items2", "store1", "store2"), (int(v) for v in st)))

@@ -851,6 +851,15 @@ int rk_view(hbi_rk* r, RkView* v) {
   return HBI_OK;
 }
 int set_error(int code, const char* msg) { return fail(code, "%s", msg); }
+// the filled leaves of a generate call, for the ensemble's tensor-core stores
+int leaf_view(const hbi_leafmtxp* lf, const double** d_body, std::vector<int64_t>* off,
+              std::vector<Leaf>* leaves) {
+  if (!lf || !d_body || !off || !leaves) return fail(HBI_ERR_ARG, "null");
+  *d_body = lf->d_body;
+  off->assign(lf->off.begin(), lf->off.begin() + lf->leaves.size());
+  *leaves = lf->leaves;
+  return HBI_OK;
+}
 // for the ensemble (hbi_ens.cu)
 int lhp_view(hbi_lhp* h, LhpView* v) {
   if (!h || !v) return fail(HBI_ERR_ARG, "null");
@@ -1098,6 +1107,123 @@ extern "C" int hbi_plan_emulate(int n, int nleaf, const int* lv6, const double* 
   if (stats) {
     stats[0] = (int64_t)P.p1.size(); stats[1] = (int64_t)P.p2.size(); stats[2] = P.vstore; stats[3] = P.ustore;
     stats[4] = P.zlen; stats[5] = P.plen1; stats[6] = P.plen2; stats[7] = nseg_conv;
+  }
+  return HBI_OK;
+}
+
+// ------------------------------------------- tensor-core plan self check (host)
+namespace {
+// round to bfloat16 (nearest even) through float, as __float2bfloat16_rn does
+float bf16_round(double x) {
+  float f = (float)x;
+  uint32_t u;
+  memcpy(&u, &f, 4);
+  if ((u & 0x7f800000u) != 0x7f800000u) u = (u + 0x7fffu + ((u >> 16) & 1u)) & 0xffff0000u;
+  else u &= 0xffff0000u;
+  memcpy(&f, &u, 4);
+  return f;
+}
+int64_t tc_offset(int np, int n, int k) {
+  const int c = k / 16, kk = k % 16;
+  return (int64_t)c * np * 32 + (int64_t)(kk / 8) * np * 8 + (int64_t)(n / 8) * 64 + (n % 8) * 8 + (kk % 8);
+}
+}  // namespace
+
+// y = H x through the tensor-core plan of the ensemble product (one member),
+// with the factors rounded to BF16 hi + lo as the device stores them; checks
+// every bound the kernels rely on.  stats (4): items of phase 1 and 2, store
+// elements of phase 1 and 2.
+extern "C" int hbi_tc_plan_emulate(int n, int nleaf, const int* lv6, const double* body, const double* x, double* y,
+                                   int64_t* stats) {
+  if (n < 1 || nleaf < 1 || !lv6 || !body || !x || !y) return fail(HBI_ERR_ARG, "hbi_tc_plan_emulate: arguments");
+  std::vector<Leaf> L(nleaf);
+  std::vector<int64_t> boff(nleaf);
+  int64_t off = 0;
+  for (int i = 0; i < nleaf; i++) {
+    const int* q = lv6 + 6 * i;
+    L[i] = Leaf{q[0], q[1], q[2], q[3], q[4], q[5]};
+    boff[i] = off;
+    off += L[i].ltmtx == 1 ? (int64_t)L[i].kt * (L[i].ndl + L[i].ndt) : (int64_t)L[i].ndl * L[i].ndt;
+  }
+  TcPlan T;
+  plan_tc(n, L, boff, T);
+  std::vector<double> S1(T.store1, 0.0), S2(T.store2, 0.0);
+  for (int ph = 1; ph <= 2; ph++) {
+    const std::vector<TcCopy>& cp = ph == 1 ? T.copy1 : T.copy2;
+    std::vector<double>& S = ph == 1 ? S1 : S2;
+    for (const TcCopy& c : cp)
+      for (int i = 0; i < c.len; i++) {
+        const int nn = c.n0 + i * c.dn, kk = c.k0 + i * c.dk;
+        if (nn >= c.np) return fail(HBI_ERR_STATE, "tc copy: n beyond the item");
+        const int64_t o = c.item + tc_offset(c.np, nn, kk);
+        const int64_t src = c.src + (int64_t)i * c.stride;
+        if (src < 0 || src >= off || o < 0 || o + (int64_t)c.np * 16 >= (int64_t)S.size() + 1)
+          return fail(HBI_ERR_STATE, "tc copy out of bounds");
+        const double v = body[src];
+        const double hi = bf16_round(v);
+        S[o] = hi;
+        S[o + (int64_t)c.np * 16] = bf16_round(v - hi);
+      }
+  }
+  std::vector<double> z(std::max<int64_t>(T.zlen, 1), 0.0), part(std::max<int64_t>(T.plen1, 1), 0.0);
+  for (const TcItem& it : T.p1) {
+    if (it.np % 8 || it.np > 256 || it.kp % 16 || it.kp > 256 || it.nv > it.np || it.kv > it.kp || it.m0 < 0 ||
+        it.m0 + it.kv > n || it.out0 + it.nv > T.zlen || it.soff + (int64_t)it.kp * it.np * 2 > T.store1 ||
+        (it.ntile > 1 && it.poff + (int64_t)it.ntile * it.nv > T.plen1))
+      return fail(HBI_ERR_STATE, "tc phase-1 item out of bounds");
+    for (int c = 0; c < it.nv; c++) {
+      double t = 0.0;
+      for (int k = 0; k < it.kv; k++) {
+        const int64_t o = it.soff + tc_offset(it.np, c, k);
+        t += (S1[o] + S1[o + (int64_t)it.np * 16]) * x[it.m0 + k];
+      }
+      if (it.ntile == 1) z[it.out0 + c] = t;
+      else part[it.poff + (int64_t)it.tile * it.nv + c] = t;
+    }
+  }
+  for (const TcItem& it : T.p1)
+    if (it.ntile > 1 && it.tile == 0)
+      for (int c = 0; c < it.nv; c++) {
+        double t = 0.0;
+        for (int q = 0; q < it.ntile; q++) t += part[it.poff + (int64_t)q * it.nv + c];
+        z[it.out0 + c] = t;
+      }
+  GroupPlan G;
+  plan_groups(n, L, G);
+  int64_t plen2 = 0;
+  for (size_t g = 0; g < G.grow0.size(); g++) plen2 += G.gndl[g];
+  std::vector<double> gp(std::max<int64_t>(plen2, 1), 0.0);
+  for (const TcItem& it : T.p2) {
+    if (it.np % 8 || it.np > 256 || it.kp % 16 || it.nv > it.np || it.kv > it.kp || it.m0 % 4 ||
+        it.m0 + it.kp > (int64_t)T.midx.size() || it.out0 + it.nv > plen2 ||
+        it.soff + (int64_t)it.kp * it.np * 2 > T.store2)
+      return fail(HBI_ERR_STATE, "tc phase-2 item out of bounds");
+    for (int r = 0; r < it.nv; r++) {
+      double t = 0.0;
+      for (int k = 0; k < it.kv; k++) {
+        const int mi = T.midx[it.m0 + k];
+        const double mu = mi >= 0 ? z[mi] : x[-mi - 1];
+        const int64_t o = it.soff + tc_offset(it.np, r, k);
+        t += (S2[o] + S2[o + (int64_t)it.np * 16]) * mu;
+      }
+      gp[it.out0 + r] = t;
+    }
+  }
+  for (int r = 0; r < n; r++) {
+    double t = 0.0;
+    const int f = G.row_fc[r];
+    int64_t base = 0;
+    (void)base;
+    for (int e = G.fc_ptr[f]; e < G.fc_ptr[f + 1]; e++) {
+      const int g = G.fc_group[e];
+      int64_t go = 0;
+      for (int q = 0; q < g; q++) go += G.gndl[q];
+      t += gp[go + r - G.grow0[g]];
+    }
+    y[r] = t;
+  }
+  if (stats) {
+    stats[0] = (int64_t)T.p1.size(); stats[1] = (int64_t)T.p2.size(); stats[2] = T.store1; stats[3] = T.store2;
   }
   return HBI_OK;
 }

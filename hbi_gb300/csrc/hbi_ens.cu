@@ -24,6 +24,7 @@
 // member's 5th-order solution is so large that y - 1 == y, the member's
 // errmax is raised to at least 10 (a rejection) instead of replaying the
 // reference's order-dependent rule.  No events, monitors or files.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -40,6 +41,25 @@
 namespace hbi {
 int set_error(int code, const char* msg);
 int lhp_view(hbi_lhp* h, LhpView* v);
+int leaf_view(const hbi_leafmtxp* lf, const double** d_body, std::vector<int64_t>* off, std::vector<Leaf>* leaves);
+struct TcMat {
+  const TcItem* p1;
+  int n1;
+  const TcItem* p2;
+  int n2;
+  const __nv_bfloat16* s1;
+  const __nv_bfloat16* s2;
+  const int32_t* midx;
+  float* z;
+  float* part;
+  int* cnt;
+  float* gpart;
+  int* err;
+};
+size_t tc_smem_bytes();
+void tc_prepare();
+void launch_tc(int phase, const TcMat& a, const TcMat& b, int nmat, const float* x, int sm, cudaStream_t st);
+void launch_tcconv(const double* body, const TcCopy* map, int64_t nmap, __nv_bfloat16* dst, cudaStream_t st);
 
 namespace {
 
@@ -603,6 +623,8 @@ using namespace hbi;
 struct hbi_ens_s {
   EnsDev E{};
   EnsMat M[2]{};
+  TcMat T[2]{};
+  bool tc = false;
   int nmat = 1, n = 0, sm = 152;
   std::vector<void*> allocs;
   int* hnd = nullptr;  // host-mapped done count
@@ -633,8 +655,13 @@ void enqueue_e(hbi_ens* e) {
   for (int s = 0; s < 6; s++) {
     const float* xin = s == 0 ? E.x0 : E.xb[s & 1];
     float* xout = E.xb[(s + 1) & 1];
-    p1e_kernel<<<g1, 256, smem1(), st>>>(e->M[0], e->M[e->nmat - 1], e->nmat, xin);
-    p2e_kernel<<<g1, 256, smem2(), st>>>(e->M[0], e->M[e->nmat - 1], e->nmat, xin);
+    if (e->tc) {
+      launch_tc(1, e->T[0], e->T[e->nmat - 1], e->nmat, xin, e->sm, st);
+      launch_tc(2, e->T[0], e->T[e->nmat - 1], e->nmat, xin, e->sm, st);
+    } else {
+      p1e_kernel<<<g1, 256, smem1(), st>>>(e->M[0], e->M[e->nmat - 1], e->nmat, xin);
+      p2e_kernel<<<g1, 256, smem2(), st>>>(e->M[0], e->M[e->nmat - 1], e->nmat, xin);
+    }
     p3e_kernel<<<blocks, 256, 0, st>>>(e->M[0], e->M[e->nmat - 1], E, s, xout);
   }
   control_e_kernel<<<1, EM, 0, st>>>(E);
@@ -642,6 +669,10 @@ void enqueue_e(hbi_ens* e) {
 }
 
 }  // namespace
+
+namespace {
+int recapture(hbi_ens* e);
+}
 
 extern "C" int hbi_ens_free(hbi_ens* e) {
   if (!e) return HBI_OK;
@@ -804,15 +835,8 @@ extern "C" int hbi_ens_run(hbi_ens* e, double eps_r, double dtinit, double dtmax
     // re-capture with the new constants
     e->E.eps = eps_r;
     e->E.dtmax = dtmax;
-    if (e->g) cudaGraphExecDestroy(e->g);
-    e->g = nullptr;
-    cudaGraph_t g;
-    if (cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
-      return efail(HBI_ERR_CUDA, "hbi_ens_run: capture");
-    enqueue_e(e);
-    if (cudaStreamEndCapture(e->st, &g) != cudaSuccess || cudaGraphInstantiate(&e->g, g, 0) != cudaSuccess)
-      return efail(HBI_ERR_CUDA, "hbi_ens_run: graph");
-    cudaGraphDestroy(g);
+    int rc = recapture(e);
+    if (rc) return rc;
   }
   if (cudaMemcpy(e->E.h, h.data(), sizeof(double) * EM, cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(e->E.x, x.data(), sizeof(double) * EM, cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -851,4 +875,68 @@ extern "C" int hbi_ens_run(hbi_ens* e, double eps_r, double dtinit, double dtmax
     out->wall_s = wall;
   }
   return HBI_OK;
+}
+
+namespace {
+int recapture(hbi_ens* e) {
+  if (e->g) cudaGraphExecDestroy(e->g);
+  e->g = nullptr;
+  cudaGraph_t g;
+  if (cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    return efail(HBI_ERR_CUDA, "capture");
+  enqueue_e(e);
+  if (cudaStreamEndCapture(e->st, &g) != cudaSuccess || cudaGraphInstantiate(&e->g, g, 0) != cudaSuccess)
+    return efail(HBI_ERR_CUDA, "graph");
+  cudaGraphDestroy(g);
+  return HBI_OK;
+}
+}  // namespace
+
+extern "C" int hbi_ens_use_tensor_cores(hbi_ens* e, const hbi_leafmtxp* lf_s, const hbi_leafmtxp* lf_n) {
+  if (!e || !lf_s || (e->nmat == 2 && !lf_n)) return efail(HBI_ERR_ARG, "hbi_ens_use_tensor_cores: null");
+  for (int k = 0; k < e->nmat; k++) {
+    const double* body = nullptr;
+    std::vector<int64_t> off;
+    std::vector<Leaf> leaves;
+    int rc = leaf_view(k ? lf_n : lf_s, &body, &off, &leaves);
+    if (rc) return rc;
+    TcPlan P;
+    plan_tc(e->n, leaves, off, P);
+    TcMat& T = e->T[k];
+    auto upload = [&](const void* h, size_t bytes) -> void* {
+      void* d = nullptr;
+      if (cudaMalloc(&d, std::max<size_t>(bytes, 16)) != cudaSuccess) return nullptr;
+      e->allocs.push_back(d);
+      if (bytes && cudaMemcpy(d, h, bytes, cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
+      return d;
+    };
+    T.p1 = (const TcItem*)upload(P.p1.data(), P.p1.size() * sizeof(TcItem));
+    T.n1 = (int)P.p1.size();
+    T.p2 = (const TcItem*)upload(P.p2.data(), P.p2.size() * sizeof(TcItem));
+    T.n2 = (int)P.p2.size();
+    T.midx = (const int32_t*)upload(P.midx.data(), P.midx.size() * sizeof(int32_t));
+    __nv_bfloat16* s1 = ealloc<__nv_bfloat16>(e, (size_t)P.store1);
+    __nv_bfloat16* s2 = ealloc<__nv_bfloat16>(e, (size_t)P.store2);
+    T.s1 = s1;
+    T.s2 = s2;
+    T.z = ealloc<float>(e, (size_t)P.zlen * EM);
+    T.part = ealloc<float>(e, (size_t)P.plen1 * EM);
+    T.cnt = ealloc<int>(e, (size_t)P.ncg);
+    T.gpart = e->M[k].gpart;
+    T.err = e->M[k].m.err;
+    if (!T.p1 || !T.p2 || !T.midx || !s1 || !s2 || !T.z || !T.part || !T.cnt)
+      return efail(HBI_ERR_NOMEM, "hbi_ens_use_tensor_cores: allocation");
+    for (int ph = 1; ph <= 2; ph++) {
+      const std::vector<TcCopy>& map = ph == 1 ? P.copy1 : P.copy2;
+      TcCopy* dm = (TcCopy*)upload(map.data(), map.size() * sizeof(TcCopy));
+      if (!dm) return efail(HBI_ERR_NOMEM, "hbi_ens_use_tensor_cores: conversion map");
+      launch_tcconv(body, dm, (int64_t)map.size(), ph == 1 ? s1 : s2, e->st);
+      if (cudaStreamSynchronize(e->st) != cudaSuccess) return efail(HBI_ERR_CUDA, "hbi_ens_use_tensor_cores: convert");
+      cudaFree(dm);
+      e->allocs.pop_back();
+    }
+  }
+  tc_prepare();
+  e->tc = true;
+  return recapture(e);
 }

@@ -496,4 +496,122 @@ void plan_stream(int n, const std::vector<Leaf>& leaves, const std::vector<int64
   });
 }
 
+void plan_tc(int n, const std::vector<Leaf>& leaves, const std::vector<int64_t>& body_off, TcPlan& tp) {
+  const int nl = (int)leaves.size();
+  const int TR = 256;
+  tp = TcPlan();
+  // ---- phase 1: column groups; K = rows of a tile, N = columns (<= 256 per item)
+  std::vector<std::pair<std::pair<int, int>, int>> ck;
+  for (int i = 0; i < nl; i++)
+    if (leaves[i].ltmtx == 1 && leaves[i].kt > 0) ck.push_back({{leaves[i].nstrtt - 1, -leaves[i].ndt}, i});
+  std::stable_sort(ck.begin(), ck.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+  std::vector<int32_t> leaf_z(nl, -1);
+  int64_t off = 0, z = 0, poff = 0, ncg = 0;
+  for (size_t a = 0; a < ck.size();) {
+    size_t b = a;
+    while (b < ck.size() && ck[b].first == ck[a].first) b++;
+    const int col0 = ck[a].first.first, ndt = -ck[a].first.second;
+    // the group's columns in leaf order: (leaf, k)
+    std::vector<std::pair<int, int>> cols;
+    for (size_t e = a; e < b; e++) {
+      leaf_z[ck[e].second] = (int32_t)(z + cols.size());
+      for (int k = 0; k < leaves[ck[e].second].kt; k++) cols.push_back({ck[e].second, k});
+    }
+    const int ncols = (int)cols.size();
+    const int ntile = (ndt + TR - 1) / TR;
+    for (int c0 = 0; c0 < ncols; c0 += 256) {
+      const int nv = std::min(256, ncols - c0);
+      const int np = (nv + 7) / 8 * 8;
+      const int64_t poff0 = poff;
+      if (ntile > 1) poff += (int64_t)ntile * nv;
+      for (int t = 0; t < ntile; t++) {
+        const int kv = std::min(TR, ndt - t * TR);
+        const int kp = (kv + 15) / 16 * 16;
+        TcItem it{};
+        it.soff = off;
+        it.np = np; it.kp = kp; it.nv = nv; it.kv = kv;
+        it.m0 = col0 + t * TR;
+        it.out0 = (int32_t)(z + c0);
+        it.cg = (int32_t)ncg;
+        it.tile = t; it.ntile = ntile;
+        it.poff = ntile > 1 ? (int32_t)poff0 : -1;
+        tp.p1.push_back(it);
+        for (int c = 0; c < nv; c++) {
+          const int li = cols[c0 + c].first, k = cols[c0 + c].second;
+          const Leaf& L = leaves[li];
+          // V(row, k) at body + row + k*ndt; run along K (the tile's rows)
+          tp.copy1.push_back(TcCopy{off, body_off[li] + (int64_t)k * L.ndt + (int64_t)t * TR, np, c, 0, 0, 1, kv, 1});
+        }
+        off += (int64_t)kp * np * 2;
+      }
+      ncg++;
+    }
+    z += ncols;
+    a = b;
+  }
+  tp.store1 = off;
+  tp.zlen = z;
+  tp.plen1 = poff;
+  tp.ncg = ncg;
+  // ---- phase 2: row groups; N = rows of a tile, K = the group's columns
+  GroupPlan gp;
+  plan_groups(n, leaves, gp);
+  const int ng = (int)gp.grow0.size();
+  off = 0;
+  int64_t p2off = 0;
+  for (int g = 0; g < ng; g++) {
+    const int ndl = gp.gndl[g];
+    while (tp.midx.size() % 4) tp.midx.push_back(0);
+    const int m0 = (int)tp.midx.size();
+    std::vector<std::pair<int, int>> cols;
+    for (int e = gp.gleaf_ptr[g]; e < gp.gleaf_ptr[g + 1]; e++) {
+      const int li = gp.gleaf[e];
+      const Leaf& L = leaves[li];
+      const int nc = L.ltmtx == 1 ? L.kt : L.ndt;
+      for (int k = 0; k < nc; k++) {
+        tp.midx.push_back(L.ltmtx == 1 ? leaf_z[li] + k : -(L.nstrtt - 1 + k) - 1);
+        cols.push_back({li, k});
+      }
+    }
+    const int ncols = (int)cols.size();
+    const int64_t gpoff = p2off;
+    p2off += ndl;
+    if (ncols == 0) continue;
+    const int kp = (ncols + 15) / 16 * 16;
+    const int ntile = (ndl + TR - 1) / TR;
+    for (int t = 0; t < ntile; t++) {
+      const int nv = std::min(TR, ndl - t * TR);
+      const int np = (nv + 7) / 8 * 8;
+      TcItem it{};
+      it.soff = off;
+      it.np = np; it.kp = kp; it.nv = nv; it.kv = ncols;
+      it.m0 = m0;
+      it.out0 = (int32_t)(gpoff + t * TR);
+      it.cg = -1; it.tile = t; it.ntile = ntile; it.poff = -1;
+      tp.p2.push_back(it);
+      for (int c = 0; c < ncols; c++) {
+        const int li = cols[c].first, k = cols[c].second;
+        const Leaf& L = leaves[li];
+        if (L.ltmtx == 1) {
+          const int64_t u0 = body_off[li] + (int64_t)L.ndt * L.kt + (int64_t)k * L.ndl + (int64_t)t * TR;
+          tp.copy2.push_back(TcCopy{off, u0, np, 0, c, 1, 0, nv, 1});  // run along N (rows)
+        } else {
+          // a1(ndt, ndl): (it, il) at it + il*ndt; column it = k, rows il
+          tp.copy2.push_back(TcCopy{off, body_off[li] + k + (int64_t)t * TR * L.ndt, np, 0, c, 1, 0, nv, L.ndt});
+        }
+      }
+      off += (int64_t)kp * np * 2;
+    }
+  }
+  while (tp.midx.size() % 4) tp.midx.push_back(0);
+  tp.midx.resize(tp.midx.size() + 64, 0);
+  tp.store2 = off;
+  std::stable_sort(tp.p1.begin(), tp.p1.end(), [](const TcItem& a, const TcItem& b) {
+    return (int64_t)a.np * a.kp > (int64_t)b.np * b.kp;
+  });
+  std::stable_sort(tp.p2.begin(), tp.p2.end(), [](const TcItem& a, const TcItem& b) {
+    return (int64_t)a.np * a.kp > (int64_t)b.np * b.kp;
+  });
+}
+
 }  // namespace hbi

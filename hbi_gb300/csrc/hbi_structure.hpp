@@ -155,6 +155,39 @@ inline int chunk_cols(int ntp, int esz) {
   const int c = (16384 / (ntp * esz)) / 32 * 32;
   return c < 256 ? c : 256;
 }
+// ---- tensor-core plan of the ensemble product ---------------------------
+// Both contractions as D (64 members x N) = A (64 x K) * B^T with B (N x K)
+// from the factor store: phase 2 N = the rows of a row-group tile (<= 256),
+// K = the group's columns; phase 1 N = the columns of a column group (<= 256
+// per item), K = the rows of a tile (<= 256).  B is stored as BF16 hi + lo
+// halves (x = hi + lo to ~16 bits) in the canonical no-swizzle K-major layout,
+// per 16-K chunk: [hi: 2 K-blocks x N/8 core matrices of 8 x 8][lo: same].
+// N is padded to 8 and K to 16 with zeros.
+struct TcItem {
+  int64_t soff;            // bf16 element offset of the item's first chunk
+  int32_t np, kp;          // N padded to 8, K padded to 16
+  int32_t nv, kv;          // valid N, valid K
+  int32_t m0;              // phase 2: midx of column 0; phase 1: x row of K index 0
+  int32_t out0;            // phase 2: gpart row offset; phase 1: z index of column 0
+  int32_t cg, tile, ntile, poff;  // phase 1 multi-tile reduction (as S1Item)
+  int32_t pad[2];
+};
+struct TcCopy {            // one run of a column (or tile-row) from the FP64 body
+  int64_t item, src;       // bf16 offset of the item, body offset of element 0
+  int32_t np;              // the item's padded N
+  int32_t n0, k0;          // canonical (n, k) of element 0
+  int32_t dn, dk;          // step per element along n and k (one of them 0)
+  int32_t len, stride;     // elements, body stride
+};
+struct TcPlan {
+  std::vector<TcItem> p1, p2;
+  int64_t store1 = 0, store2 = 0;  // bf16 elements (hi and lo halves included)
+  int64_t zlen = 0, plen1 = 0, ncg = 0;
+  std::vector<int32_t> midx;       // as StreamPlan::midx
+  std::vector<TcCopy> copy1, copy2;
+};
+void plan_tc(int n, const std::vector<Leaf>& leaves, const std::vector<int64_t>& body_off, TcPlan& tp);
+
 // body_off: element offset of each leaf in the HACApK FP64 body (low rank:
 // [V ndt x kt][U ndl x kt] column-major; dense a1(ndt, ndl))
 void plan_stream(int n, const std::vector<Leaf>& leaves, const std::vector<int64_t>& body_off, int vec,

@@ -316,8 +316,19 @@ int hbi_ens_free(hbi_ens* e);
 /* y (3*ncell*members), vel (ncell*members: the slip rate before the loop) */
 int hbi_ens_set_state(hbi_ens* e, const double* y, const double* vel);
 int hbi_ens_get_state(hbi_ens* e, double* y, double* slip, double* x);
+/* Run the ensemble's multi-vector product on the tensor cores (tcgen05,
+ * BF16 hi + lo operands, FP32 accumulation in tensor memory) built from the
+ * FP64 factors of the generate calls lh_s / lh_n were made from. */
+int hbi_ens_use_tensor_cores(hbi_ens* e, const hbi_leafmtxp* lf_s, const hbi_leafmtxp* lf_n);
 /* every member from x = 0 to exactly t_limit (s) */
 int hbi_ens_run(hbi_ens* e, double eps_r, double dtinit, double dtmax, double t_limit, hbi_ens_status* st);
+
+/* Host-only self check of the tensor-core plan of the ensemble product (no
+ * reference counterpart): y = H x through that plan with the factors rounded
+ * to BF16 hi + lo as stored, and every bound its kernels rely on.
+ * stats[4]: items of phase 1 and 2, store elements of phase 1 and 2. */
+int hbi_tc_plan_emulate(int n, int nleaf, const int* leaves6, const double* body, const double* x, double* y,
+                        int64_t* stats);
 
 /* Self test of the tensor-core path (no reference counterpart): one
  * tcgen05 MMA, D[128][64] = A[128][16] * B[64][16]^T with BF16 operands (raw

@@ -803,7 +803,7 @@ extern "C" int hbi_rk_create(hbi_rk** out, const hbi_rsf_params* p, hbi_lhp* ls,
   int bad = 0;
   bad |= cp(&R.a, p->a); bad |= cp(&R.b, p->b); bad |= cp(&R.dc, p->dc); bad |= cp(&R.f0, p->f0);
   bad |= cp(&R.taudot, p->taudot); bad |= cp(&R.sigdot, p->sigdot); bad |= cp(&R.vpl, p->vpl);
-  bad |= mk(&R.y, 3 * n); bad |= mk(&R.ys, 3 * n); bad |= mk(&R.vs, n); bad |= mk(&R.x0, n);
+  bad |= mk(&R.y, 3 * n); bad |= mk(&R.ys, 3 * n); bad |= mk(&R.vs, n); bad |= mk(&R.ws, n); bad |= mk(&R.x0, n);
   bad |= mk(&R.xb[0], n); bad |= mk(&R.xb[1], n); bad |= mk(&R.K, 18 * (size_t)n);
   bad |= mk(&R.yout, 3 * n); bad |= mk(&R.yerr, 3 * n); bad |= mk(&R.ebuf, 3 * n); bad |= mk(&R.ctl, 4);
   if (bad || cudaMallocHost(&r->h_ctl, 4 * sizeof(double)) != cudaSuccess ||

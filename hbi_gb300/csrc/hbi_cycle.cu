@@ -34,6 +34,7 @@
 
 #include "../../include/hbi_gpu.h"
 #include "hbi_kernels.cuh"
+#include "hbi_rsf.cuh"
 
 namespace hbi {
 int rk_view(hbi_rk* r, RkView* v);
@@ -331,7 +332,7 @@ __global__ void __launch_bounds__(256) cycle_update_kernel(RkDev R, CycleConst P
       R.y[3 * i + 1] = tau;
       R.y[3 * i + 2] = sig;
       s = slip[i] + (vel[i] + 0.0) * dt * 0.5;
-      v = 2 * R.vref * exp(-psi / R.a[i]) * sinh(tau / sig / R.a[i]);
+      v = slip_rate(R.vref, psi, tau, sig, R.a[i]);
       s = s + (v + 0.0) * dt * 0.5;
       slip[i] = s;
       vel[i] = v;

@@ -86,7 +86,7 @@ struct EnsDev {
   double vref, minsig, maxsig, rigid_over_2vs;
   const double *a, *f0, *taudot, *sigdot, *vpl;  // per element
   const double *b, *dc;                          // per (element, member)
-  double *y, *ys, *vs, *K, *yout, *vel, *slip;   // (element[,component], member)
+  double *y, *ys, *vs, *ws, *K, *yout, *vel, *slip;  // (element[,component], member)
   float *x0, *xb[2];                             // product inputs (element, member)
   double *h, *x, *hdid, *tlim;                   // per member
   int *accepted, *done, *failed, *nr;            // per member
@@ -462,7 +462,7 @@ __global__ void __launch_bounds__(256) p3e_kernel(EnsMat A, EnsMat B, EnsDev E, 
     const double a = E.a[r], f0 = E.f0[r];
     const double bb = E.b[(int64_t)r * EM + m], dc = E.dc[(int64_t)r * EM + m];
     double k[3];
-    deriv_dev(E, gs, gn, psi, tau, sig, E.vs[(int64_t)r * EM + m], a, bb, dc, f0, k);
+    deriv_dev(E, gs, gn, psi, tau, sig, E.vs[(int64_t)r * EM + m], E.ws[(int64_t)r * EM + m], a, bb, dc, f0, k);
     double* Ks = E.K + (int64_t)s * n3 * EM + i0;
     Ks[0] = k[0]; Ks[EM] = k[1]; Ks[2 * EM] = k[2];
     const double h = E.h[m];
@@ -486,8 +486,10 @@ __global__ void __launch_bounds__(256) p3e_kernel(EnsMat A, EnsMat B, EnsDev E, 
         yn[c] = v;
         E.ys[i0 + c * EM] = v;
       }
-      const double vn = slip_rate(E.vref, yn[0], yn[1], yn[2], a);
+      double vn, wn;
+      slip_rate_w(E.vref, yn[0], yn[1], yn[2], a, &vn, &wn);
       E.vs[(int64_t)r * EM + m] = vn;
+      E.ws[(int64_t)r * EM + m] = wn;
       xnext[(int64_t)r * EM + m] = (float)(E.backslip ? (vn + 0.0) - E.vpl[r] : vn + 0.0);
     } else {
 #pragma unroll
@@ -536,8 +538,10 @@ __global__ void prepare_e_kernel(EnsDev E) {
   const int64_t i0 = (3LL * r) * EM + m;
   const double psi = E.y[i0], tau = E.y[i0 + EM], sig = E.y[i0 + 2 * EM];
   E.ys[i0] = psi; E.ys[i0 + EM] = tau; E.ys[i0 + 2 * EM] = sig;
-  const double v = slip_rate(E.vref, psi, tau, sig, E.a[r]);
+  double v, wv;
+  slip_rate_w(E.vref, psi, tau, sig, E.a[r], &v, &wv);
   E.vs[(int64_t)r * EM + m] = v;
+  E.ws[(int64_t)r * EM + m] = wv;
   E.x0[(int64_t)r * EM + m] = (float)(E.backslip ? (v + 0.0) - E.vpl[r] : v + 0.0);
 }
 
@@ -734,6 +738,7 @@ extern "C" int hbi_ens_create(hbi_ens** out, const hbi_rsf_params* p, hbi_lhp* l
   E.y = ealloc<double>(e, 3 * nm);
   E.ys = ealloc<double>(e, 3 * nm);
   E.vs = ealloc<double>(e, nm);
+  E.ws = ealloc<double>(e, nm);
   E.K = ealloc<double>(e, 18 * nm);
   E.yout = ealloc<double>(e, 3 * nm);
   E.vel = ealloc<double>(e, nm);

@@ -179,14 +179,25 @@ __global__ void __launch_bounds__(128, 2) tc_kernel(TcMat A, TcMat B, int nmat, 
     // A: FP32 rows (k, member) -> BF16 hi / lo, canonical K-major (member, k)
     const float* rows = (const float*)(stg[s] + kB);
     unsigned char* aop = stg[s] + kB + kS;
-    for (int e = tid; e < kc * EMT; e += blockDim.x) {
-      const int k = e / EMT, m = e % EMT;
-      const float v = k < nrow ? rows[k * EMT + m] : 0.f;
-      const __nv_bfloat16 hi = __float2bfloat16_rn(v);
-      const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
-      const uint32_t o = (uint32_t)(k / 16) * 4096 + umma::kmajor_offset(m, k % 16, 1024, 128);
-      *(__nv_bfloat16*)(aop + o) = hi;
-      *(__nv_bfloat16*)(aop + o + 2048) = lo;
+    // one task = one core-matrix row: member m, 8 consecutive k -> 16 bytes
+    // of hi and 16 bytes of lo
+    for (int e = tid; e < (kc / 8) * EMT; e += blockDim.x) {
+      const int kb = e / EMT, m = e % EMT;
+      uint32_t hw[4], lw[4];
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        const int k0 = kb * 8 + 2 * i;
+        const float v0 = k0 < nrow ? rows[k0 * EMT + m] : 0.f;
+        const float v1 = k0 + 1 < nrow ? rows[(k0 + 1) * EMT + m] : 0.f;
+        const __nv_bfloat162 h2 = __floats2bfloat162_rn(v0, v1);
+        const float2 hf = __bfloat1622float2(h2);
+        const __nv_bfloat162 l2 = __floats2bfloat162_rn(v0 - hf.x, v1 - hf.y);
+        hw[i] = *reinterpret_cast<const uint32_t*>(&h2);
+        lw[i] = *reinterpret_cast<const uint32_t*>(&l2);
+      }
+      const uint32_t o = (uint32_t)(kb / 2) * 4096 + umma::kmajor_offset(m, (kb % 2) * 8, 1024, 128);
+      *reinterpret_cast<uint4*>(aop + o) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+      *reinterpret_cast<uint4*>(aop + o + 2048) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
     }
     fasync();
     umma::fence_before();
@@ -225,21 +236,26 @@ __global__ void __launch_bounds__(128, 2) tc_kernel(TcMat A, TcMat B, int nmat, 
     {
       const int m = 16 * warp + lane;  // valid for lane < 16
       const uint32_t taddr = tbase + ((uint32_t)(32 * warp) << 16);
-      for (int n0c = 0; n0c < Dc.np; n0c += 16) {
-        float v[16];
-        umma::ld_32x32b_x16(taddr + n0c, v);
+      // 64 columns per round: four loads in flight, one wait
+      for (int n0c = 0; n0c < Dc.np; n0c += 64) {
+        uint32_t v[4][16];
+#pragma unroll
+        for (int q = 0; q < 4; q++) umma::ld_32x32b_x16_nowait(taddr + n0c + 16 * q, v[q]);
+        umma::wait_ld();
         if (lane < 16) {
 #pragma unroll
-          for (int i = 0; i < 16; i++) {
-            const int nn = n0c + i;
-            if (nn < Dc.nv) {
-              float* dst;
-              if (PH == 2) dst = M.gpart + ((int64_t)Dc.out0 + nn) * EMT;
-              else if (Dc.ntile == 1) dst = M.z + ((int64_t)Dc.out0 + nn) * EMT;
-              else dst = M.part + ((int64_t)Dc.poff + (int64_t)Dc.tile * Dc.nv + nn) * EMT;
-              dst[m] = v[i];
+          for (int q = 0; q < 4; q++)
+#pragma unroll
+            for (int i = 0; i < 16; i++) {
+              const int nn = n0c + 16 * q + i;
+              if (nn < Dc.nv) {
+                float* dst;
+                if (PH == 2) dst = M.gpart + ((int64_t)Dc.out0 + nn) * EMT;
+                else if (Dc.ntile == 1) dst = M.z + ((int64_t)Dc.out0 + nn) * EMT;
+                else dst = M.part + ((int64_t)Dc.poff + (int64_t)Dc.tile * Dc.nv + nn) * EMT;
+                dst[m] = __uint_as_float(v[q][i]);
+              }
             }
-          }
         }
       }
     }

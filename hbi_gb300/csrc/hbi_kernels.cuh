@@ -80,6 +80,7 @@ struct RkDev {
   double* y;       // accepted state (3n): psi,tau,sigma interleaved
   double* ys;      // stage state (3n)
   double* vs;      // slip rate of the stage state (n)
+  double* ws;      // 2 vref e^(-psi/a) cosh(tau/(sigma a)) of the stage state (n)
   double* x0;      // matvec input of stage 0 (n)
   double* xb[2];   // ping-pong matvec inputs of stages 1..5 (n)
   double* K;       // stage derivatives, 6 x 3n

@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(128) p3_rk_kernel(MatDev m0, MatDev m1, RkDev 
       const double gs = row_value(m0, r) + R.taudot[r];
       const double gn = (R.nmat == 2 ? row_value(m1, r) : 0.0) + R.sigdot[r];
       const double psi = R.ys[3 * r], tau = R.ys[3 * r + 1], sig = R.ys[3 * r + 2];
-      deriv_dev(R, gs, gn, psi, tau, sig, R.vs[r], R.a[r], R.b[r], R.dc[r], R.f0[r], k);
+      deriv_dev(R, gs, gn, psi, tau, sig, R.vs[r], R.ws[r], R.a[r], R.b[r], R.dc[r], R.f0[r], k);
       Ks[0] = k[0]; Ks[1] = k[1]; Ks[2] = k[2];
     }
     const double h = R.ctl[0];
@@ -99,8 +99,10 @@ __global__ void __launch_bounds__(128) p3_rk_kernel(MatDev m0, MatDev m1, RkDev 
         yn[c] = v;
       }
       R.ys[3 * r] = yn[0]; R.ys[3 * r + 1] = yn[1]; R.ys[3 * r + 2] = yn[2];
-      const double vn = slip_rate(R.vref, yn[0], yn[1], yn[2], R.a[r]);
+      double vn, wn;
+      slip_rate_w(R.vref, yn[0], yn[1], yn[2], R.a[r], &vn, &wn);
       R.vs[r] = vn;
+      R.ws[r] = wn;
       xnext[r] = R.backslip ? (vn + 0.0) - R.vpl[r] : vn + 0.0;
     } else {
       const double eps = R.ctl[1];
@@ -147,8 +149,10 @@ __global__ void rk_prepare_kernel(RkDev R) {
   if (r >= R.n) return;
   const double psi = R.y[3 * r], tau = R.y[3 * r + 1], sig = R.y[3 * r + 2];
   R.ys[3 * r] = psi; R.ys[3 * r + 1] = tau; R.ys[3 * r + 2] = sig;
-  const double v = slip_rate(R.vref, psi, tau, sig, R.a[r]);
+  double v, w;
+  slip_rate_w(R.vref, psi, tau, sig, R.a[r], &v, &w);
   R.vs[r] = v;
+  R.ws[r] = w;
   R.x0[r] = R.backslip ? (v + 0.0) - R.vpl[r] : v + 0.0;
 }
 

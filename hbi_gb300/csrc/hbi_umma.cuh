@@ -74,6 +74,17 @@ __device__ __forceinline__ void ld_32x32b_x16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// as ld_32x32b_x16 without the wait: several loads in flight, then wait_ld()
+__device__ __forceinline__ void ld_32x32b_x16_nowait(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+}
+__device__ __forceinline__ void wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
 // byte offset of element (row, k) of a K-major operand whose rows are
 // grouped in blocks of 8 (core matrices) with the given LBO / SBO
 __host__ __device__ inline uint32_t kmajor_offset(int row, int k, uint32_t lbo, uint32_t sbo) {

@@ -41,7 +41,7 @@ EXPORTS = [
     "hbi_mlp_create", "hbi_mlp_free", "hbi_mlp_set_params", "hbi_mlp_get_params", "hbi_mlp_loss_grad",
     "hbi_mlp_train", "hbi_mlp_predict", "hbi_plan_emulate", "hbi_umma_probe",
     "hbi_ens_create", "hbi_ens_free", "hbi_ens_set_state", "hbi_ens_get_state", "hbi_ens_run",
-    "hbi_tc_plan_emulate", "hbi_ens_use_tensor_cores",
+    "hbi_tc_plan_emulate", "hbi_ens_use_tensor_cores", "hbi_cycle_restart", "hbi_restart_point",
 ]
 
 
@@ -417,7 +417,8 @@ class Cycle:
 
     def __init__(self, rk, vel, ds, eps_r=1e-4, dtinit=1.0, dtmax=1e10, tmax_yr=1e4,
                  velth=float(np.float32(1e-2)), velmax=1e7, velmin=1e-20, dtout_yr=1.0, dtout_co=1000.0,
-                 rigid=32.04, nstep=1000000, interval=0, number=0, outdir=None, inflight=4):
+                 rigid=32.04, nstep=1000000, interval=0, number=0, outdir=None, inflight=4, restart=False):
+        """restart=True continues the run whose files are in outdir (vel is then ignored)."""
         p = CycleParams()
         p.eps_r, p.dtinit, p.dtmax, p.tmax = eps_r, dtinit, dtmax, tmax_yr * YEAR
         p.velth, p.velmax, p.velmin = velth, velmax, velmin
@@ -428,7 +429,10 @@ class Cycle:
         vel = np.ascontiguousarray(vel, dtype=np.float64)
         ds = np.ascontiguousarray(ds, dtype=np.float64)
         self.h = C.c_void_p()
-        _check(lib().hbi_cycle_create(C.byref(self.h), rk.h, _p(vel), _p(ds), C.byref(p)), "hbi_cycle_create")
+        if restart:
+            _check(lib().hbi_cycle_restart(C.byref(self.h), rk.h, _p(ds), C.byref(p)), "hbi_cycle_restart")
+        else:
+            _check(lib().hbi_cycle_create(C.byref(self.h), rk.h, _p(vel), _p(ds), C.byref(p)), "hbi_cycle_create")
         self.rk, self.n = rk, rk.n
         _register(self, 0)
 
@@ -668,3 +672,12 @@ def tc_plan_emulate(n, leaves, body, x):
     _check(lib().hbi_tc_plan_emulate(n, len(lv), lv.ctypes.data_as(_ip), _p(body), _p(x), _p(y),
                                      st.ctypes.data_as(_i64p)), "hbi_tc_plan_emulate")
     return y, dict(zip(("items1", "items2", "store1", "store2"), (int(v) for v in st)))
+
+
+def restart_point(monitor_path, interval):
+    """(k, x, next trial step, last step listed) of a monitor file (host only)."""
+    k, kend = C.c_longlong(), C.c_longlong()
+    x, dt = C.c_double(), C.c_double()
+    _check(lib().hbi_restart_point(str(monitor_path).encode(), C.c_longlong(interval), C.byref(k), C.byref(x),
+                                   C.byref(dt), C.byref(kend)), "hbi_restart_point")
+    return k.value, x.value, dt.value, kend.value

@@ -477,6 +477,14 @@ __global__ void cycle_resume_kernel(CycleState* S, int* flags, double* ctl, long
   }
   S->k_limit = k_limit;
   S->t_limit = t_limit;
+  if (t_limit <= S->x) {
+    // already at (or past) the time limit: nothing to run
+    S->stop = HBI_STOP_TLIMIT;
+    S->halted = 1;
+    flags[0] = 1;
+    flags[1] = 1;
+    return;
+  }
   double h = S->h;
   if (S->clamped) {
     h = S->h_pending;
@@ -576,6 +584,7 @@ struct hbi_cycle_s {
   std::vector<double> trace;
   long long nlaunch = 0;
   long long attempts = 0;
+  long long kend = -1;  // a restart does not rewrite monitor lines up to this step
   CycleState last{};
   std::FILE *fmon = nullptr, *ftime = nullptr, *fevent = nullptr;
   std::FILE* ffield[5] = {};
@@ -618,7 +627,7 @@ double wall_since(const std::chrono::steady_clock::time_point& t) {
 
 // monitor line (main_LH.f90:1489-1493): '(i7,f19.4,7e16.5,i4,f16.4)'
 void write_monitor(hbi_cycle* c, const CycleState& s, double errmax, double dtdid, int nrjct) {
-  if (!c->fmon) return;
+  if (!c->fmon || s.k <= c->kend) return;
   std::string l;
   fort_i(l, 7, s.k);
   fort_f(l, 19, 4, s.x);
@@ -775,8 +784,26 @@ extern "C" int hbi_cycle_free(hbi_cycle* c) {
   return HBI_OK;
 }
 
+namespace {
+// where a restarted loop resumes (main_LH.f90:836-957)
+struct RestartPoint {
+  long long k, kend;   // steps done; last step already in the monitor file
+  double x, h;
+  std::vector<double> slip;
+};
+
+int cycle_create_impl(hbi_cycle** out, hbi_rk* rk, const double* vel, const double* ds, const hbi_cycle_params* p,
+                      const RestartPoint* rs);
+}  // namespace
+
 extern "C" int hbi_cycle_create(hbi_cycle** out, hbi_rk* rk, const double* vel, const double* ds,
                                 const hbi_cycle_params* p) {
+  return cycle_create_impl(out, rk, vel, ds, p, nullptr);
+}
+
+namespace {
+int cycle_create_impl(hbi_cycle** out, hbi_rk* rk, const double* vel, const double* ds, const hbi_cycle_params* p,
+                      const RestartPoint* rs) {
   if (!out || !rk || !vel || !ds || !p) return cfail(HBI_ERR_ARG, "hbi_cycle_create: null argument");
   if (p->inflight < 1 || p->inflight > hbi_cycle_s::kMaxInflight)
     return cfail(HBI_ERR_ARG, "inflight must be in 1..%d", hbi_cycle_s::kMaxInflight);
@@ -846,24 +873,27 @@ extern "C" int hbi_cycle_create(hbi_cycle** out, hbi_rk* rk, const double* vel, 
     c->m_rest[i].skip = c->dflags;
   }
   CycleState s0{};
-  s0.x = 0.0;
-  s0.h = p->dtinit;
+  s0.x = rs ? rs->x : 0.0;
+  s0.k = rs ? rs->k : 0;
+  s0.h = rs ? rs->h : p->dtinit;
+  c->kend = rs ? rs->kend : -1;
   s0.dtout = p->dtout_inter;
   s0.tout = s0.dtout;
   s0.t_limit = INFINITY;
   s0.k_limit = p->nstep > 0 ? p->nstep : (1LL << 62);
   s0.snap = -1;
   s0.hist_e1 = 0.5;
-  s0.hist_h1 = p->dtinit;
+  s0.hist_h1 = s0.h;
   s0.learned = 0;
   const int zf[4] = {0, 0, 0, 0};
-  const double ctl2[2] = {p->dtinit, p->eps_r};
+  const double ctl2[2] = {s0.h, p->eps_r};
   cudaStream_t st = c->st;
   if (cudaMemcpyAsync(c->dS, &s0, sizeof s0, cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemcpyAsync(c->dflags, zf, sizeof zf, cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemcpyAsync(c->R.ctl, ctl2, sizeof ctl2, cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemcpyAsync(c->dvel, vel, sizeof(double) * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
-      cudaMemsetAsync(c->dslip, 0, sizeof(double) * n, st) != cudaSuccess ||
+      (rs ? cudaMemcpyAsync(c->dslip, rs->slip.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st)
+          : cudaMemsetAsync(c->dslip, 0, sizeof(double) * n, st)) != cudaSuccess ||
       cudaMemsetAsync(c->dislip, 0, sizeof(double) * n, st) != cudaSuccess ||
       cudaMemcpyAsync(c->dds, ds, sizeof(double) * n, cudaMemcpyHostToDevice, st) != cudaSuccess)
     return fail_free(HBI_ERR_CUDA, "upload");
@@ -885,16 +915,17 @@ extern "C" int hbi_cycle_create(hbi_cycle** out, hbi_rk* rk, const double* vel, 
       snprintf(fn, sizeof fn, "%s/%s%d.dat", p->outdir, stem, p->number);
       return std::fopen(fn, mode);
     };
-    c->fmon = open("monitor", "w");
-    c->ftime = open("time", "w");
-    c->fevent = open("event", "w");
+    // a restart appends to the files of the run it continues (EQslip restarts)
+    c->fmon = open("monitor", rs ? "a" : "w");
+    c->ftime = open("time", rs ? "a" : "w");
+    c->fevent = open("event", rs ? "a" : "w");
     const char* stems[5] = {"vel", "slip", "sigma", "tau", "EQslip"};
-    for (int f = 0; f < 5; f++) c->ffield[f] = open(stems[f], "wb");
+    for (int f = 0; f < 5; f++) c->ffield[f] = open(stems[f], (rs && f < 4) ? "ab" : "wb");
     if (!c->fmon || !c->ftime || !c->fevent || !c->ffield[0] || !c->ffield[4])
       return fail_free(HBI_ERR_ARG, "cannot open output files");
   }
   c->t1 = std::chrono::steady_clock::now();
-  if (p->outdir) {
+  if (p->outdir && !rs) {
     // k = 0 outputs: time line, monitor line, fields (vel, slip=0, sigma, tau)
     write_time(c, 0, 0.0);
     write_monitor(c, s, 0.0, 0.0, 0);
@@ -921,6 +952,110 @@ extern "C" int hbi_cycle_create(hbi_cycle** out, hbi_rk* rk, const double* vel, 
   if (ie != cudaSuccess) return fail_free(HBI_ERR_CUDA, "graph instantiate");
   *out = c;
   return HBI_OK;
+}
+
+// one Fortran E/F field: also accepts the exponent without its letter
+// ("0.12345-100") that Ew.d writes for three-digit exponents
+bool fort_read(const char*& p, double* v) {
+  while (*p == ' ' || *p == '\t') p++;
+  if (!*p || *p == '\n') return false;
+  char* end = nullptr;
+  double d = strtod(p, &end);
+  if (end == p) return false;
+  if ((*end == '+' || *end == '-') && end[1] >= '0' && end[1] <= '9') {
+    char* e2 = nullptr;
+    const long ex = strtol(end, &e2, 10);
+    d *= pow(10.0, (double)ex);
+    end = e2;
+  }
+  p = end;
+  *v = d;
+  return true;
+}
+}  // namespace
+
+extern "C" int hbi_restart_point(const char* monitor_path, long long interval, long long* k, double* x,
+                                 double* dtnxt, long long* kend) {
+  if (!monitor_path || !k || !x || !dtnxt || interval < 1) return cfail(HBI_ERR_ARG, "hbi_restart_point: arguments");
+  std::FILE* f = std::fopen(monitor_path, "r");
+  if (!f) return cfail(HBI_ERR_ARG, "hbi_restart_point: cannot open %s", monitor_path);
+  char line[1024];
+  long long kk = -1, klast = -1;
+  double xx = 0, dn = 0;
+  while (std::fgets(line, sizeof line, f)) {
+    const char* q = line;
+    double v[11];
+    int nv = 0;
+    while (nv < 11 && fort_read(q, &v[nv])) nv++;
+    if (nv < 10) continue;
+    const long long kl = (long long)v[0];
+    klast = kl;
+    if (kl % interval == 0) {
+      // main_LH.f90:841-845: x and the next trial step of the last line
+      // whose step is a multiple of the output interval
+      kk = kl;
+      xx = v[1];
+      const double errmax = v[7], dtdid = v[8];
+      dn = std::min(2 * dtdid, (double)0.9f * dtdid * pow(errmax, (double)-0.2f));
+    }
+  }
+  std::fclose(f);
+  if (kk < 0) return cfail(HBI_ERR_STATE, "hbi_restart_point: no step at a multiple of the interval in %s", monitor_path);
+  *k = kk;
+  *x = xx;
+  *dtnxt = dn;
+  if (kend) *kend = klast;
+  return HBI_OK;
+}
+
+extern "C" int hbi_cycle_restart(hbi_cycle** out, hbi_rk* rk, const double* ds, const hbi_cycle_params* p) {
+  if (!out || !rk || !ds || !p || !p->outdir) return cfail(HBI_ERR_ARG, "hbi_cycle_restart: arguments");
+  RkView V{};
+  int rc = rk_view(rk, &V);
+  if (rc) return rc;
+  const int n = V.n;
+  char fn[1024];
+  snprintf(fn, sizeof fn, "%s/monitor%d.dat", p->outdir, p->number);
+  const long long interval = p->interval > 0 ? p->interval : (p->nstep > 0 ? p->nstep : 1LL << 62);
+  RestartPoint rs;
+  long long k0;
+  rc = hbi_restart_point(fn, interval, &k0, &rs.x, &rs.h, &rs.kend);
+  if (rc) return rc;
+  rs.k = k0;
+  // the last snapshot of each field file (main_LH.f90:867-897)
+  std::vector<double> fld[4];
+  const char* stems[4] = {"vel", "slip", "sigma", "tau"};
+  for (int f = 0; f < 4; f++) {
+    snprintf(fn, sizeof fn, "%s/%s%d.dat", p->outdir, stems[f], p->number);
+    std::FILE* fp = std::fopen(fn, "rb");
+    if (!fp) return cfail(HBI_ERR_ARG, "hbi_cycle_restart: cannot open %s", fn);
+    std::fseek(fp, 0, SEEK_END);
+    const long sz = std::ftell(fp);
+    if (sz < (long)sizeof(double) * n) {
+      std::fclose(fp);
+      return cfail(HBI_ERR_STATE, "hbi_cycle_restart: %s holds no snapshot", fn);
+    }
+    fld[f].resize(n);
+    std::fseek(fp, sz - (long)sizeof(double) * n, SEEK_SET);
+    const size_t got = std::fread(fld[f].data(), sizeof(double), n, fp);
+    std::fclose(fp);
+    if (got != (size_t)n) return cfail(HBI_ERR_STATE, "hbi_cycle_restart: short read of %s", fn);
+  }
+  rs.slip = fld[1];
+  // psi from the slip rate and stresses (main_LH.f90:899)
+  std::vector<double> a(n), y(3 * (size_t)n);
+  if (cudaMemcpy(a.data(), V.R.a, sizeof(double) * n, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return cfail(HBI_ERR_CUDA, "hbi_cycle_restart: a");
+  const double vref = V.R.vref;
+  for (int i = 0; i < n; i++) {
+    const double vel = fld[0][i], sig = fld[2][i], tau = fld[3][i];
+    y[3 * (size_t)i] = a[i] * log(2 * vref / vel * sinh(tau / sig / a[i]));
+    y[3 * (size_t)i + 1] = tau;
+    y[3 * (size_t)i + 2] = sig;
+  }
+  rc = hbi_rk_set_state(rk, y.data());
+  if (rc) return rc;
+  return cycle_create_impl(out, rk, fld[0].data(), ds, p, &rs);
 }
 
 extern "C" int hbi_cycle_run(hbi_cycle* c, long long k_limit, double t_limit, hbi_cycle_status* out) {

@@ -247,6 +247,17 @@ int hbi_cycle_create(hbi_cycle** c, hbi_rk* rk, const double* vel, const double*
 /* Runs until a stop control fires, until k reaches k_limit (<=0: none) or x
  * reaches t_limit (<=0: none; the last step is shortened to land on it). */
 int hbi_cycle_run(hbi_cycle* c, long long k_limit, double t_limit, hbi_cycle_status* st);
+/* Restart (main_LH.f90:836-957): continue the loop of an earlier run with the
+ * same outdir, number and interval.  From monitor<number>.dat the last step k
+ * that is a multiple of `interval` gives x and the next trial step
+ * min(2 dtdid, 0.9 dtdid errmax^-0.2); the last snapshots of the vel, slip,
+ * sigma and tau files give the state (psi from vel, tau, sigma, main_LH.f90:
+ * 899).  The loop resumes at step k + 1, appends to the files (EQslip starts
+ * anew) and does not rewrite monitor lines already in the file. */
+int hbi_cycle_restart(hbi_cycle** c, hbi_rk* rk, const double* ds, const hbi_cycle_params* p);
+/* the restart point of a monitor file: k, x, next trial step, last step listed */
+int hbi_restart_point(const char* monitor_path, long long interval, long long* k, double* x, double* dtnxt,
+                      long long* kend);
 /* slip and slip rate (ncell, cluster order); the state y via hbi_rk_get_state */
 int hbi_cycle_fields(hbi_cycle* c, double* vel, double* slip);
 /* finished events so far; *count = their number (up to max are copied) */

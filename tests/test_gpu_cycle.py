@@ -150,3 +150,37 @@ def test_zero_proposer_is_the_classic_controller(system):
     c.set_proposer(w)
     c.run(k_limit=250)
     assert c.trace()[-1, 1] < a.trace()[-1, 1]
+
+
+def test_cycle_restart_continues_a_run(system, tmp_path):
+    """A run stopped at step 100 and restarted from its own files
+    (main_LH.f90:836-957) reaches the same state at a later time as an
+    uninterrupted run (before the first earthquake).  The restart point
+    carries x to 1e-4 s and the next step to 5 digits (the monitor file's
+    formats) and psi is rebuilt from V, so the two runs take different steps
+    at the RK tolerance: the states agree to 1e-5, the slip to 1e-4."""
+    out = str(tmp_path)
+    a = _cycle(system, outdir=out, number=3, interval=50)
+    sa = a.run(k_limit=100)  # about 12.7 years: interseismic
+    a.close()
+    assert sa["x"] < 16.0 * H.YEAR
+    T = 16.0 * H.YEAR  # the nucleation starts after 21 years
+    p = system["p"]
+    rk = H.RK(system["lh"], None, evlaw=0, a=p["a"], b=p["b"], dc=p["dc"], f0=p["f0"], vpl=p["vpl"])
+    b = H.Cycle(rk, p["vel"], system["ds"], eps_r=1e-6, tmax_yr=1500.0, outdir=out, number=3, interval=100,
+                restart=True)
+    sb = b.run(t_limit=T)
+    yb = rk.get_state()
+    _, slip_b = b.fields()
+    c = _cycle(system)
+    sc = c.run(t_limit=T)
+    yc = c.rk.get_state()
+    _, slip_c = c.fields()
+    assert sb["x"] == T and sc["x"] == T
+    assert np.linalg.norm(yb - yc) <= 1e-5 * np.linalg.norm(yc)
+    assert np.linalg.norm(slip_b - slip_c) <= 1e-4 * np.linalg.norm(slip_c)
+    mon = open(os.path.join(out, "monitor3.dat")).read().splitlines()
+    ks = [int(l[:7]) for l in mon]
+    assert ks[:101] == list(range(101)) and ks[101] == 101 and len(set(ks)) == len(ks)
+    # a limit already reached runs nothing
+    assert b.run(t_limit=T)["stop_name"] == "tlimit"

@@ -91,3 +91,36 @@ def test_stl_roundtrip(tmp_path):
     assert np.array_equal(xs[0], tri[:, 0, 0]) and np.array_equal(zs[2], tri[:, 2, 2])
     # the reference counts facets as lines/7
     assert len(open(p).read().splitlines()) // 7 == len(tri)
+
+
+def _fort_e(v, w=16, d=5):
+    if v == 0:
+        s = "0." + "0" * d + "E+00"
+    else:
+        m, e = f"{abs(v):.{d - 1}e}".split("e")
+        e = int(e) + 1
+        digits = m.replace(".", "")
+        ex = f"E{'+' if e >= 0 else '-'}{abs(e):02d}" if abs(e) <= 99 else f"{'+' if e >= 0 else '-'}{abs(e):03d}"
+        s = ("-" if v < 0 else "") + "0." + digits + ex
+    return s.rjust(w)
+
+
+def test_restart_point_follows_the_reference_rule(tmp_path):
+    """main_LH.f90:836-849: the last monitor line with k % interval == 0 gives
+    x and the next trial step min(2 dtdid, 0.9 dtdid errmax**-0.2); Fortran's
+    exponent without its letter (three digits) is read too."""
+    lines = []
+    for k in range(0, 251):
+        x = 1000.0 * k
+        errmax, dtdid = 0.25 + 0.001 * k, 10.0 + k
+        wall = 1e-120 if k == 200 else 0.5
+        l = f"{k:7d}{x:19.4f}" + "".join(_fort_e(v) for v in (-9.0, 1e-3, 0.6, 50.0, 50.0, errmax, dtdid))
+        l += f"{0:4d}{wall:16.4f}" if k != 200 else f"{0:4d}" + _fort_e(wall)
+        lines.append(l)
+    p = tmp_path / "monitor1.dat"
+    p.write_text("\n".join(lines) + "\n")
+    k, x, dt, kend = H.restart_point(p, 100)
+    assert (k, kend) == (200, 250)
+    assert x == 200000.0
+    e, h = float(_fort_e(0.45)), float(_fort_e(210.0))
+    assert abs(dt - min(2 * h, float(np.float32(0.9)) * h * e ** float(np.float32(-0.2)))) <= 1e-12 * dt

@@ -18,7 +18,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "lib", "libhbigpu.so")
 
-HBI_2DVS, HBI_3DPH, HBI_3DNR, HBI_3DNT = 1, 2, 3, 4
+HBI_2DVS, HBI_3DPH, HBI_3DNR, HBI_3DNT, HBI_2DPH, HBI_2DN, HBI_3DHT = 1, 2, 3, 4, 5, 6, 7
 STORE_F64, STORE_F32, STORE_BF16 = 0, 1, 2
 STORE_NAMES = {"f64": STORE_F64, "f32": STORE_F32, "bf16": STORE_BF16}
 HBI_ERR_CONVERGE = -5
@@ -60,7 +60,8 @@ class Bemv(C.Structure):
                 + [(f, _dp) for f in ("xcol", "ycol", "zcol", "xel", "xer", "ang", "angd", "dsl", "dsd", "rake")]
                 + [("w", C.c_double)]
                 + [(f, _dp) for f in ("xs1", "xs2", "xs3", "ys1", "ys2", "ys3", "zs1", "zs2", "zs3", "ev11",
-                                      "ev12", "ev13", "ev21", "ev22", "ev23", "ev31", "ev32", "ev33")])
+                                      "ev12", "ev13", "ev21", "ev22", "ev23", "ev31", "ev32", "ev33",
+                                      "yel", "yer")])
 
 
 class CycleParams(C.Structure):

@@ -95,6 +95,13 @@ def c3_3dnt(nx=500, nz=200, length=60.0, width=30.0, seed=0, eps_h=1e-4):
     return Workload(f"c3_3dnt_{n}", HBI_3DNT, n, g, 2, 1, area, params, eps_h, 100.0)
 
 
+def c5_3dnt(seed=0):
+    """Configuration 5: the c3 fault meshed with 500,000 triangles."""
+    w = c3_3dnt(1000, 250, seed=seed)
+    w.name = f"c5_3dnt_{w.nd}"
+    return w
+
+
 def ensemble_params(M=64, seed=0):
     """c4: per-member b in [0.012, 0.018] and Dc in [5, 30] mm."""
     rng = np.random.default_rng(seed)

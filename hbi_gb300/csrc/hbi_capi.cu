@@ -96,11 +96,16 @@ struct DevGeom {
     rc |= put(&b.ev11, h->ev11, n, st); rc |= put(&b.ev12, h->ev12, n, st); rc |= put(&b.ev13, h->ev13, n, st);
     rc |= put(&b.ev21, h->ev21, n, st); rc |= put(&b.ev22, h->ev22, n, st); rc |= put(&b.ev23, h->ev23, n, st);
     rc |= put(&b.ev31, h->ev31, n, st); rc |= put(&b.ev32, h->ev32, n, st); rc |= put(&b.ev33, h->ev33, n, st);
+    rc |= put(&b.yel, h->yel, n, st); rc |= put(&b.yer, h->yer, n, st);
     // host-evaluated trig of the per-source angles, as okada_ij / okada form them
     if (h->ang) {
-      std::vector<double> c(n), s(n);
-      for (int i = 0; i < n; i++) { c[i] = std::cos(h->ang[i]); s[i] = std::sin(h->ang[i]); }
+      std::vector<double> c(n), s(n), c2(n), s2(n);
+      for (int i = 0; i < n; i++) {
+        c[i] = std::cos(h->ang[i]); s[i] = std::sin(h->ang[i]);
+        c2[i] = std::cos(2 * h->ang[i]); s2[i] = std::sin(2 * h->ang[i]);
+      }
       rc |= put_vec(&b.cang, c, st); rc |= put_vec(&b.sang, s, st);
+      rc |= put_vec(&b.cang2, c2, st); rc |= put_vec(&b.sang2, s2, st);
     }
     if (h->rake) {
       std::vector<double> c(n), s(n);
@@ -142,11 +147,17 @@ int check_bemv(const hbi_bemv* b) {
       if (!b->xcol || !b->ycol || !b->zcol || !b->ang || !b->angd || !b->dsl || !b->dsd || !b->rake || !(b->w > 0))
         return fail(HBI_ERR_ARG, "okada problems need xcol,ycol,zcol,ang,angd,dsl,dsd,rake and w>0");
       break;
+    case HBI_2DPH:
+    case HBI_2DN:
+      if (!b->xcol || !b->ycol || !b->xel || !b->xer || !b->yel || !b->yer || !b->ang)
+        return fail(HBI_ERR_ARG, "2dph / 2dn need xcol, ycol, xel, xer, yel, yer, ang");
+      break;
     case HBI_3DNT:
+    case HBI_3DHT:
       if (!b->xcol || !b->ycol || !b->zcol || !b->xs1 || !b->xs2 || !b->xs3 || !b->ys1 || !b->ys2 || !b->ys3 ||
           !b->zs1 || !b->zs2 || !b->zs3 || !b->ev11 || !b->ev12 || !b->ev13 || !b->ev21 || !b->ev22 || !b->ev23 ||
           !b->ev31 || !b->ev32 || !b->ev33 || !b->rake)
-        return fail(HBI_ERR_ARG, "3dnt needs collocation points, vertices, ev frames and rake");
+        return fail(HBI_ERR_ARG, "3dnt / 3dht need collocation points, vertices, ev frames and rake");
       break;
     default:
       return fail(HBI_ERR_ARG, "problem %d is not on the hot path", b->problem);
@@ -1022,6 +1033,17 @@ extern "C" int hbi_rkqs(hbi_rk* r, double* x, double htry, double eps, double dt
 // stage, 16-byte alignment, indices inside z / x / partials).  stats (8):
 // phase-1 items, phase-2 items, V store, U store (elements), z length,
 // phase-1 partials, phase-2 partials, conversion segments.
+//
+// chunks_fit: a column segment of ntp rows gives whole chunks of 16 to 128
+// columns inside both stage sizes of the phase kernels (8 KB and 16 KB).
+static bool chunks_fit(int ntp, int esz) {
+  for (int sb : {8192, 16384}) {
+    const int cc = chunk_cols(ntp, esz, sb);
+    if (cc < 16 || cc > 128 || (int64_t)cc * ntp * esz > sb) return false;
+  }
+  return true;
+}
+
 extern "C" int hbi_plan_emulate(int n, int nleaf, const int* lv6, const double* body, int vec, const double* x,
                                 double* y, int64_t* stats) {
   if (n < 1 || nleaf < 1 || !lv6 || !body || !x || !y || (vec != 2 && vec != 4 && vec != 8))
@@ -1052,8 +1074,7 @@ extern "C" int hbi_plan_emulate(int n, int nleaf, const int* lv6, const double* 
   }
   std::vector<double> z(std::max<int64_t>(P.zlen, 1), 0.0), part(std::max<int64_t>(P.plen1, 1), 0.0);
   for (const S1Item& it : P.p1) {
-    if (it.ncols < 1 || it.ntp % vec || it.ntp > 32 * vec || chunk_cols(it.ntp, esz) < 32 ||
-        chunk_cols(it.ntp, esz) > 256 || (int64_t)chunk_cols(it.ntp, esz) * it.ntp * esz > 16384 || it.soff % vec ||
+    if (it.ncols < 1 || it.ntp % vec || it.ntp > 32 * vec || !chunks_fit(it.ntp, esz) || it.soff % vec ||
         it.soff + (int64_t)it.ncols * it.ntp > P.vstore || it.x0 < 0 || it.x0 + it.nt > n || it.nt > it.ntp ||
         it.z0 < 0 || it.z0 + it.ncols > P.zlen ||
         (it.ntile > 1 && (it.cg < 0 || it.cg >= P.ncg || it.poff < 0 ||
@@ -1075,13 +1096,9 @@ extern "C" int hbi_plan_emulate(int n, int nleaf, const int* lv6, const double* 
       }
   std::vector<double> gp(std::max<int64_t>(P.plen2, 1), 0.0);
   for (const S2Item& it : P.p2) {
-    const int cc = chunk_cols(it.ntp, esz);
-    const int64_t last_chunk = (int64_t)(it.ncols - 1) / cc * cc;
-    const int64_t midx_end = it.m0 + last_chunk + ((it.ncols - last_chunk + 3) / 4) * 4;
-    if (it.ncols < 1 || it.ntp % vec || it.ntp > 32 * vec || cc < 32 || cc > 256 || (int64_t)cc * it.ntp * esz > 16384 ||
-        ((cc + 3) / 4) * 16 > 1024 || it.soff % vec ||
-        it.soff + (int64_t)it.ncols * it.ntp > P.ustore || it.nr > it.ntp || it.m0 < 0 || it.m0 % 4 ||
-        midx_end > (int64_t)P.midx.size() || it.pout < 0 || it.pout + it.nr > P.plen2)
+    if (it.ncols < 1 || it.ntp % vec || it.ntp > 32 * vec || !chunks_fit(it.ntp, esz) || it.soff % vec ||
+        it.soff + (int64_t)it.ncols * it.ntp > P.ustore || it.nr > it.ntp || it.m0 < 0 ||
+        it.m0 + (int64_t)it.ncols > (int64_t)P.midx.size() || it.pout < 0 || it.pout + it.nr > P.plen2)
       return fail(HBI_ERR_STATE, "phase-2 item out of bounds");
     for (int r = 0; r < it.nr; r++) {
       double t = 0.0;

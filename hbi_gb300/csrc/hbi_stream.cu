@@ -3,20 +3,19 @@
 // streams of bulk asynchronous copies.
 //
 // The factor store is laid out in row tiles (hbi_structure.cpp, plan_stream):
-// every work item reads one contiguous region of at most 16 KB -- up to 32
-// column segments of one tile of a column group (phase 1) or of a row group
-// (phase 2).  Each warp of a block owns NS shared-memory stages with one
-// mbarrier each; one lane starts a cp.async.bulk (TMA) copy of an item's
-// region into a free stage while the warp consumes an earlier stage, so the
-// bytes in flight per SM are set by the stages (NW x NS x 16 KB), not by
-// registers.  The small per-item operands (x rows, z / x multipliers) are
-// loaded by the lanes one item ahead of their use.
+// every work item reads one contiguous region -- the column segments of one
+// tile of a column group (phase 1) or of a row group (phase 2) -- in chunks of
+// whole columns that fill one shared-memory stage (8 KB or 16 KB).  Each warp
+// of a block owns NS stages with one mbarrier each; one lane starts a
+// cp.async.bulk (TMA) copy of a chunk into a free stage while the warp
+// consumes an earlier stage.  The small per-item operands (x rows) are loaded
+// one item ahead of their use, phase 2's multipliers one chunk ahead.
 //
 // Lanes work on a stage as column slots: a segment of ntp rows is covered by
 // LW = pow2ceil(ntp / VEC) lanes with one 16-byte vector each, and CS = 32/LW
 // slots take different columns.  Phase 1 reduces each column over its LW
 // lanes (z = V^T x, partial per row tile, combined by the last tile of a
-// column chunk); phase 2 accumulates y rows per lane and reduces over the
+// column group); phase 2 accumulates y rows per lane and reduces over the
 // slots once per item.  Every sum has a fixed order: results are
 // deterministic run to run.
 //
@@ -36,7 +35,6 @@ namespace hbi {
 
 namespace {
 
-constexpr int kStage = 16384;  // bytes per stage: 32 segments x 512 bytes
 constexpr long long kWaitCycles = 2LL << 30;
 
 template <typename T>
@@ -113,19 +111,19 @@ __device__ __forceinline__ void lds16(const __nv_bfloat16* p, float* o) {
 
 __device__ __forceinline__ int log2ceil(int n) { return n <= 1 ? 0 : 32 - __clz(n - 1); }
 
-// shared memory of a block: per warp NS stages of [16 KB data][1 KB column
-// indices], then per warp 256 multipliers, then the stage barriers
-constexpr int kIdx = 1024;
-constexpr int kStageAll = kStage + kIdx;
-template <int NW, int NS>
+// shared memory of a block: per warp NS stages of SB bytes, then per warp the
+// 128 multipliers of its current phase-2 chunk, then the stage barriers
+constexpr int kMaxCols = 128;  // columns of a chunk at most (chunk_cols)
+constexpr int kMu = kMaxCols * 8;
+template <int NW, int NS, int SB>
 struct Ring {
-  unsigned char* buf;  // stage s at buf + s * kStageAll
-  void* mu;            // 256 multipliers (Acc) of the warp
+  unsigned char* buf;  // stage s at buf + s * SB
+  void* mu;            // kMaxCols multipliers (Acc) of the warp
   uint64_t* bar;
   __device__ Ring(unsigned char* smem, int warp) {
-    buf = smem + (size_t)warp * NS * kStageAll;
-    mu = smem + (size_t)NW * NS * kStageAll + (size_t)warp * 256 * 8;
-    bar = reinterpret_cast<uint64_t*>(smem + (size_t)NW * NS * kStageAll + (size_t)NW * 256 * 8) + warp * NS;
+    buf = smem + (size_t)warp * NS * SB;
+    mu = smem + (size_t)NW * NS * SB + (size_t)warp * kMu;
+    bar = reinterpret_cast<uint64_t*>(smem + (size_t)NW * NS * SB + (size_t)NW * kMu) + warp * NS;
   }
 };
 
@@ -153,8 +151,12 @@ __device__ void drain(uint64_t* bar, int c_seq, int p_seq) {
   __syncwarp();
 }
 
-// as chunk_cols (hbi_structure.hpp): whole columns in 16 KB, multiple of 32, at most 256
-__device__ __forceinline__ int chunk_cols_dev(int ntp, int esz) { return min((kStage / (ntp * esz)) / 32 * 32, 256); }
+// as chunk_cols (hbi_structure.hpp): whole columns in SB bytes, a multiple of
+// 16, at most 128
+template <int SB>
+__device__ __forceinline__ int chunk_cols_dev(int ntp, int esz) {
+  return min((SB / (ntp * esz)) / 16 * 16, kMaxCols);
+}
 
 // arrival count with release (prior writes of the warp, ordered by the
 // __syncwarp before it) and acquire (the partials of the other tiles)
@@ -168,18 +170,20 @@ __device__ __forceinline__ int arrive_acq_rel(int* p) {
 
 // ---------------------------------------------------------------- phase 1
 // Item = one row tile of a column group over all its columns; streamed in
-// chunks of up to 16 KB.  Column sums of a chunk go to z (one tile) or to the
-// tile's partials; the last tile of the group to finish sums the partials.
-template <typename T, int NW, int NS>
+// chunks of up to SB bytes.  Column sums of a chunk go to z (one tile) or to
+// the tile's partials; the last tile of the group to finish sums the
+// partials.
+template <typename T, int NW, int NS, int SB>
 __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev m1, int nmat,
                                                                const double* __restrict__ x) {
   typedef typename AccT<T>::type Acc;
   constexpr int VEC = 16 / sizeof(T);
   constexpr int ESZ = sizeof(T);
+  constexpr int BF = SB / 512;  // columns of a chunk of full-height (512-byte) segments
   extern __shared__ __align__(128) unsigned char smem[];
   if (m0.skip && __ldcg(m0.skip)) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  Ring<NW, NS> R(smem, warp);
+  Ring<NW, NS, SB> R(smem, warp);
   if (lane == 0) {
     for (int s = 0; s < NS; s++) mbar_init(&R.bar[s], 1);
     fence_mbar_init();
@@ -197,14 +201,14 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
   S1ItemDev Dp = desc(p_it), Dpn = desc(p_it + GW);
   auto produce = [&]() {
     if (p_it >= ntot) return;
-    const int nc = min(chunk_cols_dev(Dp.ntp, ESZ), Dp.ncols - p_c0);
+    const int nc = min(chunk_cols_dev<SB>(Dp.ntp, ESZ), Dp.ncols - p_c0);
     const int s = p_seq % NS;
     if (lane == 0) {
       const uint32_t bytes = (uint32_t)(nc * Dp.ntp * ESZ);
       const T* src = (const T*)(p_it < n0 ? m0.vstore : m1.vstore) + Dp.soff + (int64_t)p_c0 * Dp.ntp;
       fence_proxy_async();
       mbar_expect_tx(&R.bar[s], bytes);
-      bulk_g2s(R.buf + s * kStageAll, src, bytes, &R.bar[s]);
+      bulk_g2s(R.buf + s * SB, src, bytes, &R.bar[s]);
     }
     p_seq++;
     p_c0 += nc;
@@ -239,21 +243,22 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
       drain<NS>(R.bar, c_seq, p_seq);
       return;
     }
-    const int nc = min(chunk_cols_dev(Dc.ntp, ESZ), Dc.ncols - c_c0);
-    const T* st = (const T*)(R.buf + s * kStageAll);
+    const int nc = min(chunk_cols_dev<SB>(Dc.ntp, ESZ), Dc.ncols - c_c0);
+    const T* st = (const T*)(R.buf + s * SB);
     const int nq = Dc.ntp / VEC;
     const int lw = log2ceil(nq), LW = 1 << lw, CS = 32 >> lw;
     const int slot = lane >> lw, j = lane & (LW - 1);
     Acc* z = (Acc*)M.z;
     Acc* part = (Acc*)M.part;
     if (LW == 32) {
-      // full-height tiles: 32 columns at a time, reduced by a butterfly
-      // reduce-scatter (31 shuffle-adds per lane for 32 columns); lane L ends
-      // with the sum of column r0 + L
-      for (int r0 = 0; r0 < nc; r0 += 32) {
-        Acc p[32];
+      // tall tiles: BF columns at a time, reduced by a butterfly
+      // reduce-scatter inside groups of BF lanes (BF-1 shuffle-adds per lane
+      // for BF columns), then across the groups; lane L ends with the sum of
+      // column r0 + L % BF
+      for (int r0 = 0; r0 < nc; r0 += BF) {
+        Acc p[BF];
 #pragma unroll
-        for (int u = 0; u < 32; u++) {
+        for (int u = 0; u < BF; u++) {
           p[u] = 0;
           if (r0 + u < nc && j < nq) {
             Acc a[VEC];
@@ -263,7 +268,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
           }
         }
 #pragma unroll
-        for (int lev = 16; lev >= 1; lev >>= 1) {
+        for (int lev = BF / 2; lev >= 1; lev >>= 1) {
           const bool upper = (lane & lev) != 0;
 #pragma unroll
           for (int i = 0; i < lev; i++) {
@@ -272,7 +277,9 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
             p[i] = keep + __shfl_xor_sync(0xffffffffu, send, lev);
           }
         }
-        if (r0 + lane < nc) {
+#pragma unroll
+        for (int o = BF; o < 32; o <<= 1) p[0] += __shfl_xor_sync(0xffffffffu, p[0], o);
+        if (lane < BF && r0 + lane < nc) {
           const int col = c_c0 + r0 + lane;
           if (Dc.ntile == 1) z[Dc.z0 + col] = p[0];
           else part[Dc.poff + (int64_t)Dc.tile * Dc.ncols + col] = p[0];
@@ -344,20 +351,24 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
 
 // ---------------------------------------------------------------- phase 2
 // Item = one row tile of a row group over all its columns, streamed in chunks
-// of up to 16 KB together with the chunk's multiplier indices; the lanes
-// gather the multipliers (z for low-rank columns, x for dense ones) into
-// shared memory, then accumulate their rows; one reduction over the column
-// slots per item.
-template <typename T, int NW, int NS>
+// of up to SB bytes.  A chunk's multipliers (z for low-rank columns, x for
+// dense ones) are fetched ahead of it: the column indices when the chunk's
+// copy starts (NS chunks ahead), the gather of z / x one chunk ahead, so that
+// neither latency falls between a stage's arrival and its use.  Lanes
+// accumulate their rows over the item's chunks; one reduction over the
+// column slots per item.
+template <typename T, int NW, int NS, int SB>
 __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev m1, int nmat,
                                                                const double* __restrict__ x) {
   typedef typename AccT<T>::type Acc;
   constexpr int VEC = 16 / sizeof(T);
   constexpr int ESZ = sizeof(T);
+  constexpr int KP = kMaxCols / 32;  // multipliers per lane of one chunk
+  static_assert(NS >= 2, "the multiplier gather runs one chunk ahead");
   extern __shared__ __align__(128) unsigned char smem[];
   if (m0.skip && __ldcg(m0.skip)) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  Ring<NW, NS> R(smem, warp);
+  Ring<NW, NS, SB> R(smem, warp);
   Acc* musm = (Acc*)R.mu;
   if (lane == 0) {
     for (int s = 0; s < NS; s++) mbar_init(&R.bar[s], 1);
@@ -371,22 +382,36 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
     if (it < ntot) d = it < n0 ? m0.s2[it] : m1.s2[it - n0];
     return d;
   };
+  // column indices of a chunk in flight: lane L holds columns L + 32 i
+  struct Pend {
+    int32_t idx[KP];
+    int nc, sec;
+  };
   int p_it = gw, p_c0 = 0, p_seq = 0;
   S2ItemDev Dp = desc(p_it), Dpn = desc(p_it + GW);
-  auto produce = [&]() {
+  auto produce = [&](Pend& pd) {
+    pd.nc = 0;
+    pd.sec = 0;
+#pragma unroll
+    for (int i = 0; i < KP; i++) pd.idx[i] = 0;
     if (p_it >= ntot) return;
-    const int nc = min(chunk_cols_dev(Dp.ntp, ESZ), Dp.ncols - p_c0);
+    const int nc = min(chunk_cols_dev<SB>(Dp.ntp, ESZ), Dp.ncols - p_c0);
     const int s = p_seq % NS;
+    const MatDev& PM = p_it < n0 ? m0 : m1;
     if (lane == 0) {
       const uint32_t bytes = (uint32_t)(nc * Dp.ntp * ESZ);
-      const uint32_t ibytes = (uint32_t)(((nc + 3) / 4) * 16);
-      const MatDev& PM = p_it < n0 ? m0 : m1;
       const T* src = (const T*)PM.ustore + Dp.soff + (int64_t)p_c0 * Dp.ntp;
       fence_proxy_async();
-      mbar_expect_tx(&R.bar[s], bytes + ibytes);
-      bulk_g2s(R.buf + s * kStageAll, src, bytes, &R.bar[s]);
-      bulk_g2s(R.buf + s * kStageAll + kStage, PM.midx + Dp.m0 + p_c0, ibytes, &R.bar[s]);
+      mbar_expect_tx(&R.bar[s], bytes);
+      bulk_g2s(R.buf + s * SB, src, bytes, &R.bar[s]);
     }
+#pragma unroll
+    for (int i = 0; i < KP; i++) {
+      const int k = lane + 32 * i;
+      if (k < nc) pd.idx[i] = __ldg(&PM.midx[Dp.m0 + p_c0 + k]);
+    }
+    pd.nc = nc;
+    pd.sec = p_it >= n0;
     p_seq++;
     p_c0 += nc;
     if (p_c0 >= Dp.ncols) {
@@ -396,7 +421,21 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
       Dpn = desc(p_it + GW);
     }
   };
-  for (int q = 0; q < NS; q++) produce();
+  auto gather = [&](const Pend& pd, Acc* mu) {
+    const Acc* zv = (const Acc*)(pd.sec ? m1.z : m0.z);
+#pragma unroll
+    for (int i = 0; i < KP; i++) {
+      const int k = lane + 32 * i;
+      const int mi = pd.idx[i];
+      mu[i] = k < pd.nc ? (mi >= 0 ? __ldcg(&zv[mi]) : (Acc)__ldg(&x[-mi - 1])) : Acc(0);
+    }
+  };
+  // FIFO of the chunks in flight, oldest first
+  Pend fifo[NS];
+#pragma unroll
+  for (int q = 0; q < NS; q++) produce(fifo[q]);
+  Acc mu[KP];
+  gather(fifo[0], mu);
   int c_it = gw, c_c0 = 0, c_seq = 0;
   S2ItemDev Dc = desc(c_it), Dn = desc(c_it + GW);
   Acc acc[VEC];
@@ -410,16 +449,13 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
       drain<NS>(R.bar, c_seq, p_seq);
       return;
     }
-    const int nc = min(chunk_cols_dev(Dc.ntp, ESZ), Dc.ncols - c_c0);
-    const T* st = (const T*)(R.buf + s * kStageAll);
-    const int32_t* ix = (const int32_t*)(R.buf + s * kStageAll + kStage);
-    // multipliers of the chunk's columns
-    const Acc* zv = (const Acc*)M.z;
-    for (int k = lane; k < nc; k += 32) {
-      const int mi = ix[k];
-      musm[k] = mi >= 0 ? __ldcg(&zv[mi]) : (Acc)__ldg(&x[-mi - 1]);
-    }
+    const int nc = min(chunk_cols_dev<SB>(Dc.ntp, ESZ), Dc.ncols - c_c0);
+    const T* st = (const T*)(R.buf + s * SB);
+    // this chunk's multipliers to shared memory; start the next chunk's gather
+#pragma unroll
+    for (int i = 0; i < KP; i++) musm[lane + 32 * i] = mu[i];
     __syncwarp();
+    gather(fifo[1], mu);
     const int nq = Dc.ntp / VEC;
     const int lw = log2ceil(nq), LW = 1 << lw, CS = 32 >> lw;
     const int slot = lane >> lw, j = lane & (LW - 1);
@@ -444,11 +480,11 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
       for (; r0 < nc; r0 += CS) {
         const int sg = r0 + slot;
         if (sg < nc) {
-          const Acc mu = musm[sg];
+          const Acc m = musm[sg];
           Acc a[VEC];
           lds16(st + sg * Dc.ntp + j * VEC, a);
 #pragma unroll
-          for (int v = 0; v < VEC; v++) acc[v] += a[v] * mu;
+          for (int v = 0; v < VEC; v++) acc[v] += a[v] * m;
         }
       }
 #pragma unroll
@@ -456,7 +492,9 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
     }
     __syncwarp();
     c_seq++;
-    produce();
+#pragma unroll
+    for (int q = 0; q + 1 < NS; q++) fifo[q] = fifo[q + 1];
+    produce(fifo[NS - 1]);
     c_c0 += nc;
     if (c_c0 < Dc.ncols) continue;
     // item done: combine the column slots, write the tile's rows
@@ -500,11 +538,11 @@ __global__ void segcopy_kernel(const double* __restrict__ body, const SegCopyDev
 // ------------------------------------------------------------- launchers
 namespace {
 
-// warps per block and stages per warp (one block per SM); the block's
-// shared memory: NW x NS x 17 KB + multipliers + barriers
-template <int NW, int NS>
+// warps per block, stages per warp and stage bytes (one block per SM); the
+// block's shared memory: NW x NS x SB + multipliers + barriers
+template <int NW, int NS, int SB>
 constexpr size_t smem_bytes() {
-  return (size_t)NW * NS * kStageAll + (size_t)NW * 256 * 8 + (size_t)NW * NS * 8;
+  return (size_t)NW * NS * SB + (size_t)NW * kMu + (size_t)NW * NS * 8;
 }
 
 template <typename K>
@@ -519,32 +557,32 @@ void set_smem_once(K kernel, size_t bytes) {
   if (ndone < 64) done[ndone++] = (const void*)kernel;
 }
 
-// pipeline shape: 6 warps x 2 stages (default; measured fastest on c2 for
-// all three storage types), 4 x 3 or 3 x 4 -- HBI_STREAM_SHAPE = 1, 0, 2
+// pipeline shape, HBI_STREAM_SHAPE: 0 = 12 warps x 2 stages x 8 KB (default),
+// 1 = 6 warps x 2 stages x 16 KB, 2 = 8 warps x 3 stages x 8 KB
 int stream_shape() {
   static int shape = -1;
   if (shape < 0) {
     const char* e = getenv("HBI_STREAM_SHAPE");
-    shape = e ? atoi(e) : 1;
-    if (shape < 0 || shape > 2) shape = 1;
+    shape = e ? atoi(e) : 0;
+    if (shape < 0 || shape > 2) shape = 0;
   }
   return shape;
 }
 
-template <typename T, int NW, int NS>
+template <typename T, int NW, int NS, int SB>
 void launch_p1_shape(const MatDev& m0, const MatDev& m1, int nmat, const double* x, int sm, int n, cudaStream_t st) {
   const int need = (n + NW - 1) / NW;
   const int grid = need < sm ? (need > 0 ? need : 1) : sm;
-  set_smem_once(p1_stream_kernel<T, NW, NS>, smem_bytes<NW, NS>());
-  p1_stream_kernel<T, NW, NS><<<grid, NW * 32, smem_bytes<NW, NS>(), st>>>(m0, m1, nmat, x);
+  set_smem_once(p1_stream_kernel<T, NW, NS, SB>, smem_bytes<NW, NS, SB>());
+  p1_stream_kernel<T, NW, NS, SB><<<grid, NW * 32, smem_bytes<NW, NS, SB>(), st>>>(m0, m1, nmat, x);
 }
 
-template <typename T, int NW, int NS>
+template <typename T, int NW, int NS, int SB>
 void launch_p2_shape(const MatDev& m0, const MatDev& m1, int nmat, const double* x, int sm, int n, cudaStream_t st) {
   const int need = (n + NW - 1) / NW;
   const int grid = need < sm ? (need > 0 ? need : 1) : sm;
-  set_smem_once(p2_stream_kernel<T, NW, NS>, smem_bytes<NW, NS>());
-  p2_stream_kernel<T, NW, NS><<<grid, NW * 32, smem_bytes<NW, NS>(), st>>>(m0, m1, nmat, x);
+  set_smem_once(p2_stream_kernel<T, NW, NS, SB>, smem_bytes<NW, NS, SB>());
+  p2_stream_kernel<T, NW, NS, SB><<<grid, NW * 32, smem_bytes<NW, NS, SB>(), st>>>(m0, m1, nmat, x);
 }
 
 template <typename T>
@@ -552,9 +590,9 @@ void launch_p1(const MatDev& m0, const MatDev& m1, int nmat, const double* x, in
   const int n = m0.ns1 + (nmat == 2 ? m1.ns1 : 0);
   if (n == 0) return;
   switch (stream_shape()) {
-    case 1: launch_p1_shape<T, 6, 2>(m0, m1, nmat, x, sm, n, st); break;
-    case 2: launch_p1_shape<T, 3, 4>(m0, m1, nmat, x, sm, n, st); break;
-    default: launch_p1_shape<T, 4, 3>(m0, m1, nmat, x, sm, n, st);
+    case 1: launch_p1_shape<T, 6, 2, 16384>(m0, m1, nmat, x, sm, n, st); break;
+    case 2: launch_p1_shape<T, 8, 3, 8192>(m0, m1, nmat, x, sm, n, st); break;
+    default: launch_p1_shape<T, 12, 2, 8192>(m0, m1, nmat, x, sm, n, st);
   }
 }
 
@@ -563,20 +601,20 @@ void launch_p2(const MatDev& m0, const MatDev& m1, int nmat, const double* x, in
   const int n = m0.ns2 + (nmat == 2 ? m1.ns2 : 0);
   if (n == 0) return;
   switch (stream_shape()) {
-    case 1: launch_p2_shape<T, 6, 2>(m0, m1, nmat, x, sm, n, st); break;
-    case 2: launch_p2_shape<T, 3, 4>(m0, m1, nmat, x, sm, n, st); break;
-    default: launch_p2_shape<T, 4, 3>(m0, m1, nmat, x, sm, n, st);
+    case 1: launch_p2_shape<T, 6, 2, 16384>(m0, m1, nmat, x, sm, n, st); break;
+    case 2: launch_p2_shape<T, 8, 3, 8192>(m0, m1, nmat, x, sm, n, st); break;
+    default: launch_p2_shape<T, 12, 2, 8192>(m0, m1, nmat, x, sm, n, st);
   }
 }
 
 template <typename T>
 void prepare_type() {
-  set_smem_once(p1_stream_kernel<T, 4, 3>, smem_bytes<4, 3>());
-  set_smem_once(p1_stream_kernel<T, 6, 2>, smem_bytes<6, 2>());
-  set_smem_once(p1_stream_kernel<T, 3, 4>, smem_bytes<3, 4>());
-  set_smem_once(p2_stream_kernel<T, 4, 3>, smem_bytes<4, 3>());
-  set_smem_once(p2_stream_kernel<T, 6, 2>, smem_bytes<6, 2>());
-  set_smem_once(p2_stream_kernel<T, 3, 4>, smem_bytes<3, 4>());
+  set_smem_once(p1_stream_kernel<T, 12, 2, 8192>, smem_bytes<12, 2, 8192>());
+  set_smem_once(p1_stream_kernel<T, 6, 2, 16384>, smem_bytes<6, 2, 16384>());
+  set_smem_once(p1_stream_kernel<T, 8, 3, 8192>, smem_bytes<8, 3, 8192>());
+  set_smem_once(p2_stream_kernel<T, 12, 2, 8192>, smem_bytes<12, 2, 8192>());
+  set_smem_once(p2_stream_kernel<T, 6, 2, 16384>, smem_bytes<6, 2, 16384>());
+  set_smem_once(p2_stream_kernel<T, 8, 3, 8192>, smem_bytes<8, 3, 8192>());
 }
 
 }  // namespace

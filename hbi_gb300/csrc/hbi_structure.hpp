@@ -148,12 +148,12 @@ struct StreamPlan {
   std::vector<SegCopy> vcopy, ucopy; // conversion maps
   int64_t factor_elems = 0;
 };
-// columns of one streamed chunk: as many whole columns as fit in 16 KB, a
-// multiple of 32 (ntp * esz <= 512, so at least 32), and at most 256 (the
-// per-warp multiplier and column-index buffers of the phase-2 kernel)
-inline int chunk_cols(int ntp, int esz) {
-  const int c = (16384 / (ntp * esz)) / 32 * 32;
-  return c < 256 ? c : 256;
+// columns of one streamed chunk in a shared-memory stage of stage_bytes (8 KB
+// or 16 KB): as many whole columns as fit, a multiple of 16 (ntp * esz <= 512,
+// so at least 16), and at most 128 (four phase-2 multipliers per lane)
+inline int chunk_cols(int ntp, int esz, int stage_bytes) {
+  const int c = (stage_bytes / (ntp * esz)) / 16 * 16;
+  return c < 128 ? c : 128;
 }
 // ---- tensor-core plan of the ensemble product ---------------------------
 // Both contractions as D (64 members x N) = A (64 x K) * B^T with B (N x K)

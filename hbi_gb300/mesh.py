@@ -2,6 +2,8 @@
 geometries used for the benchmark configurations.
 
 coordinate2dp    main_LH.f90:1701-1718   (2dvs)
+coordinate2dph   main_LH.f90:1720-1737   (2dph)
+coordinate2dn    main_LH.f90:1739-1750   (2dn / 2dnh, element ends from a geometry file)
 coordinate3ddip  main_LH.f90:1781-1835   (3dph)
 .stl reader      main_LH.f90:357-368, 485-509 (3dnt; 7 lines per facet)
 evcalc           main_LH.f90:1940-1990
@@ -25,6 +27,47 @@ def mesh_2dp(n, ds0):
     xer = i * ds0
     xcol = 0.5 * (xel + xer)
     return xel, xer, xcol, np.full(n, float(ds0))
+
+
+def mesh_2dph(n, ds0, dipangle):
+    """xel, xer, yel, yer, xcol, ycol, ang, ds of a planar 2D fault of n
+    elements of size ds0 dipping `dipangle` degrees from the free surface
+    (y is depth, positive down)."""
+    c = math.cos(dipangle * PI / 180)
+    s = math.sin(dipangle * PI / 180)
+    i = np.arange(1, n + 1, dtype=np.float64)
+    xel, xer = (i - 1) * ds0 * c, i * ds0 * c
+    yel, yer = (i - 1) * ds0 * s, i * ds0 * s
+    return _mesh_2d_from_ends(xel, xer, yel, yer, np.full(n, float(ds0)))
+
+
+def mesh_2dn(xel, xer, yel, yer):
+    """xel, xer, yel, yer, xcol, ycol, ang, ds of a 2D fault given by its
+    element ends (the rows of a 2dn / 2dnh geometry file)."""
+    xel, xer, yel, yer = (np.asarray(a, dtype=np.float64) for a in (xel, xer, yel, yer))
+    ds = np.sqrt((xer - xel) ** 2 + (yer - yel) ** 2)
+    return _mesh_2d_from_ends(xel, xer, yel, yer, ds)
+
+
+def _mesh_2d_from_ends(xel, xer, yel, yer, ds):
+    xcol = 0.5 * (xel + xer)
+    ycol = 0.5 * (yel + yer)
+    ang = np.array([math.atan2(yer[k] - yel[k], xer[k] - xel[k]) for k in range(len(xel))])
+    return xel, xer, yel, yer, xcol, ycol, ang, ds
+
+
+def bent_fault_2d(n, length, depth0, bend_deg, seed=0, rough=0.0):
+    """Element ends of a seeded 2D fault for the 2dn / 2dnh problems: a trace
+    from depth depth0 whose strike angle turns linearly by bend_deg over its
+    length, with optional seeded roughness of relative amplitude `rough`."""
+    rng = np.random.default_rng(seed)
+    ds = length / n
+    turn = np.deg2rad(bend_deg) * np.arange(n) / max(1, n - 1)
+    if rough > 0:
+        turn = turn + rough * np.cumsum(rng.standard_normal(n)) / math.sqrt(n)
+    x = np.concatenate([[0.0], np.cumsum(ds * np.cos(turn))])
+    y = depth0 + np.concatenate([[0.0], np.cumsum(ds * np.sin(turn))])
+    return x[:-1], x[1:], y[:-1], y[1:]
 
 
 def mesh_3ddip(imax, jmax, ds0, dipangle):

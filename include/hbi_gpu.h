@@ -35,6 +35,9 @@ extern "C" {
 #define HBI_3DPH 2 /* 3D rectangles, Okada half space (okada_ij :1065-1145) */
 #define HBI_3DNR 3 /* 3D rectangles, Okada full space                    */
 #define HBI_3DNT 4 /* 3D triangles, TDstressFS full space (matel3dn_ij :802-851) */
+#define HBI_2DPH 5 /* 2D plane strain, half space; also '2dnh' (matel2dph2_ij :92-166) */
+#define HBI_2DN 6  /* 2D plane strain, full space (tensor2d_ij :300-339) */
+#define HBI_3DHT 7 /* 3D triangles, TDstressHS half space (matel3dh_ij :852-898) */
 
 /* factor storage of the matvec operator */
 #define HBI_STORE_F64 0
@@ -44,16 +47,17 @@ extern "C" {
 /* st_HACApK_calc_entry (m_HACApK_calc_entry_ij.f90:7-19): geometry in the
  * global (input) numbering, all arrays of length nd; unused ones may be NULL. */
 typedef struct {
-  int problem;  /* HBI_2DVS .. HBI_3DNT */
+  int problem;  /* HBI_2DVS .. HBI_3DHT */
   int nd;
   char v;       /* 's' shear or 'n' normal traction (st_bemv%v) */
   char md;      /* 's' slip along rake (st_bemv%md); only 's' is supported */
   const double *xcol, *ycol, *zcol;
-  const double *xel, *xer;                      /* 2dvs element ends */
-  const double *ang, *angd, *dsl, *dsd, *rake;  /* okada; rake also for 3dnt (radians) */
+  const double *xel, *xer;                      /* 2dvs, 2dph, 2dn element ends */
+  const double *ang, *angd, *dsl, *dsd, *rake;  /* okada; ang also 2D; rake also triangles (radians) */
   double w;                                     /* okada length scale (ds0) */
   const double *xs1, *xs2, *xs3, *ys1, *ys2, *ys3, *zs1, *zs2, *zs3; /* triangles */
   const double *ev11, *ev12, *ev13, *ev21, *ev22, *ev23, *ev31, *ev32, *ev33;
+  const double *yel, *yer;                      /* 2dph / 2dn element ends (with xel, xer) */
 } hbi_bemv;
 
 typedef struct hbi_ctl_s hbi_ctl;           /* st_HACApK_lcontrol */

@@ -33,6 +33,9 @@ extern "C" {
 #define ORC_3DPH 2
 #define ORC_3DNR 3
 #define ORC_3DNT 4
+#define ORC_2DPH 5 /* also 2dnh: matel2dph2_ij */
+#define ORC_2DN 6  /* tensor2d_ij */
+#define ORC_3DHT 7 /* matel3dh_ij */
 
 /* Geometry / kernel selector, the restatement of st_HACApK_calc_entry
  * (m_HACApK_calc_entry_ij.f90:7-19).  All arrays have length n (global order). */
@@ -47,6 +50,7 @@ typedef struct {
   double w;                                    /* okada normalisation ds0 */
   const double *xs1, *xs2, *xs3, *ys1, *ys2, *ys3, *zs1, *zs2, *zs3; /* TD */
   const double *ev11, *ev12, *ev13, *ev21, *ev22, *ev23, *ev31, *ev32, *ev33;
+  const double *yel, *yer;                     /* 2dph / 2dn element ends (with xel, xer) */
 } orc_bemv;
 
 /* Leaf record (st_HACApK_leafmtx, m_HACApK_base.f90:57-72). 1-based starts. */
@@ -71,6 +75,10 @@ void orc_okada(double alpha, double x, double y, double z, double depth, double 
                double al1, double al2, double aw1, double aw2, double disl1,
                double disl2, double disl3, double* u12, int fullspace);
 void orc_tdstressfs(double X, double Y, double Z, const double* P1, const double* P2,
+                    const double* P3, double Ss, double Ds, double Ts, double mu,
+                    double lambda, double* S6);
+/* TDstressHS (TDstressFS.f90:7-44), half space z <= 0 */
+void orc_tdstresshs(double X, double Y, double Z, const double* P1, const double* P2,
                     const double* P3, double Ss, double Ds, double Ts, double mu,
                     double lambda, double* S6);
 

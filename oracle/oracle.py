@@ -16,7 +16,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = os.path.join(_HERE, "_build", "liborc.so")
 
-ORC_2DVS, ORC_3DPH, ORC_3DNR, ORC_3DNT = 1, 2, 3, 4
+ORC_2DVS, ORC_3DPH, ORC_3DNR, ORC_3DNT, ORC_2DPH, ORC_2DN, ORC_3DHT = 1, 2, 3, 4, 5, 6, 7
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 
@@ -33,7 +33,7 @@ class Bemv(C.Structure):
                 + [("w", C.c_double)]
                 + [(f, _dp) for f in ("xs1", "xs2", "xs3", "ys1", "ys2", "ys3", "zs1", "zs2",
                                       "zs3", "ev11", "ev12", "ev13", "ev21", "ev22", "ev23",
-                                      "ev31", "ev32", "ev33")])
+                                      "ev31", "ev32", "ev33", "yel", "yer")])
 
 
 class Rsf(C.Structure):
@@ -222,6 +222,14 @@ def tdstressfs(X, Y, Z, P1, P2, P3, Ss, Ds, Ts, mu, lam):
     s = np.zeros(6)
     P = [np.ascontiguousarray(p, dtype=np.float64) for p in (P1, P2, P3)]
     lib().orc_tdstressfs(C.c_double(X), C.c_double(Y), C.c_double(Z), _p(P[0]), _p(P[1]), _p(P[2]),
+                         C.c_double(Ss), C.c_double(Ds), C.c_double(Ts), C.c_double(mu), C.c_double(lam), _p(s))
+    return s
+
+
+def tdstresshs(X, Y, Z, P1, P2, P3, Ss, Ds, Ts, mu, lam):
+    s = np.zeros(6)
+    P = [np.ascontiguousarray(p, dtype=np.float64) for p in (P1, P2, P3)]
+    lib().orc_tdstresshs(C.c_double(X), C.c_double(Y), C.c_double(Z), _p(P[0]), _p(P[1]), _p(P[2]),
                          C.c_double(Ss), C.c_double(Ds), C.c_double(Ts), C.c_double(mu), C.c_double(lam), _p(s))
     return s
 

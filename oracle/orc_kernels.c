@@ -531,6 +531,491 @@ static double matel3dn_ij(int i, int j, const orc_bemv* b) {
   return p[4] * cos(b->rake[i]) + p[5] * sin(b->rake[i]);
 }
 
+/* ---------------- half space: free-surface correction -------------------- */
+/* Strain (v11, v22, v33, v12, v13, v23) of the harmonic (free-surface
+ * correction) part of an angular dislocation of angle beta whose vertex is at
+ * depth a, at (y1, y2, y3) in its own frame, for Burgers vector (b1, b2, b3)
+ * (AngDisStrainFSC, TDstressFS.f90:629-1011; Nikkhoo & Walter 2015, after
+ * Comninou & Dundurs 1975).  The published expressions are kept term by term;
+ * the factors that recur across components are named once (R*, Q*). */
+static void ang_dis_strain_fsc(double y1, double y2, double y3, double beta, double b1, double b2,
+                               double b3, double nu, double a, double v[6]) {
+  const double sB = sin(beta), cB = cos(beta), ctB = cB / sB;
+  const double y3b = y3 + 2 * a;
+  const double z1b = y1 * cB + y3b * sB;
+  const double z3b = -y1 * sB + y3b * cB;
+  const double rb2 = y1 * y1 + y2 * y2 + y3b * y3b;
+  const double rb = sqrt(rb2);
+  const double W1 = rb * cB + y3b, W2 = cB + a / rb, W3 = cB + y3b / rb, W4 = nu + a / rb;
+  const double W5 = 2 * nu + a / rb, W6 = rb + y3b, W7 = rb + z3b, W8 = y3 + a, W9 = 1 + a / rb / cB;
+  const double N1 = 1 - 2 * nu, nu2 = 2 - 2 * nu;
+  /* derivatives of the Burgers function */
+  const double F2 = z1b / rb / (rb + z3b) - y1 / rb / (rb + y3b);
+  const double F1 = y2 / rb / (rb + y3b) - cB * y2 / rb / (rb + z3b);
+  const double F3 = -sB * y2 / rb / (rb + z3b);
+  const double rb3 = rb * rb * rb, rb4 = rb2 * rb2, rb5 = rb * rb * rb * rb * rb;
+  const double W6s = W6 * W6, W7s = W7 * W7, ct2 = ctB * ctB, cB2 = cB * cB;
+  const double y1s = y1 * y1, y2s = y2 * y2, y1c = y1 * y1 * y1, y2c = y2 * y2 * y2;
+  const double Ys = y1 / rb - sB, Y3 = y3b / rb + 1, C3 = cB * y3b / rb + 1;
+  const double Q1 = W1 * (N1 * cB - a / rb) * ctB + nu2 * (rb * sB - y1) * cB;
+  const double Q2 = cB / W7 * Q1 - a * y3b * cB * ctB / rb2;
+  const double R1 = -N1 * ctB + y1 / W6 * W5 + a * y1 / rb2;
+  const double R2 = N1 * ctB - 2 * nu * y1 / W6 - a * y1 / rb * (1 / rb + 1 / W6);
+  const double R3 = (-2 + 2 * nu) * cB + W1 / W7 * W9 + a * y3b / rb2 / cB;
+  const double R5 = nu2 * cB - W1 / W7 * W9;
+  const double R4 = -cB * sB + a * y1 * y3b / rb3 / cB + (rb * sB - y1) / rb * R5;
+  const double R7 = y2s * cB2 - a * z1b * ctB / rb * W1;
+  const double R6 = cB2 - 1 / rb * (N1 * z1b * ctB + a * cB) + a * y3b * z1b * ctB / rb3 - 1 / rb / W7 * R7;
+  const double R9 = y2s * cB * sB - a * z1b / rb * W1;
+  const double R8 = sB * (cB - a / rb) + z1b / rb * (1 + a * y3b / rb2) - 1 / rb / W7 * R9;
+  const double R10 = W1 / W7 * W2 + a * y3b / rb2;
+  const double R11 = a / rb2 + 1 / W6;
+  const double R12 = 2 * nu + 1 / rb * (N1 * y1 * ctB + a) - y1s / rb / W6 * W5 - a * y1s / rb3;
+  const double R13 = -2 * nu + 1 / rb * (N1 * y1 * ctB - a) + y2s / rb / W6 * W5 + a * y2s / rb3;
+  const double R14 = 1 - 2 * nu - W1 / W7 * W2 - a * y3b / rb2;
+  const double R15a = nu2 * cB - W1 / W7;
+  const double R15b = sB - y3b * z1b / rb2 - z1b * W1 / rb / W7;
+  const double R15 = cB * sB + W1 * ctB / rb * R15a + a / rb * R15b;
+  const double R16 = 1 + W1 / W7 * W2 + a * y3b / rb2;
+  const double R17 = 2 * nu / W6 + a / rb2;
+  const double R18 = z1b * cB - a * (rb * sB - y1) / rb / cB;
+  const double R19 = -N1 * y1 * ctB + nu * y3b - a + a * y1 * ctB / rb + y1s / W6 * W4;
+  const double R20 = y1 * ctB * (1 - W5) + nu * y3b - a + y2s / W6 * W4;
+  const double R21 = (1 - W5) * ctB - y1 / W6 * W4;
+  const double R22 = (W5 - 1) * ctB + y1 / W6 * W4;
+  const double R23 = N1 * ctB - 2 * nu * y1 / W6 - a * y1 / rb2;
+
+  /* ---- v11 ---- */
+  const double T11_1 = (-2 + 2 * nu) * N1 * F1 * ct2 - N1 * y2 / W6s * R21 / rb * y1 +
+      N1 * y2 / W6 * (a / rb3 * y1 * ctB - 1 / W6 * W4 + y1s / W6s * W4 / rb + y1s / W6 * a / rb3) -
+      N1 * y2 * cB * ctB / W7s * W2 * Ys - N1 * y2 * cB * ctB / W7 * a / rb3 * y1 -
+      3 * a * y2 * W8 * ctB / rb5 * y1 - y2 * W8 / rb3 / W6 * R1 * y1 - y2 * W8 / rb2 / W6s * R1 * y1 +
+      y2 * W8 / rb / W6 * (1 / W6 * W5 - y1s / W6s * W5 / rb - y1s / W6 * a / rb3 + a / rb2 - 2 * a * y1s / rb4) -
+      y2 * W8 / rb3 / W7 * Q2 * y1 - y2 * W8 / rb / W7s * Q2 * Ys +
+      y2 * W8 / rb / W7 *
+          (-cB / W7s * Q1 * Ys +
+           cB / W7 * (1 / rb * cB * y1 * (N1 * cB - a / rb) * ctB + W1 * a / rb3 * y1 * ctB + nu2 * (1 / rb * sB * y1 - 1) * cB) +
+           2 * a * y3b * cB * ctB / rb4 * y1);
+  const double T11_2 = N1 * ((nu2 * ct2 + nu) / rb * y1 / W6 - (nu2 * ct2 + 1) * cB * Ys / W7) -
+      N1 / W6s * R19 / rb * y1 +
+      N1 / W6 * (-N1 * ctB + a * ctB / rb - a * y1s * ctB / rb3 + 2 * y1 / W6 * W4 - y1c / W6s * W4 / rb - y1c / W6 * a / rb3) +
+      N1 * ctB / W7s * R18 * Ys -
+      N1 * ctB / W7 * (cB2 - a * (1 / rb * sB * y1 - 1) / rb / cB + a * (rb * sB - y1) / rb3 / cB * y1) -
+      a * W8 * ctB / rb3 + 3 * a * y1s * W8 * ctB / rb5 - W8 / W6s * R12 / rb * y1 +
+      W8 / W6 * (-1 / rb3 * (N1 * y1 * ctB + a) * y1 + 1 / rb * N1 * ctB - 2 * y1 / rb / W6 * W5 + y1c / rb3 / W6 * W5 +
+                 y1c / rb2 / W6s * W5 + y1c / rb4 / W6 * a - 2 * a / rb3 * y1 + 3 * a * y1c / rb5) -
+      W8 * ctB / W7s * R4 * Ys +
+      W8 * ctB / W7 *
+          (a * y3b / rb3 / cB - 3 * a * y1s * y3b / rb5 / cB + (1 / rb * sB * y1 - 1) / rb * R5 - (rb * sB - y1) / rb3 * R5 * y1 +
+           (rb * sB - y1) / rb * (-1 / rb * cB * y1 / W7 * W9 + W1 / W7s * W9 * Ys + W1 / W7 * a / rb3 / cB * y1));
+  const double T11_3 =
+      N1 * (-y2 / W6s * (1 + a / rb) / rb * y1 - y2 / W6 * a / rb3 * y1 + y2 * cB / W7s * W2 * Ys + y2 * cB / W7 * a / rb3 * y1) +
+      y2 * W8 / rb3 * R11 * y1 - y2 * W8 / rb * (-2 * a / rb4 * y1 - 1 / W6s / rb * y1) -
+      y2 * W8 * cB / rb3 / W7 * R10 * y1 - y2 * W8 * cB / rb / W7s * R10 * Ys +
+      y2 * W8 * cB / rb / W7 * (1 / rb * cB * y1 / W7 * W2 - W1 / W7s * W2 * Ys - W1 / W7 * a / rb3 * y1 - 2 * a * y3b / rb4 * y1);
+
+  /* ---- v22 ---- */
+  const double T22_1 = N1 * ((nu2 * ct2 - nu) / rb * y2 / W6 - (nu2 * ct2 + 1 - 2 * nu) * cB / rb * y2 / W7) +
+      N1 / W6s * R20 / rb * y2 -
+      N1 / W6 * (a * y1 * ctB / rb3 * y2 + 2 * y2 / W6 * W4 - y2c / W6s * W4 / rb - y2c / W6 * a / rb3) +
+      N1 * z1b * ctB / W7s * W2 / rb * y2 + N1 * z1b * ctB / W7 * a / rb3 * y2 + 3 * a * y2 * W8 * ctB / rb5 * y1 -
+      W8 / W6s * R13 / rb * y2 +
+      W8 / W6 * (-1 / rb3 * (N1 * y1 * ctB - a) * y2 + 2 * y2 / rb / W6 * W5 - y2c / rb3 / W6 * W5 - y2c / rb2 / W6s * W5 -
+                 y2c / rb4 / W6 * a + 2 * a / rb3 * y2 - 3 * a * y2c / rb5) -
+      W8 / W7s * R6 / rb * y2 +
+      W8 / W7 *
+          (1 / rb3 * (N1 * z1b * ctB + a * cB) * y2 - 3 * a * y3b * z1b * ctB / rb5 * y2 + 1 / rb3 / W7 * R7 * y2 +
+           1 / rb2 / W7s * R7 * y2 - 1 / rb / W7 * (2 * y2 * cB2 + a * z1b * ctB / rb3 * W1 * y2 - a * z1b * ctB / rb2 * cB * y2));
+  const double T22_2 = nu2 * N1 * F2 * ct2 + N1 / W6 * R22 - N1 * y2s / W6s * R22 / rb +
+      N1 * y2 / W6 * (-a / rb3 * y2 * ctB - y1 / W6s * W4 / rb * y2 - y2 / W6 * a / rb3 * y1) - N1 * ctB / W7 * W9 +
+      N1 * y2s * ctB / W7s * W9 / rb + N1 * y2s * ctB / W7 * a / rb3 / cB - a * W8 * ctB / rb3 +
+      3 * a * y2s * W8 * ctB / rb5 + W8 / rb / W6 * R2 - y2s * W8 / rb3 / W6 * R2 - y2s * W8 / rb2 / W6s * R2 +
+      y2 * W8 / rb / W6 *
+          (2 * nu * y1 / W6s / rb * y2 + a * y1 / rb3 * (1 / rb + 1 / W6) * y2 - a * y1 / rb * (-1 / rb3 * y2 - 1 / W6s / rb * y2)) +
+      W8 * ctB / rb / W7 * R3 - y2s * W8 * ctB / rb3 / W7 * R3 - y2s * W8 * ctB / rb2 / W7s * R3 +
+      y2 * W8 * ctB / rb / W7 *
+          (1 / rb * cB * y2 / W7 * W9 - W1 / W7s * W9 / rb * y2 - W1 / W7 * a / rb3 / cB * y2 - 2 * a * y3b / rb4 / cB * y2);
+  const double T22_3 = N1 * (-sB / rb * y2 / W7 + y2 / W6s * (1 + a / rb) / rb * y1 + y2 / W6 * a / rb3 * y1 -
+                             z1b / W7s * W2 / rb * y2 - z1b / W7 * a / rb3 * y2) -
+      y2 * W8 / rb3 * R11 * y1 + y1 * W8 / rb * (-2 * a / rb4 * y2 - 1 / W6s / rb * y2) + W8 / W7s * R8 / rb * y2 -
+      W8 / W7 *
+          (sB * a / rb3 * y2 - z1b / rb3 * (1 + a * y3b / rb2) * y2 - 2 * z1b / rb5 * a * y3b * y2 + 1 / rb3 / W7 * R9 * y2 +
+           1 / rb2 / W7s * R9 * y2 - 1 / rb / W7 * (2 * y2 * cB * sB + a * z1b / rb3 * W1 * y2 - a * z1b / rb2 * cB * y2));
+
+  /* ---- v33 ---- */
+  const double T33_1 = nu2 * (N1 * F3 * ctB - y2 / W6s * W5 * Y3 - 0.5 * y2 / W6 * a / rb3 * 2 * y3b +
+                              y2 * cB / W7s * W2 * W3 + 0.5 * y2 * cB / W7 * a / rb3 * 2 * y3b) +
+      y2 / rb * R17 - 0.5 * y2 * W8 / rb3 * R17 * 2 * y3b + y2 * W8 / rb * (-2 * nu / W6s * Y3 - a / rb4 * 2 * y3b) +
+      y2 * cB / rb / W7 * R14 - 0.5 * y2 * W8 * cB / rb3 / W7 * R14 * 2 * y3b - y2 * W8 * cB / rb / W7s * R14 * W3 +
+      y2 * W8 * cB / rb / W7 *
+          (-C3 / W7 * W2 + W1 / W7s * W2 * W3 + 0.5 * W1 / W7 * a / rb3 * 2 * y3b - a / rb2 + a * y3b / rb4 * 2 * y3b);
+  const double T33_2 = (-2 + 2 * nu) * N1 * ctB * (Y3 / W6 - cB * W3 / W7) + nu2 * y1 / W6s * W5 * Y3 +
+      0.5 * nu2 * y1 / W6 * a / rb3 * 2 * y3b + nu2 * sB / W7 * W2 - nu2 * z1b / W7s * W2 * W3 -
+      0.5 * nu2 * z1b / W7 * a / rb3 * 2 * y3b + 1 / rb * R23 - 0.5 * W8 / rb3 * R23 * 2 * y3b +
+      W8 / rb * (2 * nu * y1 / W6s * Y3 + a * y1 / rb4 * 2 * y3b) - 1 / W7 * R15 + W8 / W7s * R15 * W3 -
+      W8 / W7 *
+          (C3 * ctB / rb * R15a - 0.5 * W1 * ctB / rb3 * R15a * 2 * y3b + W1 * ctB / rb * (-C3 / W7 + W1 / W7s * W3) -
+           0.5 * a / rb3 * R15b * 2 * y3b +
+           a / rb * (-z1b / rb2 - y3b * sB / rb2 + y3b * z1b / rb4 * 2 * y3b - sB * W1 / rb / W7 - z1b * C3 / rb / W7 +
+                     0.5 * z1b * W1 / rb3 / W7 * 2 * y3b + z1b * W1 / rb / W7s * W3));
+  const double T33_3 = nu2 * F3 - nu2 * y2 * sB / W7s * W2 * W3 - 0.5 * nu2 * y2 * sB / W7 * a / rb3 * 2 * y3b +
+      y2 * sB / rb / W7 * R16 - 0.5 * y2 * W8 * sB / rb3 / W7 * R16 * 2 * y3b - y2 * W8 * sB / rb / W7s * R16 * W3 +
+      y2 * W8 * sB / rb / W7 *
+          (C3 / W7 * W2 - W1 / W7s * W2 * W3 - 0.5 * W1 / W7 * a / rb3 * 2 * y3b + a / rb2 - a * y3b / rb4 * 2 * y3b);
+
+  /* ---- v12 ---- */
+  const double T12_A = (-2 + 2 * nu) * N1 * F2 * ct2 + N1 / W6 * R21 - N1 * y2s / W6s * R21 / rb +
+      N1 * y2 / W6 * (a / rb3 * y2 * ctB + y1 / W6s * W4 / rb * y2 + y2 / W6 * a / rb3 * y1) + N1 * cB * ctB / W7 * W2 -
+      N1 * y2s * cB * ctB / W7s * W2 / rb - N1 * y2s * cB * ctB / W7 * a / rb3 + a * W8 * ctB / rb3 -
+      3 * a * y2s * W8 * ctB / rb5 + W8 / rb / W6 * R1 - y2s * W8 / rb3 / W6 * R1 - y2s * W8 / rb2 / W6s * R1 +
+      y2 * W8 / rb / W6 * (-y1 / W6s * W5 / rb * y2 - y2 / W6 * a / rb3 * y1 - 2 * a * y1 / rb4 * y2) +
+      W8 / rb / W7 * Q2 - y2s * W8 / rb3 / W7 * Q2 - y2s * W8 / rb2 / W7s * Q2 +
+      y2 * W8 / rb / W7 *
+          (-cB / W7s * Q1 / rb * y2 +
+           cB / W7 * (1 / rb * cB * y2 * (N1 * cB - a / rb) * ctB + W1 * a / rb3 * y2 * ctB + nu2 / rb * sB * y2 * cB) +
+           2 * a * y3b * cB * ctB / rb4 * y2);
+  const double T12_B = N1 * ((nu2 * ct2 + nu) / rb * y2 / W6 - (nu2 * ct2 + 1) * cB / rb * y2 / W7) -
+      N1 / W6s * R19 / rb * y2 +
+      N1 / W6 * (-a * y1 * ctB / rb3 * y2 - y1s / W6s * W4 / rb * y2 - y1s / W6 * a / rb3 * y2) +
+      N1 * ctB / W7s * R18 / rb * y2 - N1 * ctB / W7 * (-a / rb2 * sB * y2 / cB + a * (rb * sB - y1) / rb3 / cB * y2) +
+      3 * a * y2 * W8 * ctB / rb5 * y1 - W8 / W6s * R12 / rb * y2 +
+      W8 / W6 * (-1 / rb3 * (N1 * y1 * ctB + a) * y2 + y1s / rb3 / W6 * W5 * y2 + y1s / rb2 / W6s * W5 * y2 +
+                 y1s / rb4 / W6 * a * y2 + 3 * a * y1s / rb5 * y2) -
+      W8 * ctB / W7s * R4 / rb * y2 +
+      W8 * ctB / W7 *
+          (-3 * a * y1 * y3b / rb5 / cB * y2 + 1 / rb2 * sB * y2 * R5 - (rb * sB - y1) / rb3 * R5 * y2 +
+           (rb * sB - y1) / rb * (-1 / rb * cB * y2 / W7 * W9 + W1 / W7s * W9 / rb * y2 + W1 / W7 * a / rb3 / cB * y2));
+  const double T12_C = N1 * (1 / W6 * (1 + a / rb) - y2s / W6s * (1 + a / rb) / rb - y2s / W6 * a / rb3 - cB / W7 * W2 +
+                             y2s * cB / W7s * W2 / rb + y2s * cB / W7 * a / rb3) -
+      W8 / rb * R11 + y2s * W8 / rb3 * R11 - y2 * W8 / rb * (-2 * a / rb4 * y2 - 1 / W6s / rb * y2) +
+      W8 * cB / rb / W7 * R10 - y2s * W8 * cB / rb3 / W7 * R10 - y2s * W8 * cB / rb2 / W7s * R10 +
+      y2 * W8 * cB / rb / W7 * (1 / rb * cB * y2 / W7 * W2 - W1 / W7s * W2 / rb * y2 - W1 / W7 * a / rb3 * y2 - 2 * a * y3b / rb4 * y2);
+  const double T12_D = N1 * ((nu2 * ct2 - nu) / rb * y1 / W6 - (nu2 * ct2 + 1 - 2 * nu) * cB * Ys / W7) +
+      N1 / W6s * R20 / rb * y1 -
+      N1 / W6 * ((1 - W5) * ctB + a * y1s * ctB / rb3 - y2s / W6s * W4 / rb * y1 - y2s / W6 * a / rb3 * y1) -
+      N1 * cB * ctB / W7 * W2 + N1 * z1b * ctB / W7s * W2 * Ys + N1 * z1b * ctB / W7 * a / rb3 * y1 - a * W8 * ctB / rb3 +
+      3 * a * y1s * W8 * ctB / rb5 - W8 / W6s * R13 / rb * y1 +
+      W8 / W6 * (-1 / rb3 * (N1 * y1 * ctB - a) * y1 + 1 / rb * N1 * ctB - y2s / rb3 / W6 * W5 * y1 -
+                 y2s / rb2 / W6s * W5 * y1 - y2s / rb4 / W6 * a * y1 - 3 * a * y2s / rb5 * y1) -
+      W8 / W7s * R6 * Ys +
+      W8 / W7 *
+          (1 / rb3 * (N1 * z1b * ctB + a * cB) * y1 - 1 / rb * N1 * cB * ctB + a * y3b * cB * ctB / rb3 -
+           3 * a * y3b * z1b * ctB / rb5 * y1 + 1 / rb3 / W7 * R7 * y1 + 1 / rb / W7s * R7 * Ys -
+           1 / rb / W7 * (-a * cB * ctB / rb * W1 + a * z1b * ctB / rb3 * W1 * y1 - a * z1b * ctB / rb2 * cB * y1));
+  const double T12_E = nu2 * N1 * F1 * ct2 - N1 * y2 / W6s * R22 / rb * y1 +
+      N1 * y2 / W6 * (-a / rb3 * y1 * ctB + 1 / W6 * W4 - y1s / W6s * W4 / rb - y1s / W6 * a / rb3) +
+      N1 * y2 * ctB / W7s * W9 * Ys + N1 * y2 * ctB / W7 * a / rb3 / cB * y1 + 3 * a * y2 * W8 * ctB / rb5 * y1 -
+      y2 * W8 / rb3 / W6 * R2 * y1 - y2 * W8 / rb2 / W6s * R2 * y1 +
+      y2 * W8 / rb / W6 *
+          (-2 * nu / W6 + 2 * nu * y1s / W6s / rb - a / rb * (1 / rb + 1 / W6) + a * y1s / rb3 * (1 / rb + 1 / W6) -
+           a * y1 / rb * (-1 / rb3 * y1 - 1 / W6s / rb * y1)) -
+      y2 * W8 * ctB / rb3 / W7 * R3 * y1 - y2 * W8 * ctB / rb / W7s * R3 * Ys +
+      y2 * W8 * ctB / rb / W7 *
+          (1 / rb * cB * y1 / W7 * W9 - W1 / W7s * W9 * Ys - W1 / W7 * a / rb3 / cB * y1 - 2 * a * y3b / rb4 / cB * y1);
+  const double T12_F = N1 * (-sB * Ys / W7 - 1 / W6 * (1 + a / rb) + y1s / W6s * (1 + a / rb) / rb + y1s / W6 * a / rb3 +
+                             cB / W7 * W2 - z1b / W7s * W2 * Ys - z1b / W7 * a / rb3 * y1) +
+      W8 / rb * R11 - y1s * W8 / rb3 * R11 + y1 * W8 / rb * (-2 * a / rb4 * y1 - 1 / W6s / rb * y1) + W8 / W7s * R8 * Ys -
+      W8 / W7 *
+          (sB * a / rb3 * y1 + cB / rb * (1 + a * y3b / rb2) - z1b / rb3 * (1 + a * y3b / rb2) * y1 -
+           2 * z1b / rb5 * a * y3b * y1 + 1 / rb3 / W7 * R9 * y1 + 1 / rb / W7s * R9 * Ys -
+           1 / rb / W7 * (-a * cB / rb * W1 + a * z1b / rb3 * W1 * y1 - a * z1b / rb2 * cB * y1));
+
+  /* ---- v13 ---- */
+  const double T13_A = (-2 + 2 * nu) * N1 * F3 * ct2 - N1 * y2 / W6s * R21 * Y3 +
+      N1 * y2 / W6 * (0.5 * a / rb3 * 2 * y3b * ctB + y1 / W6s * W4 * Y3 + 0.5 * y1 / W6 * a / rb3 * 2 * y3b) -
+      N1 * y2 * cB * ctB / W7s * W2 * W3 - 0.5 * N1 * y2 * cB * ctB / W7 * a / rb3 * 2 * y3b + a / rb3 * y2 * ctB -
+      1.5 * a * y2 * W8 * ctB / rb5 * 2 * y3b + y2 / rb / W6 * R1 - 0.5 * y2 * W8 / rb3 / W6 * R1 * 2 * y3b -
+      y2 * W8 / rb / W6s * R1 * Y3 +
+      y2 * W8 / rb / W6 * (-y1 / W6s * W5 * Y3 - 0.5 * y1 / W6 * a / rb3 * 2 * y3b - a * y1 / rb4 * 2 * y3b) +
+      y2 / rb / W7 * Q2 - 0.5 * y2 * W8 / rb3 / W7 * Q2 * 2 * y3b - y2 * W8 / rb / W7s * Q2 * W3 +
+      y2 * W8 / rb / W7 *
+          (-cB / W7s * Q1 * W3 +
+           cB / W7 * (C3 * (N1 * cB - a / rb) * ctB + 0.5 * W1 * a / rb3 * 2 * y3b * ctB + 0.5 * nu2 / rb * sB * 2 * y3b * cB) -
+           a * cB * ctB / rb2 + a * y3b * cB * ctB / rb4 * 2 * y3b);
+  const double T13_B = N1 * ((nu2 * ct2 + nu) * Y3 / W6 - (nu2 * ct2 + 1) * cB * W3 / W7) - N1 / W6s * R19 * Y3 +
+      N1 / W6 * (nu - 0.5 * a * y1 * ctB / rb3 * 2 * y3b - y1s / W6s * W4 * Y3 - 0.5 * y1s / W6 * a / rb3 * 2 * y3b) +
+      N1 * ctB / W7s * R18 * W3 -
+      N1 * ctB / W7 * (cB * sB - 0.5 * a / rb2 * sB * 2 * y3b / cB + 0.5 * a * (rb * sB - y1) / rb3 / cB * 2 * y3b) -
+      a / rb3 * y1 * ctB + 1.5 * a * y1 * W8 * ctB / rb5 * 2 * y3b + 1 / W6 * R12 - W8 / W6s * R12 * Y3 +
+      W8 / W6 * (-0.5 / rb3 * (N1 * y1 * ctB + a) * 2 * y3b + 0.5 * y1s / rb3 / W6 * W5 * 2 * y3b + y1s / rb / W6s * W5 * Y3 +
+                 0.5 * y1s / rb4 / W6 * a * 2 * y3b + 1.5 * a * y1s / rb5 * 2 * y3b) +
+      ctB / W7 * R4 - W8 * ctB / W7s * R4 * W3 +
+      W8 * ctB / W7 *
+          (a / rb3 / cB * y1 - 1.5 * a * y1 * y3b / rb5 / cB * 2 * y3b + 0.5 / rb2 * sB * 2 * y3b * R5 -
+           0.5 * (rb * sB - y1) / rb3 * R5 * 2 * y3b +
+           (rb * sB - y1) / rb * (-C3 / W7 * W9 + W1 / W7s * W9 * W3 + 0.5 * W1 / W7 * a / rb3 / cB * 2 * y3b));
+  const double T13_C = N1 * (-y2 / W6s * (1 + a / rb) * Y3 - 0.5 * y2 / W6 * a / rb3 * 2 * y3b + y2 * cB / W7s * W2 * W3 +
+                             0.5 * y2 * cB / W7 * a / rb3 * 2 * y3b) -
+      y2 / rb * R11 + 0.5 * y2 * W8 / rb3 * R11 * 2 * y3b - y2 * W8 / rb * (-a / rb4 * 2 * y3b - 1 / W6s * Y3) +
+      y2 * cB / rb / W7 * R10 - 0.5 * y2 * W8 * cB / rb3 / W7 * R10 * 2 * y3b - y2 * W8 * cB / rb / W7s * R10 * W3 +
+      y2 * W8 * cB / rb / W7 *
+          (C3 / W7 * W2 - W1 / W7s * W2 * W3 - 0.5 * W1 / W7 * a / rb3 * 2 * y3b + a / rb2 - a * y3b / rb4 * 2 * y3b);
+  const double T13_D = nu2 * (N1 * F1 * ctB - y1 / W6s * W5 / rb * y2 - y2 / W6 * a / rb3 * y1 + y2 * cB / W7s * W2 * Ys +
+                              y2 * cB / W7 * a / rb3 * y1) -
+      y2 * W8 / rb3 * R17 * y1 + y2 * W8 / rb * (-2 * nu / W6s / rb * y1 - 2 * a / rb4 * y1) -
+      y2 * W8 * cB / rb3 / W7 * R14 * y1 - y2 * W8 * cB / rb / W7s * R14 * Ys +
+      y2 * W8 * cB / rb / W7 * (-1 / rb * cB * y1 / W7 * W2 + W1 / W7s * W2 * Ys + W1 / W7 * a / rb3 * y1 + 2 * a * y3b / rb4 * y1);
+  const double T13_E = (-2 + 2 * nu) * N1 * ctB * (1 / rb * y1 / W6 - cB * Ys / W7) - nu2 / W6 * W5 +
+      nu2 * y1s / W6s * W5 / rb + nu2 * y1s / W6 * a / rb3 + nu2 * cB / W7 * W2 - nu2 * z1b / W7s * W2 * Ys -
+      nu2 * z1b / W7 * a / rb3 * y1 - W8 / rb3 * R23 * y1 +
+      W8 / rb * (-2 * nu / W6 + 2 * nu * y1s / W6s / rb - a / rb2 + 2 * a * y1s / rb4) + W8 / W7s * R15 * Ys -
+      W8 / W7 *
+          (1 / rb2 * cB * y1 * ctB * R15a - W1 * ctB / rb3 * R15a * y1 + W1 * ctB / rb * (-1 / rb * cB * y1 / W7 + W1 / W7s * Ys) -
+           a / rb3 * R15b * y1 +
+           a / rb * (-y3b * cB / rb2 + 2 * y3b * z1b / rb4 * y1 - cB * W1 / rb / W7 - z1b / rb2 * cB * y1 / W7 +
+                     z1b * W1 / rb3 / W7 * y1 + z1b * W1 / rb / W7s * Ys));
+  const double T13_F = nu2 * F1 - nu2 * y2 * sB / W7s * W2 * Ys - nu2 * y2 * sB / W7 * a / rb3 * y1 -
+      y2 * W8 * sB / rb3 / W7 * R16 * y1 - y2 * W8 * sB / rb / W7s * R16 * Ys +
+      y2 * W8 * sB / rb / W7 * (1 / rb * cB * y1 / W7 * W2 - W1 / W7s * W2 * Ys - W1 / W7 * a / rb3 * y1 - 2 * a * y3b / rb4 * y1);
+
+  /* ---- v23 ---- */
+  const double T23_A = N1 * ((nu2 * ct2 - nu) * Y3 / W6 - (nu2 * ct2 + 1 - 2 * nu) * cB * W3 / W7) + N1 / W6s * R20 * Y3 -
+      N1 / W6 * (0.5 * a * y1 * ctB / rb3 * 2 * y3b + nu - y2s / W6s * W4 * Y3 - 0.5 * y2s / W6 * a / rb3 * 2 * y3b) -
+      N1 * sB * ctB / W7 * W2 + N1 * z1b * ctB / W7s * W2 * W3 + 0.5 * N1 * z1b * ctB / W7 * a / rb3 * 2 * y3b -
+      a / rb3 * y1 * ctB + 1.5 * a * y1 * W8 * ctB / rb5 * 2 * y3b + 1 / W6 * R13 - W8 / W6s * R13 * Y3 +
+      W8 / W6 * (-0.5 / rb3 * (N1 * y1 * ctB - a) * 2 * y3b - 0.5 * y2s / rb3 / W6 * W5 * 2 * y3b - y2s / rb / W6s * W5 * Y3 -
+                 0.5 * y2s / rb4 / W6 * a * 2 * y3b - 1.5 * a * y2s / rb5 * 2 * y3b) +
+      1 / W7 * R6 - W8 / W7s * R6 * W3 +
+      W8 / W7 *
+          (0.5 / rb3 * (N1 * z1b * ctB + a * cB) * 2 * y3b - 1 / rb * N1 * sB * ctB + a * z1b * ctB / rb3 +
+           a * y3b * sB * ctB / rb3 - 1.5 * a * y3b * z1b * ctB / rb5 * 2 * y3b + 0.5 / rb3 / W7 * R7 * 2 * y3b +
+           1 / rb / W7s * R7 * W3 -
+           1 / rb / W7 * (-a * sB * ctB / rb * W1 + 0.5 * a * z1b * ctB / rb3 * W1 * 2 * y3b - a * z1b * ctB / rb * C3));
+  const double T23_B = nu2 * N1 * F3 * ct2 - N1 * y2 / W6s * R22 * Y3 +
+      N1 * y2 / W6 * (-0.5 * a / rb3 * 2 * y3b * ctB - y1 / W6s * W4 * Y3 - 0.5 * y1 / W6 * a / rb3 * 2 * y3b) +
+      N1 * y2 * ctB / W7s * W9 * W3 + 0.5 * N1 * y2 * ctB / W7 * a / rb3 / cB * 2 * y3b - a / rb3 * y2 * ctB +
+      1.5 * a * y2 * W8 * ctB / rb5 * 2 * y3b + y2 / rb / W6 * R2 - 0.5 * y2 * W8 / rb3 / W6 * R2 * 2 * y3b -
+      y2 * W8 / rb / W6s * R2 * Y3 +
+      y2 * W8 / rb / W6 *
+          (2 * nu * y1 / W6s * Y3 + 0.5 * a * y1 / rb3 * (1 / rb + 1 / W6) * 2 * y3b -
+           a * y1 / rb * (-0.5 / rb3 * 2 * y3b - 1 / W6s * Y3)) +
+      y2 * ctB / rb / W7 * R3 - 0.5 * y2 * W8 * ctB / rb3 / W7 * R3 * 2 * y3b - y2 * W8 * ctB / rb / W7s * R3 * W3 +
+      y2 * W8 * ctB / rb / W7 *
+          (C3 / W7 * W9 - W1 / W7s * W9 * W3 - 0.5 * W1 / W7 * a / rb3 / cB * 2 * y3b + a / rb2 / cB -
+           a * y3b / rb4 / cB * 2 * y3b);
+  const double T23_C = N1 * (-sB * W3 / W7 + y1 / W6s * (1 + a / rb) * Y3 + 0.5 * y1 / W6 * a / rb3 * 2 * y3b +
+                             sB / W7 * W2 - z1b / W7s * W2 * W3 - 0.5 * z1b / W7 * a / rb3 * 2 * y3b) +
+      y1 / rb * R11 - 0.5 * y1 * W8 / rb3 * R11 * 2 * y3b + y1 * W8 / rb * (-a / rb4 * 2 * y3b - 1 / W6s * Y3) -
+      1 / W7 * R8 + W8 / W7s * R8 * W3 -
+      W8 / W7 *
+          (0.5 * sB * a / rb3 * 2 * y3b + sB / rb * (1 + a * y3b / rb2) - 0.5 * z1b / rb3 * (1 + a * y3b / rb2) * 2 * y3b +
+           z1b / rb * (a / rb2 - a * y3b / rb4 * 2 * y3b) + 0.5 / rb3 / W7 * R9 * 2 * y3b + 1 / rb / W7s * R9 * W3 -
+           1 / rb / W7 * (-a * sB / rb * W1 + 0.5 * a * z1b / rb3 * W1 * 2 * y3b - a * z1b / rb * C3));
+  const double T23_D = nu2 * (N1 * F2 * ctB + 1 / W6 * W5 - y2s / W6s * W5 / rb - y2s / W6 * a / rb3 - cB / W7 * W2 +
+                              y2s * cB / W7s * W2 / rb + y2s * cB / W7 * a / rb3) +
+      W8 / rb * R17 - y2s * W8 / rb3 * R17 + y2 * W8 / rb * (-2 * nu / W6s / rb * y2 - 2 * a / rb4 * y2) +
+      W8 * cB / rb / W7 * R14 - y2s * W8 * cB / rb3 / W7 * R14 - y2s * W8 * cB / rb2 / W7s * R14 +
+      y2 * W8 * cB / rb / W7 * (-1 / rb * cB * y2 / W7 * W2 + W1 / W7s * W2 / rb * y2 + W1 / W7 * a / rb3 * y2 + 2 * a * y3b / rb4 * y2);
+  const double T23_E = (-2 + 2 * nu) * N1 * ctB * (1 / rb * y2 / W6 - cB / rb * y2 / W7) + nu2 * y1 / W6s * W5 / rb * y2 +
+      nu2 * y1 / W6 * a / rb3 * y2 - nu2 * z1b / W7s * W2 / rb * y2 - nu2 * z1b / W7 * a / rb3 * y2 -
+      W8 / rb3 * R23 * y2 + W8 / rb * (2 * nu * y1 / W6s / rb * y2 + 2 * a * y1 / rb4 * y2) + W8 / W7s * R15 / rb * y2 -
+      W8 / W7 *
+          (1 / rb2 * cB * y2 * ctB * R15a - W1 * ctB / rb3 * R15a * y2 + W1 * ctB / rb * (-cB / rb * y2 / W7 + W1 / W7s / rb * y2) -
+           a / rb3 * R15b * y2 +
+           a / rb * (2 * y3b * z1b / rb4 * y2 - z1b / rb2 * cB * y2 / W7 + z1b * W1 / rb3 / W7 * y2 + z1b * W1 / rb2 / W7s * y2));
+  const double T23_F = nu2 * F2 + nu2 * sB / W7 * W2 - nu2 * y2s * sB / W7s * W2 / rb - nu2 * y2s * sB / W7 * a / rb3 +
+      W8 * sB / rb / W7 * R16 - y2s * W8 * sB / rb3 / W7 * R16 - y2s * W8 * sB / rb2 / W7s * R16 +
+      y2 * W8 * sB / rb / W7 * (1 / rb * cB * y2 / W7 * W2 - W1 / W7s * W2 / rb * y2 - W1 / W7 * a / rb3 * y2 - 2 * a * y3b / rb4 * y2);
+
+  /* each block enters as b * (1/4 T / pi / (1 - nu)); shear blocks with b/2 */
+#define FSC_K(T) (0.25 * (T) / PI / (1 - nu))
+  v[0] = b1 * FSC_K(T11_1) + b2 * FSC_K(T11_2) + b3 * FSC_K(T11_3);
+  v[1] = b1 * FSC_K(T22_1) + b2 * FSC_K(T22_2) + b3 * FSC_K(T22_3);
+  v[2] = b1 * FSC_K(T33_1) + b2 * FSC_K(T33_2) + b3 * FSC_K(T33_3);
+  v[3] = b1 / 2 * FSC_K(T12_A) + b2 / 2 * FSC_K(T12_B) + b3 / 2 * FSC_K(T12_C) + b1 / 2 * FSC_K(T12_D) +
+         b2 / 2 * FSC_K(T12_E) + b3 / 2 * FSC_K(T12_F);
+  v[4] = b1 / 2 * FSC_K(T13_A) + b2 / 2 * FSC_K(T13_B) + b3 / 2 * FSC_K(T13_C) + b1 / 2 * FSC_K(T13_D) +
+         b2 / 2 * FSC_K(T13_E) + b3 / 2 * FSC_K(T13_F);
+  v[5] = b1 / 2 * FSC_K(T23_A) + b2 / 2 * FSC_K(T23_B) + b3 / 2 * FSC_K(T23_C) + b1 / 2 * FSC_K(T23_D) +
+         b2 / 2 * FSC_K(T23_E) + b3 / 2 * FSC_K(T23_F);
+#undef FSC_K
+}
+
+/* Free-surface correction of one edge PA -> PB of a triangle: the pair of
+ * angular dislocations at PA and PB (AngSetupFSC_S, TDstressFS.f90:405-558).
+ * Edges within 1e-3 rad of vertical contribute nothing (the reference's
+ * threshold).  Output: stress (Sxx, Syy, Szz, Sxy, Sxz, Syz). */
+static void ang_setup_fsc_s(double X, double Y, double Z, double bX, double bY, double bZ, const double* PA,
+                            const double* PB, double mu, double lambda, double S[6]) {
+  const double nu = lambda / (lambda + mu) / 2;
+  double side[3] = {PB[0] - PA[0], PB[1] - PA[1], PB[2] - PA[2]};
+  const double beta = acos(-side[2] / sqrt(dot3(side, side)));
+  for (int k = 0; k < 6; k++) S[k] = 0.0;
+  if (fabs(beta) < 1e-3 || fabs(PI - beta) < 1e-3) return;
+  /* the edge's frame: ey1 horizontal along the edge, ey3 up (-eZ), ey2 = ey3 x ey1 */
+  double ey1[3] = {side[0], side[1], 0.0};
+  const double n1 = sqrt(dot3(ey1, ey1));
+  for (int k = 0; k < 3; k++) ey1[k] = ey1[k] / n1;
+  const double ey3[3] = {-0.0, -0.0, -1.0};
+  double ey2[3];
+  dcross(ey3, ey1, ey2);
+  double A[3][3];
+  for (int k = 0; k < 3; k++) { A[0][k] = ey1[k]; A[1][k] = ey2[k]; A[2][k] = ey3[k]; }
+  double yA[3], yAB[3], b[3];
+  coord_trans(X - PA[0], Y - PA[1], Z - PA[2], (const double(*)[3])A, yA);
+  coord_trans(side[0], side[1], side[2], (const double(*)[3])A, yAB);
+  const double yB[3] = {yA[0] - yAB[0], yA[1] - yAB[1], yA[2] - yAB[2]};
+  coord_trans(bX, bY, bZ, (const double(*)[3])A, b);
+  /* configuration I (beta * y1A >= 0) takes the angle -pi + beta */
+  const double ang = (beta * yA[0] >= 0.0) ? -PI + beta : beta;
+  double vA[6], vB[6], v[6];
+  ang_dis_strain_fsc(yA[0], yA[1], yA[2], ang, b[0], b[1], b[2], nu, -PA[2], vA);
+  ang_dis_strain_fsc(yB[0], yB[1], yB[2], ang, b[0], b[1], b[2], nu, -PB[2], vB);
+  for (int k = 0; k < 6; k++) v[k] = vB[k] - vA[k];
+  /* back to the fault-independent frame: E = A^T v A */
+  double E[6];
+  tens_trans(v[0], v[1], v[2], v[3], v[4], v[5], (const double(*)[3])A, E);
+  const double tr = E[0] + E[1] + E[2];
+  S[0] = 2 * mu * E[0] + lambda * tr;
+  S[1] = 2 * mu * E[1] + lambda * tr;
+  S[2] = 2 * mu * E[2] + lambda * tr;
+  S[3] = 2 * mu * E[3];
+  S[4] = 2 * mu * E[4];
+  S[5] = 2 * mu * E[5];
+}
+
+/* Harmonic (free-surface) part of a triangular dislocation in the half space
+ * z <= 0 (TDstress_HarFunc, TDstressFS.f90:236-293): the slip vector in the
+ * fault-independent frame, then the three edges' angular-dislocation pairs. */
+static void td_stress_harfunc(double X, double Y, double Z, const double* P1, const double* P2, const double* P3,
+                              double Ss, double Ds, double Ts, double mu, double lambda, double S[6]) {
+  const double bx = Ts, by = Ss, bz = Ds;
+  double a[3] = {P2[0] - P1[0], P2[1] - P1[1], P2[2] - P1[2]}, c[3] = {P3[0] - P1[0], P3[1] - P1[1], P3[2] - P1[2]};
+  double Vn[3], Vs[3], Vd[3];
+  dcross(a, c, Vn);
+  double s = sqrt(dot3(Vn, Vn));
+  for (int k = 0; k < 3; k++) Vn[k] = Vn[k] / s;
+  const double eY[3] = {0.0, 1.0, 0.0}, eZ[3] = {0.0, 0.0, 1.0};
+  dcross(eZ, Vn, Vs);
+  s = sqrt(dot3(Vs, Vs));
+  for (int k = 0; k < 3; k++) Vs[k] = Vs[k] / s;
+  if (dot3(Vs, Vs) == 0.0)
+    for (int k = 0; k < 3; k++) Vs[k] = eY[k] * Vn[2];
+  s = sqrt(dot3(Vs, Vs));
+  for (int k = 0; k < 3; k++) Vs[k] = Vs[k] / s;
+  dcross(Vn, Vs, Vd);
+  /* columns Vn, Vs, Vd: slip from the triangle's frame to x, y, z */
+  double At[3][3];
+  for (int k = 0; k < 3; k++) { At[k][0] = Vn[k]; At[k][1] = Vs[k]; At[k][2] = Vd[k]; }
+  double bg[3];
+  coord_trans(bx, by, bz, (const double(*)[3])At, bg);
+  double S1[6], S2[6], S3[6];
+  ang_setup_fsc_s(X, Y, Z, bg[0], bg[1], bg[2], P1, P2, mu, lambda, S1);
+  ang_setup_fsc_s(X, Y, Z, bg[0], bg[1], bg[2], P2, P3, mu, lambda, S2);
+  ang_setup_fsc_s(X, Y, Z, bg[0], bg[1], bg[2], P3, P1, mu, lambda, S3);
+  for (int k = 0; k < 6; k++) S[k] = S1[k] + S2[k] + S3[k];
+}
+
+/* TDstressHS (TDstressFS.f90:7-44): main dislocation + its image through
+ * z = 0 + the harmonic correction, half space z <= 0 */
+void orc_tdstresshs(double X, double Y, double Z, const double* P1, const double* P2, const double* P3, double Ss,
+                    double Ds, double Ts, double mu, double lambda, double* S6) {
+  double Sm[6], Sh[6], Si[6];
+  orc_tdstressfs(X, Y, Z, P1, P2, P3, Ss, Ds, Ts, mu, lambda, Sm);
+  td_stress_harfunc(X, Y, Z, P1, P2, P3, Ss, Ds, Ts, mu, lambda, Sh);
+  const double Q1[3] = {P1[0], P1[1], -P1[2]}, Q2[3] = {P2[0], P2[1], -P2[2]}, Q3[3] = {P3[0], P3[1], -P3[2]};
+  orc_tdstressfs(X, Y, Z, Q1, Q2, Q3, Ss, Ds, Ts, mu, lambda, Si);
+  for (int k = 0; k < 6; k++) S6[k] = Sm[k] + Si[k] + Sh[k];
+}
+
+/* matel3dh_ij (m_HACApK_calc_entry_ij.f90:852-898), md='s': the source slips
+ * along its own rake (unlike matel3dn_ij, which uses the receiver's) */
+static double matel3dh_ij(int i, int j, const orc_bemv* b) {
+  double lambda = 2 * POIS / (1 - 2 * POIS) * RIGID;
+  double P1[3] = {b->xs1[j], b->ys1[j], b->zs1[j]};
+  double P2[3] = {b->xs2[j], b->ys2[j], b->zs2[j]};
+  double P3[3] = {b->xs3[j], b->ys3[j], b->zs3[j]};
+  double S[6];
+  orc_tdstresshs(b->xcol[i], b->ycol[i], b->zcol[i], P1, P2, P3, cos(b->rake[j]), sin(b->rake[j]), 0.0, RIGID,
+                 lambda, S);
+  double A[3][3];
+  A[0][0] = b->ev11[i]; A[0][1] = b->ev21[i]; A[0][2] = b->ev31[i];
+  A[1][0] = b->ev12[i]; A[1][1] = b->ev22[i]; A[1][2] = b->ev32[i];
+  A[2][0] = b->ev13[i]; A[2][1] = b->ev23[i]; A[2][2] = b->ev33[i];
+  double p[6];
+  tens_trans(S[0], S[1], S[2], S[3], S[4], S[5], (const double(*)[3])A, p);
+  if (b->v == 'n') return -p[2];
+  return p[4] * cos(b->rake[i]) + p[5] * sin(b->rake[i]);
+}
+
+/* ---- 2D plane strain (problems 2dph / 2dnh and 2dn) ---------------------- */
+static const double VS = 3.464, VP = 6.0; /* m_const.f90 */
+
+/* Stress (sxx, syy, sxy) at (X, Y) of an edge dislocation at (xs, ys) with unit
+ * Burgers vector (s1, s2) = (glide, climb) in the half space Y >= 0 whose free
+ * surface is Y = 0: the full-space pair at (xs, +-ys) plus the surface
+ * correction (D2dip2, m_HACApK_calc_entry_ij.f90:145-166). */
+static void edge_disl_hs(double X, double Y, double xs, double ys, double s1, double s2, double out[3]) {
+  const double dx = X - xs, ym = Y - ys, yp = Y + ys;
+  const double r1 = sqrt(dx * dx + ym * ym), r2 = sqrt(dx * dx + yp * yp);
+  const double q1 = r1 * r1 * r1 * r1, q2 = r2 * r2 * r2 * r2, q3 = r2 * r2 * r2 * r2 * r2 * r2;
+  const double dx2 = dx * dx, dx4 = dx2 * dx2, ym2 = ym * ym, yp2 = yp * yp, yp3 = yp2 * yp;
+  const double c = RIGID / 2.0 / PI / (1.0 - POIS);
+  /* glide (s1) and climb (s2) parts of each component */
+  const double gxx = ym * (ym2 + 3 * dx2) / q1 - yp * (yp2 + 3 * dx2) / q2 +
+                     2 * ys / q3 * (6 * Y * yp * dx2 - ym * yp3 - dx4);
+  const double cxx = dx * (ym2 - dx2) / q1 - dx * (yp2 - dx2) / q2 +
+                     4 * ys * dx / q3 * ((2 * ys - Y) * yp2 + (3 * Y + 2 * ys) * dx2);
+  const double gyy = ym * (ym2 - dx2) / q1 - yp * (yp2 - dx2) / q2 -
+                     2 * ys / q3 * (6 * Y * yp * dx2 - (3 * Y + ys) * yp3 + dx4);
+  const double cyy = dx * (3 * ym2 + dx2) / q1 - dx * (3 * yp2 + dx2) / q2 -
+                     4 * ys * dx * Y / q3 * (3 * yp2 - dx2);
+  const double gxy = dx * (ym2 - dx2) / q1 - dx * (yp2 - dx2) / q2 + 4 * ys * dx * Y / q3 * (3 * yp2 - dx2);
+  const double cxy = ym * (ym2 - dx2) / q1 - yp * (yp2 - dx2) / q2 +
+                     2 * ys / q3 * (6 * Y * yp * dx2 - dx4 + (ys - Y) * yp3);
+  out[0] = s1 * c * gxx + s2 * c * cxx;
+  out[1] = s1 * c * gyy - s2 * c * cyy;
+  out[2] = s1 * c * gxy + s2 * c * cxy;
+}
+
+/* traction on a plane at angle a of the x axis from (sxx, syy, sxy): shear
+ * (v='s') or normal, compression positive (v='n') */
+static double traction_2d_hs(double sxx, double syy, double sxy, double a, char v) {
+  if (v == 'n') return -0.5 * (sxx + syy) + 0.5 * (sxx - syy) * cos(2 * a) + sxy * sin(2 * a);
+  return -0.5 * (sxx - syy) * sin(2 * a) + sxy * cos(2 * a);
+}
+
+/* matel2dph2_ij (m_HACApK_calc_entry_ij.f90:92-116): unit slip on element j
+ * (between its ends, along its dip ang(j)) in the half space */
+static double matel2dph(int i, int j, const orc_bemv* b) {
+  const double s1 = cos(b->ang[j]), s2 = sin(b->ang[j]);
+  double p[3], q[3];
+  edge_disl_hs(b->xcol[i], b->ycol[i], b->xel[j], b->yel[j], s1, s2, p);
+  edge_disl_hs(b->xcol[i], b->ycol[i], b->xer[j], b->yer[j], s1, s2, q);
+  return traction_2d_hs(p[0] - q[0], p[1] - q[1], p[2] - q[2], b->ang[i], b->v);
+}
+
+/* the full-space integrals inte11s / inte12s / inte22s (:697-722): stress
+ * kernel components of a dislocation end at (x1, x2) in its own frame */
+static void plane_kernel(double x1, double x2, double k[3]) {
+  const double r = sqrt(x1 * x1 + x2 * x2);
+  const double r4 = r * r * r * r;
+  const double pa = VS / VP;
+  k[0] = -2 * VS / PI * (1 - pa * pa) * x2 * (3 * x1 * x1 + x2 * x2) / r4;
+  k[1] = 2 * VS / PI * (1 - pa * pa) * x1 * (x1 * x1 - x2 * x2) / r4;
+  k[2] = 2 * VS / PI * (1 - pa * pa) * x2 * (x1 * x1 - x2 * x2) / r4;
+}
+
+/* tensor2d_ij (m_HACApK_calc_entry_ij.f90:300-339), md='s': full space */
+static double tensor2d(int i, int j, const orc_bemv* b) {
+  const double cj = cos(b->ang[j]), sj = sin(b->ang[j]);
+  const double dxl = b->xcol[i] - b->xel[j], dyl = b->ycol[i] - b->yel[j];
+  const double dxr = b->xcol[i] - b->xer[j], dyr = b->ycol[i] - b->yer[j];
+  double kl[3], kr[3];
+  plane_kernel(cj * dxl + sj * dyl, -sj * dxl + cj * dyl, kl);
+  plane_kernel(cj * dxr + sj * dyr, -sj * dxr + cj * dyr, kr);
+  const double g = -0.5 * RIGID / VS;
+  const double k11 = g * (kl[0] - kr[0]), k12 = g * (kl[1] - kr[1]), k22 = g * (kl[2] - kr[2]);
+  /* rotate from the source frame to x, y */
+  const double s2 = sin(-2 * b->ang[j]), c2 = cos(-2 * b->ang[j]);
+  const double sxx = 0.5 * (k11 + k22) + 0.5 * (k11 - k22) * c2 + k12 * s2;
+  const double sxy = -0.5 * (k11 - k22) * s2 + k12 * c2;
+  const double syy = 0.5 * (k11 + k22) - 0.5 * (k11 - k22) * c2 - k12 * s2;
+  const double a = b->ang[i];
+  if (b->v == 'n') return -(0.5 * (sxx + syy) - 0.5 * (sxx - syy) * cos(2 * a) - sxy * sin(2 * a));
+  return 0.5 * (sxx - syy) * sin(-2 * a) + sxy * cos(-2 * a);
+}
+
 double orc_entry_ij(int i, int j, const orc_bemv* b) {
   int i0 = i - 1, j0 = j - 1;
   switch (b->problem) {
@@ -542,6 +1027,9 @@ double orc_entry_ij(int i, int j, const orc_bemv* b) {
     case ORC_3DPH: return okada_ij(i0, j0, b, 0);
     case ORC_3DNR: return okada_ij(i0, j0, b, 1);
     case ORC_3DNT: return matel3dn_ij(i0, j0, b);
+    case ORC_2DPH: return matel2dph(i0, j0, b);
+    case ORC_2DN: return tensor2d(i0, j0, b);
+    case ORC_3DHT: return matel3dh_ij(i0, j0, b);
   }
   return NAN;
 }

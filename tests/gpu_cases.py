@@ -26,10 +26,30 @@ def case(kind, n_hint=None):
         n = len(tri)
         g["rake"] = np.zeros(n)
         return H.HBI_3DNT, n, g, 0.0, 1e-4
+    if kind == "3dht":
+        nx, nz = (n_hint or (24, 12))
+        tri = mesh.rough_fault(nx, nz, 6.0, 3.0, seed=7)
+        tri[:, :, 2] -= 0.5  # buried: top edge 0.5 km below the free surface
+        g, _ = mesh.tri_geometry(tri)
+        n = len(tri)
+        g["rake"] = np.linspace(0.0, 0.5 * mesh.PI, n)  # the source's own rake enters the 3dht entry
+        return H.HBI_3DHT, n, g, 0.0, 1e-4
+    if kind == "2dph":
+        n = n_hint or 600
+        xel, xer, yel, yer, xcol, ycol, ang, _ = mesh.mesh_2dph(n, 40.0 / n, 30.0)
+        return H.HBI_2DPH, n, dict(xcol=xcol, ycol=ycol, zcol=np.zeros(n), xel=xel, xer=xer, yel=yel, yer=yer,
+                                   ang=ang), 0.0, 1e-6
+    if kind == "2dn":
+        n = n_hint or 600
+        xel, xer, yel, yer, xcol, ycol, ang, _ = mesh.mesh_2dn(*mesh.bent_fault_2d(n, 40.0, 0.0, 25.0, seed=3,
+                                                                                   rough=0.2))
+        return H.HBI_2DN, n, dict(xcol=xcol, ycol=ycol, zcol=np.zeros(n), xel=xel, xer=xer, yel=yel, yer=yer,
+                                  ang=ang), 0.0, 1e-6
     raise ValueError(kind)
 
 
-ORC_PROBLEM = {H.HBI_2DVS: 1, H.HBI_3DPH: 2, H.HBI_3DNR: 3, H.HBI_3DNT: 4}
+ORC_PROBLEM = {H.HBI_2DVS: 1, H.HBI_3DPH: 2, H.HBI_3DNR: 3, H.HBI_3DNT: 4, H.HBI_2DPH: 5, H.HBI_2DN: 6,
+               H.HBI_3DHT: 7}
 
 
 def oracle_geometry(O, problem, n, g, w, v):

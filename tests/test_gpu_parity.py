@@ -20,7 +20,7 @@ from gpu_cases import case, oracle_geometry, product_geometry
 
 pytestmark = pytest.mark.gpu
 
-KINDS = ["2dvs", "3dph", "3dnr", "3dnt"]
+KINDS = ["2dvs", "3dph", "3dnr", "3dnt", "2dph", "2dn", "3dht"]
 
 
 @pytest.fixture(scope="module")

@@ -36,6 +36,33 @@ def test_okada_equals_two_triangles(oracle, pt, slip):
     assert np.max(np.abs(so - st)) <= 1e-12 * np.max(np.abs(so))
 
 
+@pytest.mark.parametrize("dip", [30.0, 60.0, 90.0, 120.0])
+@pytest.mark.parametrize("pt", [(0.3, 0.7, -3.2), (2.5, -1.0, -2.0), (0.0, 1.0, -0.3), (1.5, -0.5, -6.0)])
+@pytest.mark.parametrize("slip", [(1, 0), (0, 1)])
+def test_okada_half_space_equals_two_half_space_triangles(oracle, dip, pt, slip):
+    """'3dht': Nikkhoo-Walter triangles in a half space (main + image
+    dislocation + the free-surface correction of AngDisStrainFSC) tile Okada's
+    half-space rectangle, close to the surface too (z = -0.3 km, where the
+    full-space answer is off by order one)."""
+    d, dep = math.radians(dip), 3.0
+    cw = lambda e: (e * math.cos(d), -dep + e * math.sin(d))
+    A, B, C, D = (-1, *cw(-0.5)), (1, *cw(-0.5)), (1, *cw(0.5)), (-1, *cw(0.5))
+    so = okada_stress(oracle, *pt, *slip, dip=dip, depth=dep, full=False)
+    st = (oracle.tdstresshs(*pt, A, B, C, slip[0], slip[1], 0, MU, LAM)
+          + oracle.tdstresshs(*pt, A, C, D, slip[0], slip[1], 0, MU, LAM))
+    assert np.max(np.abs(so - st)) <= 1e-12 * np.max(np.abs(so))
+
+
+def test_half_space_triangle_leaves_the_surface_traction_free(oracle):
+    """sigma_xz, sigma_yz, sigma_zz of '3dht' vanish on z = 0 for a buried
+    triangle with mixed strike, dip and tensile slip."""
+    P1, P2, P3 = (0, 0, -2), (2, 1, -3), (1, 2, -1.5)
+    for pt in [(0.5, 0.5, 0.0), (3, -2, 0.0), (-1, 4, 0.0), (8, 3, 0.0)]:
+        s = oracle.tdstresshs(*pt, P1, P2, P3, 1, 0.5, 0.2, MU, LAM)
+        deep = oracle.tdstresshs(pt[0], pt[1], -1.0, P1, P2, P3, 1, 0.5, 0.2, MU, LAM)
+        assert max(abs(s[2]), abs(s[4]), abs(s[5])) <= 1e-13 * np.max(np.abs(deep)), pt
+
+
 def test_okada_long_fault_is_2d_antiplane(oracle):
     """A very long vertical strike-slip rectangle in a half space reproduces the
     2D antiplane half-space kernel of '2dvs' (matels2dpa_ij minus its image)."""
@@ -52,6 +79,51 @@ def test_okada_long_fault_is_2d_antiplane(oracle):
         sxy = MU * (u[6] + u[4])  # 2 mu e_xy
         # same magnitude; the 2D kernel's sign convention is opposite to Okada's disl1
         assert abs(sxy / e2d + 1.0) <= 2e-6, (i, j, sxy, e2d)
+
+
+def _geometry_2d(oracle, problem, v, xel, xer, yel, yer):
+    from hbi_gb300 import mesh
+    xel, xer, yel, yer, xcol, ycol, ang, _ = mesh.mesh_2dn(xel, xer, yel, yer)
+    n = len(xel)
+    return oracle.Geometry(problem, n, v, xcol=xcol, ycol=ycol, zcol=np.zeros(n), xel=xel, xer=xer, yel=yel,
+                           yer=yer, ang=ang)
+
+
+def test_2dph_free_surface_is_traction_free(oracle):
+    """Edge dislocations of '2dph' (D2dip2) leave the free surface y = 0
+    traction free: receivers on y = 0 with horizontal planes (ang = 0) feel
+    neither shear nor normal traction, whatever the source."""
+    from hbi_gb300 import mesh
+    src = mesh.bent_fault_2d(8, 4.0, 1.5, 40.0, seed=1)
+    m = 7
+    xs = np.linspace(-4, 8, m)
+    xel = np.concatenate([xs - 0.05, src[0]]); xer = np.concatenate([xs + 0.05, src[1]])
+    yel = np.concatenate([np.zeros(m), src[2]]); yer = np.concatenate([np.zeros(m), src[3]])
+    for v in "sn":
+        g = _geometry_2d(oracle, oracle.ORC_2DPH, v, xel, xer, yel, yer)
+        at_depth = max(abs(oracle.entry(g, m + k, m + k)) for k in range(1, 9))
+        for i in range(1, m + 1):
+            for j in range(m + 1, m + 9):
+                assert abs(oracle.entry(g, i, j)) <= 1e-13 * at_depth, (v, i, j)
+
+
+def test_2dph_deep_is_2dn_full_space(oracle):
+    """Far below the free surface the half-space edge dislocations of '2dph'
+    (D2dip2) reduce to the full-space plane-strain kernel of '2dn'
+    (tensor2d_ij, written with vs / vp instead of nu): the two formulations
+    agree for shear and normal traction on a bent fault 2000 km deep (the
+    image's share is ~(L / 4000 km)^2 = 1e-6).  The two prefactors differ by
+    the rounding of the constants: mu/(2 pi (1-nu)) with nu = 0.25 against
+    mu (1 - vs^2/vp^2)/pi with vs = 3.464 (not sqrt(12)) and vp = 6."""
+    from hbi_gb300 import mesh
+    ends = mesh.bent_fault_2d(40, 4.0, 2000.0, 35.0, seed=2, rough=0.3)
+    prefactor_ratio = (1 - (3.464 / 6.0) ** 2) * 2 * (1 - 0.25)
+    for v in "sn":
+        gh = _geometry_2d(oracle, oracle.ORC_2DPH, v, *ends)
+        gf = _geometry_2d(oracle, oracle.ORC_2DN, v, *ends)
+        A = np.array([[oracle.entry(gh, i, j) for j in range(1, 41)] for i in range(1, 41)])
+        B = np.array([[oracle.entry(gf, i, j) for j in range(1, 41)] for i in range(1, 41)]) / prefactor_ratio
+        assert np.max(np.abs(A - B)) <= 5e-6 * np.max(np.abs(B)), v
 
 
 def test_tdstress_symmetry_and_decay(oracle):

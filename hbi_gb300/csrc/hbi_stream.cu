@@ -235,6 +235,26 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
   Acc xc[VEC], xn[VEC];
   load_x(Dc, xc);
   load_x(Dn, xn);
+  // the arrival of a finished multi-tile item is resolved one chunk later, so
+  // that the atomic's round trip overlaps the next chunk
+  int pend_old = 0, pend_cg = -1, pend_ntile = 0, pend_ncols = 0, pend_poff = 0, pend_z0 = 0, pend_sec = 0;
+  auto resolve = [&]() {
+    if (pend_cg < 0) return;
+    const int last = __shfl_sync(0xffffffffu, pend_old == pend_ntile - 1 ? 1 : 0, 0);
+    if (last) {
+      __syncwarp();  // lane 0's acquire orders the reads of every lane
+      const MatDev& PM = pend_sec ? m1 : m0;
+      Acc* z = (Acc*)PM.z;
+      const Acc* part = (const Acc*)PM.part;
+      for (int col = lane; col < pend_ncols; col += 32) {
+        Acc t = 0;
+        for (int q = 0; q < pend_ntile; q++) t += __ldcg(&part[pend_poff + (int64_t)q * pend_ncols + col]);
+        z[pend_z0 + col] = t;
+      }
+      if (lane == 0) PM.cnt[pend_cg] = 0;
+    }
+    pend_cg = -1;
+  };
   while (c_it < ntot) {
     const bool sec = c_it >= n0;
     const MatDev& M = sec ? m1 : m0;
@@ -320,23 +340,20 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
     __syncwarp();
     c_seq++;
     produce();
+    resolve();
     c_c0 += nc;
     if (c_c0 < Dc.ncols) continue;
-    // item done: the last row tile of a column group sums the tiles in order
+    // item done: the last row tile of a column group to arrive sums the
+    // tiles in order (resolved after the next chunk)
     if (Dc.ntile > 1) {
       __syncwarp();
-      int last = 0;
-      if (lane == 0) last = arrive_acq_rel(&M.cnt[Dc.cg]) == Dc.ntile - 1;
-      last = __shfl_sync(0xffffffffu, last, 0);
-      if (last) {
-        __syncwarp();  // lane 0's acquire orders the reads of every lane
-        for (int col = lane; col < Dc.ncols; col += 32) {
-          Acc t = 0;
-          for (int q = 0; q < Dc.ntile; q++) t += __ldcg(&part[Dc.poff + (int64_t)q * Dc.ncols + col]);
-          z[Dc.z0 + col] = t;
-        }
-        if (lane == 0) M.cnt[Dc.cg] = 0;
-      }
+      if (lane == 0) pend_old = arrive_acq_rel(&M.cnt[Dc.cg]);
+      pend_cg = Dc.cg;
+      pend_ntile = Dc.ntile;
+      pend_ncols = Dc.ncols;
+      pend_poff = Dc.poff;
+      pend_z0 = Dc.z0;
+      pend_sec = sec;
     }
     c_it += GW;
     c_c0 = 0;
@@ -347,6 +364,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
     load_x(Dn, xn);
     Dnn = desc(c_it + 2 * GW);
   }
+  resolve();
 }
 
 // ---------------------------------------------------------------- phase 2

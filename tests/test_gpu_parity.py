@@ -5,8 +5,13 @@ Tolerances:
   * tree, admissibility, leaf order, lod: bit-exact;
   * 2dvs entries: bit-exact (division/subtraction only, rounded as IEEE);
   * Okada / triangular entries: |gpu - oracle| <= 1e-11 max|entry| (CUDA's
-    libm differs from the C library's in the last ulp);
-  * ACA+ factors: rank per leaf equal for >= 90% of admissible leaves, and
+    libm differs from the C library's in the last ulp); half-space triangles
+    (3dht) 2e-6: the free-surface correction of edges close to vertical
+    (cot(beta) up to 1e3 at the reference's 1e-3 rad cutoff) cancels large
+    terms, so rounding alone moves an entry by ~5e-7 of scale -- the oracle
+    itself does when compiled with fused multiply-add;
+  * ACA+ factors: rank per leaf equal for >= 90% of admissible leaves (80%
+    for 3dht, whose entries carry ~5e-7 rounding noise), and
     ||H_gpu - A||_F within 3x of the oracle's own ||H_oracle - A||_F (+eps);
   * FP64 matvec: relative 1e-12 against the same factors multiplied on the CPU;
   * FP32 factors: 1e-5, BF16 factors: 2e-2 relative to the FP64 product;
@@ -21,6 +26,7 @@ from gpu_cases import case, oracle_geometry, product_geometry
 pytestmark = pytest.mark.gpu
 
 KINDS = ["2dvs", "3dph", "3dnr", "3dnt", "2dph", "2dn", "3dht"]
+ENTRY_TOL = {"3dht": 2e-6}  # relative to the largest entry; 1e-11 otherwise
 
 
 @pytest.fixture(scope="module")
@@ -66,7 +72,7 @@ def test_entries(oracle, built, kind, v):
         # scale: the shear self-interaction (normal entries of a planar fault
         # in a full space vanish analytically and are pure round-off)
         scale = max(np.max(np.abs(ref)), abs(oracle.entry(built(kind, "s")["ogeo"], 1, 1)))
-        assert np.max(np.abs(gpu - ref)) <= 1e-11 * scale
+        assert np.max(np.abs(gpu - ref)) <= ENTRY_TOL.get(kind, 1e-11) * scale
 
 
 @pytest.mark.parametrize("kind", KINDS)
@@ -100,14 +106,23 @@ def test_aca_ranks_and_accuracy(oracle, built, kind):
     lo = B["Ho"].leaves
     lr = lv[:, 0] == 1
     same = np.mean(lv[lr, 1] == lo[lr, 1])
-    assert same >= 0.9, same
+    # 3dht: rounding moves ACA's stopping tests (see ENTRY_TOL); the oracle
+    # compiled with fused multiply-add keeps 86% of its own ranks there
+    assert same >= (0.8 if kind == "3dht" else 0.9), same
     if kind == "2dvs":
         assert same == 1.0
     off, body = B["lf"].body()
     Ag = dense_from_body(B["n"], lv, off, body)
     A = oracle.dense_matrix(B["ogeo"], B["lod"])
     Ao = B["Ho"].to_dense()
-    ng = np.linalg.norm(Ag - A)
+    # each ACA against the entries it approximates: the device's own dense
+    # matrix for the device (they differ from the oracle's by the rounding
+    # noise of ENTRY_TOL)
+    lod = B["lod"]
+    n = B["n"]
+    Ad = H.entry_ij(B["geo"], np.repeat(lod, n), np.tile(lod, n)).reshape(n, n)
+    assert np.max(np.abs(Ad - A)) <= ENTRY_TOL.get(kind, 1e-11) * np.max(np.abs(A))
+    ng = np.linalg.norm(Ag - Ad)
     no = np.linalg.norm(Ao - A)
     assert ng <= 3 * no + 1e-14 * np.linalg.norm(A), (ng, no)
     # dense near-field blocks are exact entries
@@ -115,7 +130,8 @@ def test_aca_ranks_and_accuracy(oracle, built, kind):
         lt, kt, r0, ndl, c0, ndt = lv[ip]
         blk = body[off[ip]:off[ip] + ndl * ndt].reshape(ndl, ndt)
         ref = A[r0 - 1:r0 - 1 + ndl, c0 - 1:c0 - 1 + ndt]
-        assert np.max(np.abs(blk - ref)) <= 1e-11 * max(np.max(np.abs(ref)), 1e-300)
+        tol = ENTRY_TOL.get(kind, 1e-11) * (np.max(np.abs(A)) if kind in ENTRY_TOL else np.max(np.abs(ref)))
+        assert np.max(np.abs(blk - ref)) <= max(tol, 1e-300)
 
 
 @pytest.mark.parametrize("kind", KINDS)
@@ -136,7 +152,7 @@ def test_matvec_fp64(oracle, built, kind):
     assert np.array_equal(lh.matvec(u), lh.matvec(u))
 
 
-@pytest.mark.parametrize("kind", ["2dvs", "3dph", "3dnt"])
+@pytest.mark.parametrize("kind", ["2dvs", "3dph", "3dnt", "2dph", "3dht"])
 @pytest.mark.parametrize("store,tol", [("f32", 1e-5), ("bf16", 2e-2)])
 def test_matvec_mixed(built, kind, store, tol):
     B = built(kind)
@@ -175,7 +191,7 @@ def _rsf_setup(B, oracle, two_mats, evlaw=0):
     return dict(a=a, b=b, dc=dc, f0=f0, vpl=vpl), y
 
 
-@pytest.mark.parametrize("kind", ["2dvs", "3dph", "3dnt"])
+@pytest.mark.parametrize("kind", ["2dvs", "3dph", "3dnt", "2dph", "2dn", "3dht"])
 def test_derivs_and_rkck(oracle, built, kind):
     Bs = built(kind, "s")
     two = kind != "2dvs"
@@ -184,7 +200,7 @@ def test_derivs_and_rkck(oracle, built, kind):
     scale = 1.0 / Bs["w"] if kind == "3dph" else 1.0
     lhs = H.LHp(Bs["lf"], Bs["ctl"], "f64")
     lhn = H.LHp(Bn["lf"], Bn["ctl"], "f64") if two else None
-    evlaw = 1 if kind == "3dnt" else 0
+    evlaw = 1 if kind in ("3dnt", "3dht") else 0
     rk = H.RK(lhs, lhn, evlaw=evlaw, scale=scale, **prm)
     off, body = Bs["lf"].body()
     Hs = oracle.HMatrix.from_body(Bs["n"], Bs["lf"].leaves(), off, body)

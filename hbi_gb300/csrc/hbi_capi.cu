@@ -199,6 +199,7 @@ struct hbi_lhp_s {
   int32_t* d_midx = nullptr;
   int32_t *d_grow0 = nullptr, *d_gndl = nullptr, *d_gnch = nullptr, *d_gpoff = nullptr;
   int32_t *d_row_fc = nullptr, *d_fc_ptr = nullptr, *d_fc_group = nullptr;
+  int32_t *d_w1off = nullptr, *d_w1item = nullptr, *d_w2off = nullptr, *d_w2item = nullptr;
   int* d_err = nullptr;
   double *d_x = nullptr, *d_y = nullptr;
   MatDev md{};
@@ -613,6 +614,30 @@ extern "C" int hbi_construct_lh(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* 
   m.scale = 1.0;
   m.skip = nullptr;
   m.err = h->d_err;
+  // static warp schedules for the grid the phase kernels get on this device:
+  // one block of stream_warps_per_block() warps per SM, fewer for small operators
+  {
+    const int nw = stream_warps_per_block(), sb = stream_stage_bytes();
+    for (int ph = 1; ph <= 2; ph++) {
+      const int ni = ph == 1 ? (int)P.p1.size() : (int)P.p2.size();
+      if (ni == 0) continue;
+      const int need = (ni + nw - 1) / nw;
+      const int gw = (need < c->sm_count ? need : c->sm_count) * nw;
+      std::vector<int64_t> cost(ni);
+      for (int i = 0; i < ni; i++) {
+        const int ncols = ph == 1 ? P.p1[i].ncols : P.p2[i].ncols, ntp = ph == 1 ? P.p1[i].ntp : P.p2[i].ntp;
+        const int cc = chunk_cols(ntp, esz, sb);
+        // bytes streamed plus ~1 KB worth of fixed cost per chunk
+        cost[i] = (int64_t)ncols * ntp * esz + 1024 * (int64_t)((ncols + cc - 1) / cc);
+      }
+      std::vector<int32_t> woff, witem;
+      plan_warp_schedule(cost, gw, woff, witem);
+      CK(upload(ph == 1 ? &h->d_w1off : &h->d_w2off, woff, st));
+      CK(upload(ph == 1 ? &h->d_w1item : &h->d_w2item, witem, st));
+      (ph == 1 ? m.gw1 : m.gw2) = gw;
+    }
+    m.w1off = h->d_w1off; m.w1item = h->d_w1item; m.w2off = h->d_w2off; m.w2item = h->d_w2item;
+  }
   h->alg_bytes = (double)P.factor_elems * esz + (double)h->n * 8 * 2;
   prepare_stream_kernels();
   CK(cudaGetLastError());
@@ -625,6 +650,7 @@ extern "C" int hbi_free_lh(hbi_lhp* h) {
   for (void* p : {h->d_vstore, h->d_ustore, (void*)h->d_s1, (void*)h->d_s2, (void*)h->d_cnt, h->d_part, h->d_z,
                   h->d_gpart, (void*)h->d_midx, (void*)h->d_grow0, (void*)h->d_gndl, (void*)h->d_gnch,
                   (void*)h->d_gpoff, (void*)h->d_row_fc, (void*)h->d_fc_ptr, (void*)h->d_fc_group, (void*)h->d_err,
+                  (void*)h->d_w1off, (void*)h->d_w1item, (void*)h->d_w2off, (void*)h->d_w2item,
                   (void*)h->d_x, (void*)h->d_y})
     if (p) cudaFree(p);
   delete h;

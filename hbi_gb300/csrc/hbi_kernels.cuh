@@ -70,6 +70,10 @@ struct MatDev {            // one H-matrix on the device
   double scale;            // result multiplier (1/ds0 for 3dph, else 1)
   const int* skip;         // when non-null and nonzero, phases 1-2 do nothing
   int* err;                // set to nonzero when a bulk copy did not arrive in time
+  // static warp schedules (hbi_structure.hpp, plan_warp_schedule) for a grid
+  // of gw1 / gw2 warps: warp w walks item[off[w] .. off[w+1]) of its phase
+  const int32_t *w1off, *w1item, *w2off, *w2item;
+  int gw1, gw2;
 };
 
 // RK (Cash-Karp) stage state on the device; all arrays in cluster order
@@ -113,6 +117,9 @@ struct RkView {
 void launch_segcopy(const double* body, const SegCopyDev* map, int64_t nmap, void* dst, int storage,
                     cudaStream_t st);
 void prepare_stream_kernels();
+// the phase kernels' launch shape: warps per block and bytes per stage
+int stream_warps_per_block();
+int stream_stage_bytes();
 void launch_phase1(const MatDev* mats, int nmat, const double* x, int sm_count, cudaStream_t st);
 void launch_phase2(const MatDev* mats, int nmat, const double* x, int sm_count, cudaStream_t st);
 void launch_phase3_plain(const MatDev* mats, int nmat, double* const* y, cudaStream_t st);

@@ -166,6 +166,44 @@ __device__ __forceinline__ int arrive_acq_rel(int* p) {
   return old;
 }
 
+// The items one warp walks, in order: the host's schedule when it was made
+// for this grid (m0's list, then m1's), else every GW-th item.  at(k) is the
+// k-th item, ntot past the end.
+struct WarpSeq {
+  const int32_t *a0 = nullptr, *a1 = nullptr;
+  int len0 = 0, len1 = 0, n0 = 0, gw = 0, GW = 1, ntot = 0;
+  __device__ int at(int k) const {
+    if (a0) {
+      if (k < len0) return __ldg(&a0[k]);
+      k -= len0;
+      return k < len1 ? n0 + __ldg(&a1[k]) : ntot;
+    }
+    const int64_t it = gw + (int64_t)k * GW;
+    return it < ntot ? (int)it : ntot;
+  }
+};
+
+__device__ __forceinline__ WarpSeq warp_seq(const MatDev& m0, const MatDev& m1, int nmat, int phase, int gw, int GW,
+                                            int n0, int ntot) {
+  WarpSeq q;
+  q.n0 = n0;
+  q.gw = gw;
+  q.GW = GW;
+  q.ntot = ntot;
+  const int32_t* off0 = phase == 1 ? m0.w1off : m0.w2off;
+  const int32_t* off1 = phase == 1 ? m1.w1off : m1.w2off;
+  const int g0 = phase == 1 ? m0.gw1 : m0.gw2, g1 = phase == 1 ? m1.gw1 : m1.gw2;
+  if (off0 && g0 == GW && (nmat == 1 || (off1 && g1 == GW))) {
+    q.a0 = (phase == 1 ? m0.w1item : m0.w2item) + __ldg(&off0[gw]);
+    q.len0 = __ldg(&off0[gw + 1]) - __ldg(&off0[gw]);
+    if (nmat == 2) {
+      q.a1 = (phase == 1 ? m1.w1item : m1.w2item) + __ldg(&off1[gw]);
+      q.len1 = __ldg(&off1[gw + 1]) - __ldg(&off1[gw]);
+    }
+  }
+  return q;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------- phase 1
@@ -196,9 +234,11 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
     if (it < ntot) d = it < n0 ? m0.s1[it] : m1.s1[it - n0];
     return d;
   };
-  // producer: walks this warp's items chunk by chunk, NS chunks ahead
-  int p_it = gw, p_c0 = 0, p_seq = 0;
-  S1ItemDev Dp = desc(p_it), Dpn = desc(p_it + GW);
+  const WarpSeq seq = warp_seq(m0, m1, nmat, 1, gw, GW, n0, ntot);
+  // producer: walks this warp's items chunk by chunk, NS chunks ahead; the
+  // item ids are fetched two items ahead, the descriptors one
+  int p_k = 0, p_it = seq.at(0), p_itn = seq.at(1), p_itnn = seq.at(2), p_c0 = 0, p_seq = 0;
+  S1ItemDev Dp = desc(p_it), Dpn = desc(p_itn);
   auto produce = [&]() {
     if (p_it >= ntot) return;
     const int nc = min(chunk_cols_dev<SB>(Dp.ntp, ESZ), Dp.ncols - p_c0);
@@ -213,16 +253,19 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
     p_seq++;
     p_c0 += nc;
     if (p_c0 >= Dp.ncols) {
-      p_it += GW;
+      p_k++;
+      p_it = p_itn;
+      p_itn = p_itnn;
+      p_itnn = seq.at(p_k + 2);
       p_c0 = 0;
       Dp = Dpn;
-      Dpn = desc(p_it + GW);
+      Dpn = desc(p_itn);
     }
   };
   for (int q = 0; q < NS; q++) produce();
-  // consumer
-  int c_it = gw, c_c0 = 0, c_seq = 0;
-  S1ItemDev Dc = desc(c_it), Dn = desc(c_it + GW), Dnn = desc(c_it + 2 * GW);
+  // consumer: item ids three ahead, descriptors two
+  int c_k = 0, c_it = seq.at(0), c_i1 = seq.at(1), c_i2 = seq.at(2), c_i3 = seq.at(3), c_c0 = 0, c_seq = 0;
+  S1ItemDev Dc = desc(c_it), Dn = desc(c_i1), Dnn = desc(c_i2);
   auto load_x = [&](const S1ItemDev& D, Acc* xv) {
     const int lw = log2ceil(max(1, D.ntp / VEC));
     const int j = lane & ((1 << lw) - 1);
@@ -355,14 +398,18 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
       pend_z0 = Dc.z0;
       pend_sec = sec;
     }
-    c_it += GW;
+    c_k++;
+    c_it = c_i1;
+    c_i1 = c_i2;
+    c_i2 = c_i3;
+    c_i3 = seq.at(c_k + 3);
     c_c0 = 0;
     Dc = Dn;
     Dn = Dnn;
 #pragma unroll
     for (int v = 0; v < VEC; v++) xc[v] = xn[v];
     load_x(Dn, xn);
-    Dnn = desc(c_it + 2 * GW);
+    Dnn = desc(c_i2);
   }
   resolve();
 }
@@ -405,8 +452,9 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
     int32_t idx[KP];
     int nc, sec;
   };
-  int p_it = gw, p_c0 = 0, p_seq = 0;
-  S2ItemDev Dp = desc(p_it), Dpn = desc(p_it + GW);
+  const WarpSeq seq = warp_seq(m0, m1, nmat, 2, gw, GW, n0, ntot);
+  int p_k = 0, p_it = seq.at(0), p_itn = seq.at(1), p_itnn = seq.at(2), p_c0 = 0, p_seq = 0;
+  S2ItemDev Dp = desc(p_it), Dpn = desc(p_itn);
   auto produce = [&](Pend& pd) {
     pd.nc = 0;
     pd.sec = 0;
@@ -433,10 +481,13 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
     p_seq++;
     p_c0 += nc;
     if (p_c0 >= Dp.ncols) {
-      p_it += GW;
+      p_k++;
+      p_it = p_itn;
+      p_itn = p_itnn;
+      p_itnn = seq.at(p_k + 2);
       p_c0 = 0;
       Dp = Dpn;
-      Dpn = desc(p_it + GW);
+      Dpn = desc(p_itn);
     }
   };
   auto gather = [&](const Pend& pd, Acc* mu) {
@@ -454,8 +505,8 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
   for (int q = 0; q < NS; q++) produce(fifo[q]);
   Acc mu[KP];
   gather(fifo[0], mu);
-  int c_it = gw, c_c0 = 0, c_seq = 0;
-  S2ItemDev Dc = desc(c_it), Dn = desc(c_it + GW);
+  int c_k = 0, c_it = seq.at(0), c_i1 = seq.at(1), c_i2 = seq.at(2), c_c0 = 0, c_seq = 0;
+  S2ItemDev Dc = desc(c_it), Dn = desc(c_i1);
   Acc acc[VEC];
 #pragma unroll
   for (int v = 0; v < VEC; v++) acc[v] = 0;
@@ -527,10 +578,13 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
     }
 #pragma unroll
     for (int v = 0; v < VEC; v++) acc[v] = 0;
-    c_it += GW;
+    c_k++;
+    c_it = c_i1;
+    c_i1 = c_i2;
+    c_i2 = seq.at(c_k + 2);
     c_c0 = 0;
     Dc = Dn;
-    Dn = desc(c_it + GW);
+    Dn = desc(c_i1);
   }
 }
 
@@ -586,6 +640,13 @@ int stream_shape() {
   }
   return shape;
 }
+
+}  // namespace
+
+int stream_warps_per_block() { return stream_shape() == 1 ? 6 : stream_shape() == 2 ? 8 : 12; }
+int stream_stage_bytes() { return stream_shape() == 1 ? 16384 : 8192; }
+
+namespace {
 
 template <typename T, int NW, int NS, int SB>
 void launch_p1_shape(const MatDev& m0, const MatDev& m1, int nmat, const double* x, int sm, int n, cudaStream_t st) {

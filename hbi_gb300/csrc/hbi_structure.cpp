@@ -496,6 +496,35 @@ void plan_stream(int n, const std::vector<Leaf>& leaves, const std::vector<int64
   });
 }
 
+void plan_warp_schedule(const std::vector<int64_t>& cost, int nwarps, std::vector<int32_t>& woff,
+                        std::vector<int32_t>& witem) {
+  const int n = (int)cost.size();
+  std::vector<int32_t> order(n);
+  for (int i = 0; i < n; i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+  // min-heap of (load, warp)
+  std::vector<std::pair<int64_t, int>> heap;
+  heap.reserve(nwarps);
+  for (int w = 0; w < nwarps; w++) heap.push_back({0, w});
+  auto cmp = [](const std::pair<int64_t, int>& a, const std::pair<int64_t, int>& b) { return a > b; };
+  std::make_heap(heap.begin(), heap.end(), cmp);
+  std::vector<int32_t> owner(n);
+  std::vector<int32_t> count(nwarps, 0);
+  for (int q = 0; q < n; q++) {
+    std::pop_heap(heap.begin(), heap.end(), cmp);
+    auto& top = heap.back();
+    owner[q] = top.second;
+    count[top.second]++;
+    top.first += cost[order[q]];
+    std::push_heap(heap.begin(), heap.end(), cmp);
+  }
+  woff.assign(nwarps + 1, 0);
+  for (int w = 0; w < nwarps; w++) woff[w + 1] = woff[w] + count[w];
+  witem.assign(n, 0);
+  std::vector<int32_t> fill(woff.begin(), woff.end() - 1);
+  for (int q = 0; q < n; q++) witem[fill[owner[q]]++] = order[q];
+}
+
 void plan_tc(int n, const std::vector<Leaf>& leaves, const std::vector<int64_t>& body_off, TcPlan& tp) {
   const int nl = (int)leaves.size();
   const int TR = 256;

@@ -155,6 +155,13 @@ inline int chunk_cols(int ntp, int esz, int stage_bytes) {
   const int c = (stage_bytes / (ntp * esz)) / 16 * 16;
   return c < 128 ? c : 128;
 }
+// Static schedule of one phase's items over nwarps warps: longest
+// processing time first -- items in decreasing cost, each to the warp with
+// the least work so far (ties to the lower warp); a warp keeps its items in
+// that order.  woff (nwarps + 1) and witem are its CSR lists.
+void plan_warp_schedule(const std::vector<int64_t>& cost, int nwarps, std::vector<int32_t>& woff,
+                        std::vector<int32_t>& witem);
+
 // ---- tensor-core plan of the ensemble product ---------------------------
 // Both contractions as D (64 members x N) = A (64 x K) * B^T with B (N x K)
 // from the factor store: phase 2 N = the rows of a row-group tile (<= 256),

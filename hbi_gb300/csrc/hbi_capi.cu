@@ -199,6 +199,7 @@ struct hbi_lhp_s {
   int32_t* d_midx = nullptr;
   int32_t *d_grow0 = nullptr, *d_gndl = nullptr, *d_gnch = nullptr, *d_gpoff = nullptr;
   int32_t *d_row_fc = nullptr, *d_fc_ptr = nullptr, *d_fc_group = nullptr;
+  int32_t *d_fcb_ptr = nullptr, *d_fcb_base = nullptr;
   int32_t *d_w1off = nullptr, *d_w1item = nullptr, *d_w2off = nullptr, *d_w2item = nullptr;
   int* d_err = nullptr;
   double *d_x = nullptr, *d_y = nullptr;
@@ -557,7 +558,7 @@ extern "C" int hbi_construct_lh(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* 
   std::vector<int64_t> boff(lf->leaves.size());
   for (size_t i = 0; i < boff.size(); i++) boff[i] = lf->off[i];
   StreamPlan& P = h->plan;
-  plan_stream(c->nd, lf->leaves, boff, 16 / esz, P);
+  plan_stream(c->nd, lf->leaves, boff, 16 / esz, P, stream_stage_bytes());
   const size_t vbytes = (size_t)P.vstore * esz, ubytes = (size_t)P.ustore * esz;
   h->store_bytes = vbytes + ubytes;
   CK(cudaMalloc(&h->d_vstore, std::max<size_t>(vbytes, 16)));
@@ -585,6 +586,8 @@ extern "C" int hbi_construct_lh(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* 
   CK(upload(&h->d_row_fc, G.row_fc, st));
   CK(upload(&h->d_fc_ptr, G.fc_ptr, st));
   CK(upload(&h->d_fc_group, G.fc_group, st));
+  CK(upload(&h->d_fcb_ptr, P.fcb_ptr, st));
+  CK(upload(&h->d_fcb_base, P.fcb_base, st));
   CK(dalloc(&h->d_cnt, (size_t)P.ncg));
   CK(cudaMemset(h->d_cnt, 0, sizeof(int) * std::max<int64_t>(P.ncg, 1)));
   CK(dalloc(&h->d_err, 1));
@@ -611,6 +614,7 @@ extern "C" int hbi_construct_lh(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* 
   m.gpart = h->d_gpart;
   m.grow0 = h->d_grow0; m.gndl = h->d_gndl; m.gnch = h->d_gnch; m.gpoff = h->d_gpoff;
   m.row_fc = h->d_row_fc; m.fc_ptr = h->d_fc_ptr; m.fc_group = h->d_fc_group;
+  m.fcb_ptr = h->d_fcb_ptr; m.fcb_base = h->d_fcb_base;
   m.scale = 1.0;
   m.skip = nullptr;
   m.err = h->d_err;
@@ -651,6 +655,7 @@ extern "C" int hbi_free_lh(hbi_lhp* h) {
                   h->d_gpart, (void*)h->d_midx, (void*)h->d_grow0, (void*)h->d_gndl, (void*)h->d_gnch,
                   (void*)h->d_gpoff, (void*)h->d_row_fc, (void*)h->d_fc_ptr, (void*)h->d_fc_group, (void*)h->d_err,
                   (void*)h->d_w1off, (void*)h->d_w1item, (void*)h->d_w2off, (void*)h->d_w2item,
+                  (void*)h->d_fcb_ptr, (void*)h->d_fcb_base,
                   (void*)h->d_x, (void*)h->d_y})
     if (p) cudaFree(p);
   delete h;
@@ -666,13 +671,13 @@ extern "C" int hbi_lh_info(const hbi_lhp* h, int64_t* fe, int64_t* sb, double* a
 }
 
 extern "C" int hbi_adot_lattice_hyp_phase_dev(double* d_au, hbi_lhp* h, const double* d_u, void* stream, int phase) {
-  if (!h || !d_u || (phase != 1 && !d_au) || phase < 0 || phase > 2)
+  if (!h || !d_u || ((phase == 0 || phase == 3) && !d_au) || phase < 0 || phase > 3)
     return fail(HBI_ERR_ARG, "hbi_adot_lattice_hyp_phase_dev: bad arguments");
   cudaStream_t st = stream ? (cudaStream_t)stream : h->ctl->stream;
-  if (phase != 2) launch_phase1(&h->md, 1, d_u, h->ctl->sm_count, st);
-  if (phase != 1) {
+  if (phase == 0 || phase == 1) launch_phase1(&h->md, 1, d_u, h->ctl->sm_count, st);
+  if (phase == 0 || phase == 2) launch_phase2(&h->md, 1, d_u, h->ctl->sm_count, st);
+  if (phase == 0 || phase == 3) {
     double* ys[2] = {d_au, nullptr};
-    launch_phase2(&h->md, 1, d_u, h->ctl->sm_count, st);
     launch_phase3_plain(&h->md, 1, ys, st);
   }
   CK(cudaGetLastError());
@@ -741,9 +746,10 @@ extern "C" int hbi_lh_phase_bytes(const hbi_lhp* h, double* p1, double* p2) {
     if (L.ltmtx == 1) { v += (double)L.kt * L.ndt; rest += (double)L.kt * L.ndl; }
     else rest += (double)L.ndl * L.ndt;
   }
-  // phase 1 reads V and x; phase 2 reads U, dense blocks and x, writes y
+  // phase 1 reads V and x; phase 2 reads U, the dense blocks and (gathered)
+  // x; phase 3 writes y (n x 8 bytes, in neither figure)
   if (p1) *p1 = v * esz + (double)h->n * 8;
-  if (p2) *p2 = rest * esz + (double)h->n * 8 * 2;
+  if (p2) *p2 = rest * esz + (double)h->n * 8;
   return HBI_OK;
 }
 
@@ -1100,7 +1106,7 @@ extern "C" int hbi_plan_emulate(int n, int nleaf, const int* lv6, const double* 
   }
   std::vector<double> z(std::max<int64_t>(P.zlen, 1), 0.0), part(std::max<int64_t>(P.plen1, 1), 0.0);
   for (const S1Item& it : P.p1) {
-    if (it.ncols < 1 || it.ntp % vec || it.ntp > 32 * vec || !chunks_fit(it.ntp, esz) || it.soff % vec ||
+    if (it.ncols < 1 || it.ntp % vec || it.ntp > 32 * vec || !chunks_fit(it.ntp, esz) || it.cc != chunk_cols(it.ntp, esz, 8192) || it.soff % vec ||
         it.soff + (int64_t)it.ncols * it.ntp > P.vstore || it.x0 < 0 || it.x0 + it.nt > n || it.nt > it.ntp ||
         it.z0 < 0 || it.z0 + it.ncols > P.zlen ||
         (it.ntile > 1 && (it.cg < 0 || it.cg >= P.ncg || it.poff < 0 ||
@@ -1122,7 +1128,7 @@ extern "C" int hbi_plan_emulate(int n, int nleaf, const int* lv6, const double* 
       }
   std::vector<double> gp(std::max<int64_t>(P.plen2, 1), 0.0);
   for (const S2Item& it : P.p2) {
-    if (it.ncols < 1 || it.ntp % vec || it.ntp > 32 * vec || !chunks_fit(it.ntp, esz) || it.soff % vec ||
+    if (it.ncols < 1 || it.ntp % vec || it.ntp > 32 * vec || !chunks_fit(it.ntp, esz) || it.cc != chunk_cols(it.ntp, esz, 8192) || it.soff % vec ||
         it.soff + (int64_t)it.ncols * it.ntp > P.ustore || it.nr > it.ntp || it.m0 < 0 ||
         it.m0 + (int64_t)it.ncols > (int64_t)P.midx.size() || it.pout < 0 || it.pout + it.nr > P.plen2)
       return fail(HBI_ERR_STATE, "phase-2 item out of bounds");
@@ -1139,12 +1145,20 @@ extern "C" int hbi_plan_emulate(int n, int nleaf, const int* lv6, const double* 
   }
   const GroupPlan& G = P.gp;
   for (int r = 0; r < n; r++) {
-    double t = 0.0;
+    double t = 0.0, t2 = 0.0;
     const int f = G.row_fc[r];
     for (int e = G.fc_ptr[f]; e < G.fc_ptr[f + 1]; e++) {
       const int g = G.fc_group[e];
+      if (P.gnch[g] > 1) return fail(HBI_ERR_STATE, "more than one partial per group");
       for (int c = 0; c < P.gnch[g]; c++) t += gp[P.gpoff2[g] + (int64_t)c * G.gndl[g] + r - G.grow0[g]];
     }
+    // the kernels' flat lists give the same terms in the same order
+    for (int e = P.fcb_ptr[f]; e < P.fcb_ptr[f + 1]; e++) {
+      const int64_t q = (int64_t)P.fcb_base[e] + r;
+      if (q < 0 || q >= P.plen2) return fail(HBI_ERR_STATE, "phase-3 partial out of bounds");
+      t2 += gp[q];
+    }
+    if (t2 != t) return fail(HBI_ERR_STATE, "phase-3 lists disagree");
     y[r] = t;
   }
   if (stats) {

@@ -67,6 +67,7 @@ struct MatDev {            // one H-matrix on the device
   // phase 3: rows -> covering row groups -> their column chunks
   const int32_t *grow0, *gndl, *gnch, *gpoff;
   const int32_t *row_fc, *fc_ptr, *fc_group;
+  const int32_t *fcb_ptr, *fcb_base;  // per fine range: gpart offsets (+ row) of its non-empty groups
   double scale;            // result multiplier (1/ds0 for 3dph, else 1)
   const int* skip;         // when non-null and nonzero, phases 1-2 do nothing
   int* err;                // set to nonzero when a bulk copy did not arrive in time

@@ -26,19 +26,25 @@ void set_tableau(const double* B, const double* C, const double* DC) {
   cudaMemcpyToSymbol(cDC, DC, sizeof(double) * 6);
 }
 
-// phase 3: y(r) = scale * sum over the groups covering row r, coarse to fine
+// phase 3: y(r) = scale * sum over the groups covering row r, coarse to
+// fine.  The partials' offsets come from one flat list per fine range, so the
+// loads of a row are independent of one another (three levels of latency
+// whatever the tree depth); eight of them in flight at a time.
 template <typename Acc>
 __device__ __forceinline__ double group_sum(const MatDev& m, int r) {
   const Acc* gp = (const Acc*)m.gpart;
   const int f = __ldg(&m.row_fc[r]);
-  const int e0 = __ldg(&m.fc_ptr[f]), e1 = __ldg(&m.fc_ptr[f + 1]);
+  const int e0 = __ldg(&m.fcb_ptr[f]), e1 = __ldg(&m.fcb_ptr[f + 1]);
   Acc s = 0;
-  for (int e = e0; e < e1; e++) {
-    const int g = __ldg(&m.fc_group[e]);
-    const int ndl = __ldg(&m.gndl[g]), nch = __ldg(&m.gnch[g]);
-    const Acc* q = gp + __ldg(&m.gpoff[g]) + (r - __ldg(&m.grow0[g]));
-    for (int c = 0; c < nch; c++) s += __ldcg(q + (size_t)c * ndl);
+  int e = e0;
+  for (; e + 8 <= e1; e += 8) {
+    Acc v[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) v[u] = __ldcg(gp + __ldg(&m.fcb_base[e + u]) + r);
+#pragma unroll
+    for (int u = 0; u < 8; u++) s += v[u];
   }
+  for (; e < e1; e++) s += __ldcg(gp + __ldg(&m.fcb_base[e]) + r);
   return (double)s * m.scale;
 }
 

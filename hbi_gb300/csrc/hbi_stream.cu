@@ -151,13 +151,6 @@ __device__ void drain(uint64_t* bar, int c_seq, int p_seq) {
   __syncwarp();
 }
 
-// as chunk_cols (hbi_structure.hpp): whole columns in SB bytes, a multiple of
-// 16, at most 128
-template <int SB>
-__device__ __forceinline__ int chunk_cols_dev(int ntp, int esz) {
-  return min((SB / (ntp * esz)) / 16 * 16, kMaxCols);
-}
-
 // arrival count with release (prior writes of the warp, ordered by the
 // __syncwarp before it) and acquire (the partials of the other tiles)
 __device__ __forceinline__ int arrive_acq_rel(int* p) {
@@ -241,7 +234,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
   S1ItemDev Dp = desc(p_it), Dpn = desc(p_itn);
   auto produce = [&]() {
     if (p_it >= ntot) return;
-    const int nc = min(chunk_cols_dev<SB>(Dp.ntp, ESZ), Dp.ncols - p_c0);
+    const int nc = min(Dp.cc, Dp.ncols - p_c0);
     const int s = p_seq % NS;
     if (lane == 0) {
       const uint32_t bytes = (uint32_t)(nc * Dp.ntp * ESZ);
@@ -306,7 +299,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
       drain<NS>(R.bar, c_seq, p_seq);
       return;
     }
-    const int nc = min(chunk_cols_dev<SB>(Dc.ntp, ESZ), Dc.ncols - c_c0);
+    const int nc = min(Dc.cc, Dc.ncols - c_c0);
     const T* st = (const T*)(R.buf + s * SB);
     const int nq = Dc.ntp / VEC;
     const int lw = log2ceil(nq), LW = 1 << lw, CS = 32 >> lw;
@@ -461,7 +454,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
 #pragma unroll
     for (int i = 0; i < KP; i++) pd.idx[i] = 0;
     if (p_it >= ntot) return;
-    const int nc = min(chunk_cols_dev<SB>(Dp.ntp, ESZ), Dp.ncols - p_c0);
+    const int nc = min(Dp.cc, Dp.ncols - p_c0);
     const int s = p_seq % NS;
     const MatDev& PM = p_it < n0 ? m0 : m1;
     if (lane == 0) {
@@ -518,7 +511,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
       drain<NS>(R.bar, c_seq, p_seq);
       return;
     }
-    const int nc = min(chunk_cols_dev<SB>(Dc.ntp, ESZ), Dc.ncols - c_c0);
+    const int nc = min(Dc.cc, Dc.ncols - c_c0);
     const T* st = (const T*)(R.buf + s * SB);
     // this chunk's multipliers to shared memory; start the next chunk's gather
 #pragma unroll

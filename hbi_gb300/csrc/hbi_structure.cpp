@@ -363,7 +363,7 @@ void plan_chains(int n, const std::vector<Leaf>& leaves, ChainPlan& cp) {
 }
 
 void plan_stream(int n, const std::vector<Leaf>& leaves, const std::vector<int64_t>& body_off, int vec,
-                 StreamPlan& sp) {
+                 StreamPlan& sp, int stage_bytes) {
   const int nl = (int)leaves.size();
   const int tr = 32 * vec;
   sp = StreamPlan();
@@ -414,6 +414,7 @@ void plan_stream(int n, const std::vector<Leaf>& leaves, const std::vector<int64
       it.tile = t;
       it.ntile = ntile;
       it.poff = ntile > 1 ? (int32_t)poff0 : -1;
+      it.cc = chunk_cols(ntp, 16 / vec, stage_bytes);
       sp.p1.push_back(it);
       voff += (int64_t)ncols * ntp;
     }
@@ -479,12 +480,24 @@ void plan_stream(int n, const std::vector<Leaf>& leaves, const std::vector<int64
       it.nr = nr;
       it.m0 = m0;
       it.pout = (int32_t)(sp.gpoff2[g] + t * tr);
+      it.cc = chunk_cols(ntp, 16 / vec, stage_bytes);
       sp.p2.push_back(it);
       uoff += (int64_t)ncols * ntp;
     }
   }
   while (sp.midx.size() % 4) sp.midx.push_back(0);
   sp.midx.resize(sp.midx.size() + 256, 0);  // chunk copies may read a whole chunk's worth past a group
+  // phase-3 lists: one partial per non-empty covering group
+  const int nf = (int)gp.fc_ptr.size() - 1;
+  sp.fcb_ptr.assign(nf + 1, 0);
+  for (int f = 0; f < nf; f++) {
+    for (int e = gp.fc_ptr[f]; e < gp.fc_ptr[f + 1]; e++) {
+      const int g = gp.fc_group[e];
+      if (sp.gnch[g] == 0) continue;
+      sp.fcb_base.push_back(sp.gpoff2[g] - gp.grow0[g]);
+    }
+    sp.fcb_ptr[f + 1] = (int32_t)sp.fcb_base.size();
+  }
   sp.ustore = round_up(uoff, vec);
   sp.plen2 = p2off;
   // big items first, for the static warp schedule

@@ -122,14 +122,14 @@ struct S1Item {
   int32_t cg;              // column group (arrival counter) when ntile > 1
   int32_t tile, ntile;     // row tile of the column group, tiles of the group
   int32_t poff;            // phase-1 partials of the group (ntile x ncols)
-  int32_t pad;
+  int32_t cc;              // columns per streamed chunk (chunk_cols for the kernels' stage size)
 };
 struct S2Item {
   int64_t soff;            // element offset of the region in the U store
   int32_t ncols, ntp, nr;  // columns, padded rows, valid rows
   int32_t m0;              // multiplier index (into midx) of column 0; a multiple of 4
   int32_t pout;            // partial row sums: gpart[pout .. pout+nr)
-  int32_t pad;
+  int32_t cc;              // columns per streamed chunk
 };
 struct SegCopy {           // conversion of one column segment from the FP64 body
   int64_t dst, src;        // element offsets (dst in the V or U store)
@@ -145,6 +145,10 @@ struct StreamPlan {
   GroupPlan gp;                      // row groups, fine ranges
   std::vector<int32_t> gnch;         // partial columns per row group (1)
   std::vector<int32_t> gpoff2;       // partial offset per row group
+  // phase 3: fine range f -> fcb_base[fcb_ptr[f] .. fcb_ptr[f+1]), the
+  // partial of row r in each non-empty covering group at fcb_base + r,
+  // coarse to fine
+  std::vector<int32_t> fcb_ptr, fcb_base;
   std::vector<SegCopy> vcopy, ucopy; // conversion maps
   int64_t factor_elems = 0;
 };
@@ -197,7 +201,9 @@ void plan_tc(int n, const std::vector<Leaf>& leaves, const std::vector<int64_t>&
 
 // body_off: element offset of each leaf in the HACApK FP64 body (low rank:
 // [V ndt x kt][U ndl x kt] column-major; dense a1(ndt, ndl))
+// stage_bytes: the phase kernels' shared-memory stage (8 KB or 16 KB), which
+// sets each item's chunk width cc
 void plan_stream(int n, const std::vector<Leaf>& leaves, const std::vector<int64_t>& body_off, int vec,
-                 StreamPlan& sp);
+                 StreamPlan& sp, int stage_bytes = 8192);
 
 }  // namespace hbi

@@ -134,10 +134,12 @@ int hbi_adot_lattice_hyp_dev(double* d_au, hbi_lhp* st_LHp, const double* d_u, v
 int hbi_adot_lattice_hyp_noalloc(double* d_au, hbi_lhp* st_LHp, const double* d_u, void* stream);
 
 /* one phase of the product on device arrays: phase 1 forms z = V^T u for the
- * low-rank leaves, phase 2 forms au from U z and the dense leaves (phase 2
- * reads the z of the last phase 1); phase 0 runs both.  For kernel timing. */
+ * low-rank leaves, phase 2 forms the row groups' partial sums of U z and of
+ * the dense leaves (from the z of the last phase 1), phase 3 sums them into
+ * au; phase 0 runs all three.  For kernel timing. */
 int hbi_adot_lattice_hyp_phase_dev(double* d_au, hbi_lhp* st_LHp, const double* d_u, void* stream, int phase);
-/* algorithmic bytes of each phase (factor bytes + vector bytes) */
+/* algorithmic bytes of phases 1 (V factors + u) and 2 (U factors, dense
+ * blocks + u); the product adds ndc x 8 bytes for au (phase 3) */
 int hbi_lh_phase_bytes(const hbi_lhp* lh, double* phase1, double* phase2);
 
 /* HACApK_entry_ij (m_HACApK_calc_entry_ij.f90:24-90) evaluated on the GPU for

@@ -105,7 +105,7 @@ class Clocks:
 # DRAM bytes (read + write) per launch of the phase kernels on the c2 shear
 # H-matrix, from the ncu capture summarised in
 # profiles/matvec_p1_p2_c2_256x256_f32.md (FP32 store)
-NCU_TRAFFIC = {"f32": {"phase1": 329.8e6, "phase2": 379.0e6}}
+NCU_TRAFFIC = {"f32": {"phase1": 330.0e6, "phase2": 378.6e6}}
 
 
 def run_cycles(args, w, lf_s, lf_n, ctl_s, ctl_n, lodc, y0, p):

@@ -127,18 +127,20 @@ struct Ring {
   }
 };
 
-// wait for a stage's phase `parity`; all lanes acquire.  Returns false (and
-// records the error) when the copy did not arrive in time.
+// wait for a stage's phase `parity`; all lanes poll together (the loop stays
+// converged) and acquire.  Returns false (and records the error) when the
+// copy did not arrive within kWaitCycles.
 __device__ __forceinline__ bool stage_ready(uint64_t* bar, uint32_t parity, int* err) {
-  int ok = 1;
-  if ((threadIdx.x & 31) == 0) ok = mbar_wait_bounded(bar, parity) ? 1 : 0;
-  ok = __shfl_sync(0xffffffffu, ok, 0);
-  if (!ok) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const long long t0 = clock64();
+  bool ok;
+  while (!(ok = mbar_try_wait(bar, parity)))
+    if (clock64() - t0 > kWaitCycles) break;
+  // a completed phase stays completed until this warp refills the stage, so
+  // every lane saw the same answer
+  if (!__all_sync(0xffffffffu, ok)) {
     if ((threadIdx.x & 31) == 0 && err) atomicExch(err, 1);
     return false;
-  }
-  // the phase has completed: these waits return at once
-  while (!mbar_try_wait(bar, parity)) {
   }
   return true;
 }
@@ -313,14 +315,26 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
       // column r0 + L % BF
       for (int r0 = 0; r0 < nc; r0 += BF) {
         Acc p[BF];
+        if (nq == 32 && r0 + BF <= nc) {
+          // a full block of BF full-height columns: no predicates
 #pragma unroll
-        for (int u = 0; u < BF; u++) {
-          p[u] = 0;
-          if (r0 + u < nc && j < nq) {
+          for (int u = 0; u < BF; u++) {
             Acc a[VEC];
-            lds16(st + (r0 + u) * Dc.ntp + j * VEC, a);
+            lds16(st + (r0 + u) * (32 * VEC) + lane * VEC, a);
+            p[u] = a[0] * xc[0];
 #pragma unroll
-            for (int v = 0; v < VEC; v++) p[u] += a[v] * xc[v];
+            for (int v = 1; v < VEC; v++) p[u] += a[v] * xc[v];
+          }
+        } else {
+#pragma unroll
+          for (int u = 0; u < BF; u++) {
+            p[u] = 0;
+            if (r0 + u < nc && j < nq) {
+              Acc a[VEC];
+              lds16(st + (r0 + u) * Dc.ntp + j * VEC, a);
+#pragma unroll
+              for (int v = 0; v < VEC; v++) p[u] += a[v] * xc[v];
+            }
           }
         }
 #pragma unroll

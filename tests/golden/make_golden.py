@@ -7,7 +7,10 @@ against fixed numbers on every machine:
 
   * cluster structure of a 16 x 8 3dph mesh: lod and the leaf list;
   * 64 kernel entries each for 2dvs (n=256), 3dph (16 x 8) and 3dnt (rough
-    6 x 3 km fault, 24 x 12 x 2 triangles), shear and normal;
+    6 x 3 km fault, 24 x 12 x 2 triangles), shear and normal; the same for
+    2dph (600 elements dipping 30 degrees from the surface), 2dn (600
+    elements on a seeded bent fault) and 3dht (the 3dnt fault buried 0.5 km
+    in a half space);
   * derivs and one rkck step of the 2dvs system (n=256, ACA eps 1e-6, aging
     law, b tapering below 15 km) from its steady initial state.
 
@@ -39,7 +42,7 @@ def main():
     out["struct_lod"] = lod
     out["struct_leaves"] = np.array(leaves, dtype=np.int32)
     # entries
-    for kind in ("2dvs", "3dph", "3dnt"):
+    for kind in ("2dvs", "3dph", "3dnt", "2dph", "2dn", "3dht"):
         prob, n, g, w, eps = case(kind, 256 if kind == "2dvs" else None)
         ii = rng.integers(1, n + 1, 64)
         jj = rng.integers(1, n + 1, 64)

@@ -26,7 +26,7 @@ def test_oracle_reproduces_golden_structure(oracle):
     assert np.array_equal(np.array(leaves, dtype=np.int32), G["struct_leaves"])
 
 
-@pytest.mark.parametrize("kind", ["2dvs", "3dph", "3dnt"])
+@pytest.mark.parametrize("kind", ["2dvs", "3dph", "3dnt", "2dph", "2dn", "3dht"])
 def test_oracle_reproduces_golden_entries(oracle, kind):
     prob, n, g, w, eps = case(kind, 256 if kind == "2dvs" else None)
     ij = G[f"entry_{kind}_ij"]
@@ -47,7 +47,7 @@ def test_library_structure_matches_golden():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kind", ["2dvs", "3dph", "3dnt"])
+@pytest.mark.parametrize("kind", ["2dvs", "3dph", "3dnt", "2dph", "2dn", "3dht"])
 def test_gpu_entries_match_golden(kind):
     prob, n, g, w, eps = case(kind, 256 if kind == "2dvs" else None)
     ij = G[f"entry_{kind}_ij"]
@@ -60,7 +60,9 @@ def test_gpu_entries_match_golden(kind):
         if kind == "2dvs":
             assert np.array_equal(got, ref)
         else:
-            assert np.max(np.abs(got - ref)) <= 1e-11 * np.max(np.abs(ref))
+            # 3dht: rounding sensitivity of the free-surface correction (see test_gpu_parity)
+            tol = 2e-6 if kind == "3dht" else 1e-11
+            assert np.max(np.abs(got - ref)) <= tol * np.max(np.abs(ref))
 
 
 @pytest.mark.gpu

@@ -42,6 +42,7 @@ EXPORTS = [
     "hbi_mlp_train", "hbi_mlp_predict", "hbi_plan_emulate", "hbi_umma_probe",
     "hbi_ens_create", "hbi_ens_free", "hbi_ens_set_state", "hbi_ens_get_state", "hbi_ens_run",
     "hbi_tc_plan_emulate", "hbi_ens_use_tensor_cores", "hbi_cycle_restart", "hbi_restart_point",
+    "hbi_plan_warp_schedule",
 ]
 
 
@@ -566,6 +567,18 @@ class MLP:
 
     def __del__(self):
         self.close()
+
+
+def plan_warp_schedule(cost, nwarps):
+    """The product kernels' static warp schedule (hbi_plan_warp_schedule):
+    returns (woff[nwarps + 1], witem[n])."""
+    cost = np.ascontiguousarray(cost, dtype=np.int64)
+    woff = np.zeros(nwarps + 1, dtype=np.int32)
+    witem = np.zeros(max(len(cost), 1), dtype=np.int32)
+    _check(lib().hbi_plan_warp_schedule(len(cost), cost.ctypes.data_as(_i64p), int(nwarps),
+                                        woff.ctypes.data_as(_ip), witem.ctypes.data_as(_ip)),
+           "hbi_plan_warp_schedule")
+    return woff, witem[:len(cost)]
 
 
 def plan_emulate(n, leaves, body, vec, x):

@@ -1190,6 +1190,17 @@ int64_t tc_offset(int np, int n, int k) {
 // with the factors rounded to BF16 hi + lo as the device stores them; checks
 // every bound the kernels rely on.  stats (4): items of phase 1 and 2, store
 // elements of phase 1 and 2.
+extern "C" int hbi_plan_warp_schedule(int n, const int64_t* cost, int nwarps, int32_t* woff, int32_t* witem) {
+  if (n < 0 || nwarps < 1 || (n > 0 && (!cost || !witem)) || !woff)
+    return fail(HBI_ERR_ARG, "hbi_plan_warp_schedule: bad arguments");
+  std::vector<int64_t> c(cost, cost + n);
+  std::vector<int32_t> o, it;
+  plan_warp_schedule(c, nwarps, o, it);
+  std::copy(o.begin(), o.end(), woff);
+  std::copy(it.begin(), it.end(), witem);
+  return HBI_OK;
+}
+
 extern "C" int hbi_tc_plan_emulate(int n, int nleaf, const int* lv6, const double* body, const double* x, double* y,
                                    int64_t* stats) {
   if (n < 1 || nleaf < 1 || !lv6 || !body || !x || !y) return fail(HBI_ERR_ARG, "hbi_tc_plan_emulate: arguments");

@@ -430,17 +430,22 @@ __global__ void __launch_bounds__(256, 2) p2e_kernel(EnsMat A, EnsMat B, int nma
   }
 }
 
-// per (row, member): the covering groups' partial rows, coarse to fine
+// per (row, member): the covering groups' partial rows, coarse to fine, from
+// the flat per-fine-range offset list (independent loads, eight in flight)
 __device__ __forceinline__ double group_sum_e(const EnsMat& M, int r, int m) {
   const MatDev& d = M.m;
   const int f = __ldg(&d.row_fc[r]);
-  const int e0 = __ldg(&d.fc_ptr[f]), e1 = __ldg(&d.fc_ptr[f + 1]);
+  const int e0 = __ldg(&d.fcb_ptr[f]), e1 = __ldg(&d.fcb_ptr[f + 1]);
   float s = 0.f;
-  for (int e = e0; e < e1; e++) {
-    const int g = __ldg(&d.fc_group[e]);
-    if (__ldg(&d.gnch[g]) == 0) continue;
-    s += __ldcg(&M.gpart[((int64_t)__ldg(&d.gpoff[g]) + r - __ldg(&d.grow0[g])) * EM + m]);
+  int e = e0;
+  for (; e + 8 <= e1; e += 8) {
+    float v[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) v[u] = __ldcg(&M.gpart[((int64_t)__ldg(&d.fcb_base[e + u]) + r) * EM + m]);
+#pragma unroll
+    for (int u = 0; u < 8; u++) s += v[u];
   }
+  for (; e < e1; e++) s += __ldcg(&M.gpart[((int64_t)__ldg(&d.fcb_base[e]) + r) * EM + m]);
   return (double)s * d.scale;
 }
 

@@ -309,6 +309,11 @@ int hbi_mlp_predict(hbi_mlp* m, const float* x, long long n, float* out);
  * violated bound. */
 int hbi_plan_emulate(int n, int nleaf, const int* leaves6, const double* body, int vec, const double* x,
                      double* y, int64_t* stats);
+/* Host-only (no reference counterpart): the static warp schedule the product
+ * kernels walk -- n items of the given costs dealt longest-first to the
+ * least-loaded of nwarps warps.  woff[nwarps + 1] and witem[n] receive the
+ * CSR lists (warp w: witem[woff[w] .. woff[w+1])). */
+int hbi_plan_warp_schedule(int n, const int64_t* cost, int nwarps, int32_t* woff, int32_t* witem);
 
 /* ---- ensemble of simulations sharing one H-matrix pair (no reference
  * counterpart; configuration c4) -----------------------------------------

@@ -75,3 +75,24 @@ def test_tc_plan_matches_oracle_product(oracle, shape):
     y, st = H.tc_plan_emulate(n, lv, body, x)
     assert np.linalg.norm(y - ref) <= 1e-4 * np.linalg.norm(ref)
     assert st["items1"] > 0 and st["items2"] > 0
+
+
+@pytest.mark.parametrize("nwarps", [1, 7, 1824])
+def test_warp_schedule_is_balanced_permutation(nwarps):
+    """Longest-processing-time schedule of the product kernels: every item
+    exactly once, each warp's items in decreasing cost, and the busiest warp
+    within one item of the average (Graham's bound for LPT is 4/3 of the
+    optimum; this checks the weaker max <= avg + max item)."""
+    rng = np.random.default_rng(nwarps)
+    cost = np.concatenate([rng.integers(512, 300_000, 3000), rng.integers(512, 20_000, 7000)])
+    woff, witem = H.plan_warp_schedule(cost, nwarps)
+    assert woff[0] == 0 and woff[-1] == len(cost) and np.all(np.diff(woff) >= 0)
+    assert np.array_equal(np.sort(witem), np.arange(len(cost)))
+    loads = np.array([cost[witem[woff[w]:woff[w + 1]]].sum() for w in range(nwarps)])
+    assert loads.max() <= cost.sum() / nwarps + cost.max()
+    for w in range(nwarps):
+        c = cost[witem[woff[w]:woff[w + 1]]]
+        assert np.all(np.diff(c) <= 0)
+    # deterministic
+    w2, i2 = H.plan_warp_schedule(cost, nwarps)
+    assert np.array_equal(w2, woff) and np.array_equal(i2, witem)

@@ -59,10 +59,14 @@ def test_gpu_entries_match_golden(kind):
         ref = G[key]
         if kind == "2dvs":
             assert np.array_equal(got, ref)
+        elif kind == "3dht":
+            # rounding sensitivity of the free-surface correction (see
+            # test_gpu_parity): absolute noise on the scale of the shear
+            # self-interaction, so normal entries are measured against it too
+            scale = np.max(np.abs(G[f"entry_{kind}_s"]))
+            assert np.max(np.abs(got - ref)) <= 2e-6 * scale
         else:
-            # 3dht: rounding sensitivity of the free-surface correction (see test_gpu_parity)
-            tol = 2e-6 if kind == "3dht" else 1e-11
-            assert np.max(np.abs(got - ref)) <= tol * np.max(np.abs(ref))
+            assert np.max(np.abs(got - ref)) <= 1e-11 * np.max(np.abs(ref))
 
 
 @pytest.mark.gpu

@@ -2,6 +2,8 @@
 builder (hbi_cluster_structure in libhbigpu.so, no GPU needed) against the
 oracle restatement of HACApK (m_HACApK_base.f90:2372-2460, 2937-2995,
 3114-3166, 3191-3333)."""
+import math
+
 import numpy as np
 import pytest
 
@@ -124,3 +126,23 @@ def test_restart_point_follows_the_reference_rule(tmp_path):
     assert x == 200000.0
     e, h = float(_fort_e(0.45)), float(_fort_e(210.0))
     assert abs(dt - min(2 * h, float(np.float32(0.9)) * h * e ** float(np.float32(-0.2)))) <= 1e-12 * dt
+
+
+def test_2d_meshes_follow_the_reference_builders():
+    """coordinate2dph (main_LH.f90:1720-1737): element i from (i-1) ds0 to
+    i ds0 along the dip; coordinate2dn (:1739-1750): lengths, angles and
+    midpoints of given element ends."""
+    n, ds0, dip = 5, 0.25, 30.0
+    xel, xer, yel, yer, xcol, ycol, ang, ds = mesh.mesh_2dph(n, ds0, dip)
+    c, s = math.cos(dip * mesh.PI / 180), math.sin(dip * mesh.PI / 180)
+    for i in range(1, n + 1):
+        assert xel[i - 1] == (i - 1) * ds0 * c and xer[i - 1] == i * ds0 * c
+        assert yel[i - 1] == (i - 1) * ds0 * s and yer[i - 1] == i * ds0 * s
+        assert xcol[i - 1] == 0.5 * (xel[i - 1] + xer[i - 1]) and ycol[i - 1] == 0.5 * (yel[i - 1] + yer[i - 1])
+        assert ang[i - 1] == math.atan2(yer[i - 1] - yel[i - 1], xer[i - 1] - xel[i - 1])
+    assert np.all(ds == ds0)
+    ends = mesh.bent_fault_2d(64, 10.0, 1.0, 30.0, seed=4, rough=0.2)
+    assert all(np.array_equal(a, b) for a, b in zip(ends, mesh.bent_fault_2d(64, 10.0, 1.0, 30.0, seed=4, rough=0.2)))
+    xel, xer, yel, yer, xcol, ycol, ang, ds = mesh.mesh_2dn(*ends)
+    assert np.allclose(ds, 10.0 / 64, rtol=1e-12)
+    assert np.array_equal(xel[1:], xer[:-1]) and np.array_equal(yel[1:], yer[:-1])  # a connected trace

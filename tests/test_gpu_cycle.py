@@ -184,3 +184,60 @@ def test_cycle_restart_continues_a_run(system, tmp_path):
     assert ks[:101] == list(range(101)) and ks[101] == 101 and len(set(ks)) == len(ks)
     # a limit already reached runs nothing
     assert b.run(t_limit=T)["stop_name"] == "tlimit"
+
+
+@pytest.mark.parametrize("kind", ["2dph", "3dht"])
+def test_cycle_with_two_matrices_follows_oracle(oracle, kind):
+    """The loop on the newer problem kinds -- 2D edge dislocations in a half
+    space and triangles in a half space -- with both the shear and the normal
+    H-matrix (sigma evolves), against the oracle's loop on the same FP64
+    factors: the interseismic steps (80 for 2dph, whose patch starts to
+    nucleate near step 105; 150 for 3dht), times and step sizes within 1e-6
+    relative, rejection counts equal."""
+    from gpu_cases import case, product_geometry
+    prob, n, g, w, eps = case(kind)
+    lhs, keep = [], []
+    Ho = []
+    for v in ("s", "n"):
+        ctl = H.Ctl(n)
+        lf = H.LeafMtxp(ctl, product_geometry(prob, n, g, w, v), eps)
+        lhs.append(H.LHp(lf, ctl, "f64"))
+        off, body = lf.body()
+        Ho.append(oracle.HMatrix.from_body(n, lf.leaves(), off, body))
+        keep.append((ctl, lf))
+    ndc, lodc = H.HACApK_gen_lattice_vector(keep[0][0])
+    rng = np.random.default_rng(5)
+    idx = lodc - 1
+    mid = np.abs(np.arange(n) - n / 2) < 0.3 * n
+    a = np.full(n, 0.01)
+    b = np.where(mid, 0.015, 0.006)[idx]
+    dc = np.full(n, 0.01)
+    f0 = np.full(n, 0.6)
+    vpl = np.full(n, 1e-9)
+    vel = (1e-9 * (1 + 0.01 * rng.uniform(-1, 1, n)))[idx]
+    sig = np.full(n, 50.0)
+    vref = float(np.float32(1e-6))
+    psi_ss = f0 - b * np.log(vel / vref)
+    tau = a * sig * np.arcsinh(vel / (2 * vref) * np.exp(psi_ss / a))
+    psi = a * np.log(2 * vref / vel * np.sinh(tau / sig / a))
+    y0 = np.empty(3 * n)
+    y0[0::3], y0[1::3], y0[2::3] = psi, tau, sig
+    evlaw = 1 if kind == "3dht" else 0
+    ds = np.full(n, 1.0)
+    steps = 80 if kind == "2dph" else 150
+    R = oracle.RSF(n, Ho[0], Ho[1], evlaw=evlaw, a=a, b=b, dc=dc, f0=f0, vplv=vpl)
+    stop_o, rec, ev_o, y_o, vel_o, slip_o = oracle.cycle(R, y0, vel, ds, steps, eps_r=1e-6, tmax_yr=1500.0)
+    rk = H.RK(lhs[0], lhs[1], evlaw=evlaw, a=a, b=b, dc=dc, f0=f0, vpl=vpl)
+    rk.set_state(y0)
+    c = H.Cycle(rk, vel, ds, eps_r=1e-6, tmax_yr=1500.0)
+    st = c.run(k_limit=steps)
+    assert st["k"] == steps and len(rec) == steps
+    tr = c.trace()
+    acc = tr[tr[:, 4] == 1]
+    assert np.allclose(acc[:steps, 1], rec[:steps, 1], rtol=1e-6, atol=0)   # x
+    assert np.allclose(acc[:steps, 2], rec[:steps, 2], rtol=1e-6, atol=0)   # accepted h
+    assert np.array_equal(acc[:steps, 7], rec[:steps, 4])                   # nrjct
+    y = rk.get_state()
+    assert np.linalg.norm(y - y_o) <= 1e-6 * np.linalg.norm(y_o)
+    c.close()
+    rk.close()

@@ -260,7 +260,8 @@ class LHp:
         return au
 
     def matvec_dev(self, d_au, d_u, stream=0, phase=0):
-        """Product on device pointers (ints), enqueued on `stream`."""
+        """Product on device pointers (ints), enqueued on `stream`; phase 1,
+        2 or 3 runs one phase of it alone (for timing), 0 the whole product."""
         _check(lib().hbi_adot_lattice_hyp_phase_dev(C.c_void_p(d_au), self.h, C.c_void_p(d_u), C.c_void_p(stream),
                                                     int(phase)), "hbi_adot_lattice_hyp_phase_dev")
 

@@ -106,7 +106,8 @@ void plan_p2_items(const std::vector<Leaf>& leaves, const GroupPlan& gp, int vec
 // The factor store is re-laid out in row tiles of up to 32*vec rows (one
 // 16-byte vector per lane, 512 bytes per column segment) so that each work
 // item of the product is ONE contiguous region, which the kernels stream into
-// shared memory in chunks of at most 16 KB by bulk asynchronous copies (TMA):
+// shared memory in chunks of one stage (8 KB or 16 KB) by bulk asynchronous
+// copies (TMA):
 //   phase 1 (z = V^T x): the low-rank leaves sharing a column cluster form a
 //     column group; item = (column group, row tile) over all its columns;
 //   phase 2 (y = U z + A x): the leaves sharing a row cluster form a row group

@@ -22,6 +22,8 @@ HBI_2DVS, HBI_3DPH, HBI_3DNR, HBI_3DNT, HBI_2DPH, HBI_2DN, HBI_3DHT = 1, 2, 3, 4
 STORE_F64, STORE_F32, STORE_BF16 = 0, 1, 2
 STORE_NAMES = {"f64": STORE_F64, "f32": STORE_F32, "bf16": STORE_BF16}
 HBI_ERR_CONVERGE = -5
+HBI_ERR_LIMIT = -6
+HBI_ERR_DEVICE = -7
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -42,7 +44,7 @@ EXPORTS = [
     "hbi_mlp_train", "hbi_mlp_predict", "hbi_plan_emulate", "hbi_umma_probe",
     "hbi_ens_create", "hbi_ens_free", "hbi_ens_set_state", "hbi_ens_get_state", "hbi_ens_run",
     "hbi_tc_plan_emulate", "hbi_ens_use_tensor_cores", "hbi_cycle_restart", "hbi_restart_point",
-    "hbi_plan_warp_schedule",
+    "hbi_plan_warp_schedule", "hbi_lh_check_error", "hbi_lh_set_wait_limit", "hbi_rk_check_error",
 ]
 
 
@@ -89,7 +91,7 @@ class Event(C.Structure):
                 ("end", C.c_double), ("moment", C.c_double), ("mw", C.c_double)]
 
 
-STOP_NAMES = {0: "none", 1: "tmax", 2: "velmax", 3: "velmin", 4: "klimit", 5: "underflow", 6: "tlimit"}
+STOP_NAMES = {0: "none", 1: "tmax", 2: "velmax", 3: "velmin", 4: "klimit", 5: "underflow", 6: "tlimit", 7: "device"}
 YEAR = 365 * 24 * 3600.0
 
 
@@ -265,6 +267,17 @@ class LHp:
         _check(lib().hbi_adot_lattice_hyp_phase_dev(C.c_void_p(d_au), self.h, C.c_void_p(d_u), C.c_void_p(stream),
                                                     int(phase)), "hbi_adot_lattice_hyp_phase_dev")
 
+    def check_error(self):
+        """hbi_lh_check_error: raises HBIError (code HBI_ERR_DEVICE) if a
+        product kernel gave up a bulk-copy wait since the last check; call
+        after the stream of matvec_dev products has been synchronised."""
+        _check(lib().hbi_lh_check_error(self.h), "hbi_lh_check_error")
+
+    def set_wait_limit(self, cycles):
+        """Test hook: bound of the product kernels' bulk-copy waits (SM clock
+        cycles; 0 = one non-blocking probe; negative = the default)."""
+        _check(lib().hbi_lh_set_wait_limit(self.h, C.c_longlong(int(cycles))), "hbi_lh_set_wait_limit")
+
     def phase_bytes(self):
         p1, p2 = C.c_double(), C.c_double()
         _check(lib().hbi_lh_phase_bytes(self.h, C.byref(p1), C.byref(p2)), "hbi_lh_phase_bytes")
@@ -396,6 +409,11 @@ class RK:
         """cudaStream_t (as int) the handle enqueues on."""
         lib().hbi_rk_stream.restype = C.c_void_p
         return lib().hbi_rk_stream(self.h) or 0
+
+    def check_error(self):
+        """Waits for the handle's stream; raises HBIError (HBI_ERR_DEVICE) if a
+        product kernel gave up a bulk-copy wait."""
+        _check(lib().hbi_rk_check_error(self.h), "hbi_rk_check_error")
 
     def attempt_async(self, h, eps):
         """Enqueue one Cash-Karp attempt; no host synchronisation."""

@@ -618,6 +618,8 @@ extern "C" int hbi_construct_lh(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* 
   m.scale = 1.0;
   m.skip = nullptr;
   m.err = h->d_err;
+  m.wait = kWaitCyclesDefault;
+  m.ncnt = (int)P.ncg;
   // static warp schedules for the grid the phase kernels get on this device:
   // one block of stream_warps_per_block() warps per SM, fewer for small operators
   {
@@ -659,6 +661,40 @@ extern "C" int hbi_free_lh(hbi_lhp* h) {
                   (void*)h->d_x, (void*)h->d_y})
     if (p) cudaFree(p);
   delete h;
+  return HBI_OK;
+}
+
+namespace hbi {
+int take_device_error(const MatDev& m) {
+  if (!m.err) return 0;
+  int flag = 0;
+  if (cudaMemcpy(&flag, m.err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return HBI_ERR_CUDA;
+  if (!flag) return 0;
+  // a warp that gave up left before its arrivals: the counters start over
+  if (cudaMemset(m.err, 0, sizeof(int)) != cudaSuccess ||
+      (m.cnt && m.ncnt > 0 && cudaMemset(m.cnt, 0, sizeof(int) * (size_t)m.ncnt) != cudaSuccess))
+    return HBI_ERR_CUDA;
+  return 1;
+}
+}  // namespace hbi
+
+static int device_error_status(const MatDev& m, const char* where) {
+  const int t = take_device_error(m);
+  if (t < 0) return fail(HBI_ERR_CUDA, "%s: reading the device error word failed", where);
+  if (t > 0)
+    return fail(HBI_ERR_DEVICE, "%s: a product kernel gave up waiting for a bulk copy; the result is invalid "
+                "(the operator's device state has been reset)", where);
+  return HBI_OK;
+}
+
+extern "C" int hbi_lh_check_error(hbi_lhp* h) {
+  if (!h) return fail(HBI_ERR_ARG, "hbi_lh_check_error: null");
+  return device_error_status(h->md, "hbi_lh_check_error");
+}
+
+extern "C" int hbi_lh_set_wait_limit(hbi_lhp* h, long long cycles) {
+  if (!h) return fail(HBI_ERR_ARG, "hbi_lh_set_wait_limit: null");
+  h->md.wait = cycles < 0 ? kWaitCyclesDefault : cycles;
   return HBI_OK;
 }
 
@@ -727,6 +763,7 @@ extern "C" int hbi_adot_lattice_hyp_noalloc(double* d_au, hbi_lhp* h, const doub
   md.z = p + b_cnt;
   md.part = p + b_cnt + b_z;
   md.gpart = p + b_cnt + b_z + b_part;
+  md.ncnt = (int)nlr;
   cudaStream_t st = stream ? (cudaStream_t)stream : h->ctl->stream;
   // the counters must start at zero; everything else is written before it is read
   CK(cudaMemsetAsync(md.cnt, 0, nlr * sizeof(int), st));
@@ -763,7 +800,7 @@ extern "C" int hbi_adot_lattice_hyp(double* au, hbi_lhp* h, hbi_ctl* c, double* 
   if (rc) return rc;
   CK(cudaMemcpyAsync(au, h->d_y, sizeof(double) * h->n, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  return HBI_OK;
+  return device_error_status(h->md, "hbi_adot_lattice_hyp");
 }
 
 // ---------------------------------------------------------------- RK45
@@ -924,9 +961,27 @@ extern "C" int hbi_rk_set_state(hbi_rk* r, const double* y) {
   CK(cudaMemcpy(r->R.y, y, sizeof(double) * 3 * r->n, cudaMemcpyHostToDevice));
   return HBI_OK;
 }
+
+// the error words of the RK handle's operators (after its stream has drained)
+static int rk_device_error(hbi_rk* r, const char* where) {
+  for (int k = 0; k < r->nmat; k++) {
+    const int rc = device_error_status(r->mats[k], where);
+    if (rc) return rc;
+  }
+  return HBI_OK;
+}
+
+extern "C" int hbi_rk_check_error(hbi_rk* r) {
+  if (!r) return fail(HBI_ERR_ARG, "hbi_rk_check_error: null");
+  CK(cudaStreamSynchronize(r->st));
+  return rk_device_error(r, "hbi_rk_check_error");
+}
+
 extern "C" int hbi_rk_get_state(hbi_rk* r, double* y) {
   if (!r || !y) return fail(HBI_ERR_ARG, "null");
   CK(cudaStreamSynchronize(r->st));
+  int rc = rk_device_error(r, "hbi_rk_get_state");
+  if (rc) return rc;
   CK(cudaMemcpy(y, r->R.y, sizeof(double) * 3 * r->n, cudaMemcpyDeviceToHost));
   return HBI_OK;
 }
@@ -983,6 +1038,8 @@ static int run_attempt(hbi_rk* r, double h, double eps, double* errmax) {
   if (rc0) return rc0;
   CK(cudaMemcpyAsync(r->h_ctl + 2, r->R.ctl + 2, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
+  int rc1 = rk_device_error(r, "Runge-Kutta attempt");
+  if (rc1) return rc1;
   double e = r->h_ctl[2];
   long long hidx;
   memcpy(&hidx, &r->h_ctl[3], sizeof(hidx));

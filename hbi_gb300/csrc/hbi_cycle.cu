@@ -7,7 +7,8 @@
 // CUDA graph per RK attempt carries the whole decision chain:
 //
 //   rk_prepare, 6 x (phase 1, phase 2, phase 3 + RK epilogue)   the attempt
-//   cycle_control   errmax, accept/reject, next h (rkqs :2296-2360)
+//   cycle_control   errmax, accept/reject, next h (rkqs :2296-2360); stops
+//                   the loop if a product kernel gave up a bulk-copy wait
 //   cycle_update    y <- ytemp, slip, slip rate, monitors, event state,
 //                   output decision, stop controls
 //   cycle_snapshot  fields into a ring slot when the step writes output
@@ -186,15 +187,28 @@ __host__ __device__ inline void proposer_features(double e, double e_prev, doubl
 namespace {
 
 __global__ void __launch_bounds__(256) cycle_control_kernel(RkDev R, CycleConst P, CycleState* S, int* flags,
-                                                            ProposerDev M) {
+                                                            ProposerDev M, const int* err0, const int* err1) {
   __shared__ double red[8];
   __shared__ int halted;
   __shared__ float feat[16], a1[128], a2[128];
   __shared__ int use_mlp;
-  if (threadIdx.x == 0) halted = S->halted;
+  if (threadIdx.x == 0) {
+    halted = S->halted;
+    // a product kernel of this attempt gave up a wait: its result is invalid,
+    // the loop stops here (the attempt is recorded as not accepted)
+    if (!halted && ((err0 && __ldcg(err0)) || (err1 && __ldcg(err1)))) {
+      S->attempt += 1;
+      S->accepted = 0;
+      S->stop = HBI_STOP_DEVICE;
+      S->halted = 1;
+      flags[0] = 1;
+      flags[1] = 1;
+      halted = 2;
+    }
+  }
   __syncthreads();
   if (halted) {
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && halted == 1) {
       S->accepted = 0;
       S->skipped = 1;
     }
@@ -694,7 +708,8 @@ void enqueue_attempt(hbi_cycle* c) {
     launch_phase2(m, nmat, xin, sm, st);
     launch_phase3_rk(c->m_rest, nmat, R, s, xout, st);
   }
-  cycle_control_kernel<<<1, 256, 0, st>>>(R, c->P, c->dS, c->dflags, c->M);
+  cycle_control_kernel<<<1, 256, 0, st>>>(R, c->P, c->dS, c->dflags, c->M, c->V.mats[0].err,
+                                          nmat == 2 ? c->V.mats[1].err : nullptr);
   cycle_update_kernel<<<c->G, 256, 0, st>>>(R, c->P, c->dS, c->dflags, c->dvel, c->dslip, c->dds, c->dpart, 0);
   cycle_snapshot_kernel<<<c->G, 256, 0, st>>>(R, c->P, c->dS, c->dvel, c->dslip, c->dislip, c->dsnap);
   cycle_record_kernel<<<1, 32, 0, st>>>(c->dS, c->dring, c->P.nrec);
@@ -1063,6 +1078,8 @@ extern "C" int hbi_cycle_run(hbi_cycle* c, long long k_limit, double t_limit, hb
   const auto t0 = std::chrono::steady_clock::now();
   const long long kl = k_limit > 0 ? k_limit : (c->prm.nstep > 0 ? c->prm.nstep : (1LL << 62));
   const double tl = t_limit > 0 ? t_limit : INFINITY;
+  if (c->last.stop == HBI_STOP_DEVICE)
+    return cfail(HBI_ERR_DEVICE, "hbi_cycle_run: the loop stopped on a device error and cannot continue");
   if (c->last.stop && c->last.stop != HBI_STOP_KLIMIT && c->last.stop != HBI_STOP_TLIMIT) {
     // a stop control already ended the loop
     if (out) {
@@ -1128,6 +1145,13 @@ extern "C" int hbi_cycle_run(hbi_cycle* c, long long k_limit, double t_limit, hb
     out->wall_s = wall_since(t0);
   }
   if (c->last.stop == HBI_STOP_UNDERFLOW) return cfail(HBI_ERR_CONVERGE, "Runge-Kutta step size underflow at x=%.17g", c->last.x);
+  if (c->last.stop == HBI_STOP_DEVICE) {
+    // clear the operators' error words and arrival counters for their next use
+    for (int k = 0; k < c->V.nmat; k++)
+      if (take_device_error(c->V.mats[k]) < 0) return cfail(HBI_ERR_CUDA, "hbi_cycle_run: device error reset");
+    return cfail(HBI_ERR_DEVICE, "hbi_cycle_run: a product kernel gave up waiting for a bulk copy at step %lld; "
+                 "the loop stopped (the operators' device state has been reset)", c->last.k + 1);
+  }
   return HBI_OK;
 }
 

@@ -635,6 +635,7 @@ struct hbi_ens_s {
   TcMat T[2]{};
   bool tc = false;
   int nmat = 1, n = 0, sm = 152;
+  int64_t ncnt_m[2] = {0, 0}, ncnt_t[2] = {0, 0};  // arrival counters of M[k] and T[k]
   std::vector<void*> allocs;
   int* hnd = nullptr;  // host-mapped done count
   cudaStream_t st = nullptr;
@@ -771,6 +772,7 @@ extern "C" int hbi_ens_create(hbi_ens** out, const hbi_rsf_params* p, hbi_lhp* l
     M.z = ealloc<float>(e, (size_t)v.zlen * EM);
     M.part = ealloc<float>(e, (size_t)v.plen1 * EM);
     M.cnt = ealloc<int>(e, (size_t)v.ncg);
+    e->ncnt_m[k] = v.ncg;
     M.gpart = ealloc<float>(e, (size_t)v.plen2 * EM);
     if (!M.z || !M.part || !M.cnt || !M.gpart) ok = false;
   }
@@ -884,6 +886,22 @@ extern "C" int hbi_ens_run(hbi_ens* e, double eps_r, double dtinit, double dtmax
     }
     out->wall_s = wall;
   }
+  // a product kernel that gave up a bulk-copy wait invalidates the run; the
+  // operators' and the ensemble's arrival counters start over
+  bool bad = false;
+  for (int k = 0; k < e->nmat; k++) {
+    const int t = take_device_error(e->M[k].m);
+    if (t < 0) return efail(HBI_ERR_CUDA, "hbi_ens_run: device error word");
+    if (t > 0) {
+      bad = true;
+      if (cudaMemset(e->M[k].cnt, 0, sizeof(int) * (size_t)std::max<int64_t>(e->ncnt_m[k], 1)) != cudaSuccess ||
+          (e->T[k].cnt &&
+           cudaMemset(e->T[k].cnt, 0, sizeof(int) * (size_t)std::max<int64_t>(e->ncnt_t[k], 1)) != cudaSuccess))
+        return efail(HBI_ERR_CUDA, "hbi_ens_run: counter reset");
+    }
+  }
+  if (bad)
+    return efail(HBI_ERR_DEVICE, "hbi_ens_run: a product kernel gave up waiting for a bulk copy; the run is invalid");
   return HBI_OK;
 }
 
@@ -932,6 +950,7 @@ extern "C" int hbi_ens_use_tensor_cores(hbi_ens* e, const hbi_leafmtxp* lf_s, co
     T.z = ealloc<float>(e, (size_t)P.zlen * EM);
     T.part = ealloc<float>(e, (size_t)P.plen1 * EM);
     T.cnt = ealloc<int>(e, (size_t)P.ncg);
+    e->ncnt_t[k] = P.ncg;
     T.gpart = e->M[k].gpart;
     T.err = e->M[k].m.err;
     if (!T.p1 || !T.p2 || !T.midx || !s1 || !s2 || !T.z || !T.part || !T.cnt)

@@ -45,6 +45,9 @@ void launch_entries(const DevBemv& b, const int* ii, const int* jj, int n, doubl
 // ---- matvec ----------------------------------------------------------------
 enum { ST_F64 = 0, ST_F32 = 1, ST_BF16 = 2 };
 
+// bound of the product kernels' bulk-copy waits: about one second of SM clock
+constexpr long long kWaitCyclesDefault = 2LL << 30;
+
 // work items of the streamed product (plan_stream in hbi_structure.cpp)
 typedef S1Item S1ItemDev;
 typedef S2Item S2ItemDev;
@@ -71,6 +74,8 @@ struct MatDev {            // one H-matrix on the device
   double scale;            // result multiplier (1/ds0 for 3dph, else 1)
   const int* skip;         // when non-null and nonzero, phases 1-2 do nothing
   int* err;                // set to nonzero when a bulk copy did not arrive in time
+  long long wait;          // bound of a stage wait in SM clock cycles (0: one non-blocking probe)
+  int ncnt;                // number of arrival counters in cnt
   // static warp schedules (hbi_structure.hpp, plan_warp_schedule) for a grid
   // of gw1 / gw2 warps: warp w walks item[off[w] .. off[w+1]) of its phase
   const int32_t *w1off, *w1item, *w2off, *w2item;
@@ -125,6 +130,11 @@ void launch_phase1(const MatDev* mats, int nmat, const double* x, int sm_count, 
 void launch_phase2(const MatDev* mats, int nmat, const double* x, int sm_count, cudaStream_t st);
 void launch_phase3_plain(const MatDev* mats, int nmat, double* const* y, cudaStream_t st);
 void launch_phase3_rk(const MatDev* mats, int nmat, const RkDev& rk, int stage, double* xnext, cudaStream_t st);
+// host: 1 when a product kernel of the operator gave up a wait since the last
+// call (the operator's error word and arrival counters are then cleared, on
+// the legacy stream: the caller has synchronised the products), 0 if not, a
+// negative HBI_ERR_CUDA on a failed copy
+int take_device_error(const MatDev& m);
 void launch_rk_prepare(const RkDev& rk, cudaStream_t st);
 void set_tableau(const double* B15, const double* C6, const double* DC6);
 // dst[dst_off[i] : +len[i]] = src[i][0 : len[i]]

@@ -19,9 +19,10 @@
 // slots once per item.  Every sum has a fixed order: results are
 // deterministic run to run.
 //
-// Waits are bounded: a stage that does not complete within ~1 s of SM clock
-// sets the operator's error word, the warp waits (bounded again) for its other
-// copies and leaves.
+// Waits are bounded: a stage that does not complete within the operator's
+// wait bound (~1 s of SM clock) sets the operator's error word, the warp waits
+// (bounded by ~1 s again) for its other copies and leaves; the host reads and
+// clears the word at its next synchronisation (take_device_error).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -35,7 +36,7 @@ namespace hbi {
 
 namespace {
 
-constexpr long long kWaitCycles = 2LL << 30;
+constexpr long long kWaitCycles = kWaitCyclesDefault;
 
 template <typename T>
 struct AccT {
@@ -61,6 +62,18 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(saddr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(ok)
       : "r"(saddr(bar)), "r"(parity)
@@ -129,15 +142,17 @@ struct Ring {
 
 // wait for a stage's phase `parity`; all lanes poll together (the loop stays
 // converged) and acquire.  Returns false (and records the error) when the
-// copy did not arrive within kWaitCycles.
-__device__ __forceinline__ bool stage_ready(uint64_t* bar, uint32_t parity, int* err) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const long long t0 = clock64();
-  bool ok;
-  while (!(ok = mbar_try_wait(bar, parity)))
-    if (clock64() - t0 > kWaitCycles) break;
-  // a completed phase stays completed until this warp refills the stage, so
-  // every lane saw the same answer
+// copy did not arrive within `limit` SM clock cycles; limit 0 makes one
+// non-blocking probe.
+__device__ __forceinline__ bool stage_ready(uint64_t* bar, uint32_t parity, int* err, long long limit) {
+  bool ok = limit > 0 ? mbar_try_wait(bar, parity) : mbar_test_wait(bar, parity);
+  if (!ok && limit > 0) {
+    const long long t0 = clock64();
+    while (!(ok = mbar_try_wait(bar, parity)))
+      if (clock64() - t0 > limit) break;
+  }
+  // a completed phase stays completed until this warp refills the stage; a
+  // warp whose lanes disagree counts as failed
   if (!__all_sync(0xffffffffu, ok)) {
     if ((threadIdx.x & 31) == 0 && err) atomicExch(err, 1);
     return false;
@@ -297,7 +312,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
     const bool sec = c_it >= n0;
     const MatDev& M = sec ? m1 : m0;
     const int s = c_seq % NS;
-    if (!stage_ready(&R.bar[s], (uint32_t)((c_seq / NS) & 1), M.err)) {
+    if (!stage_ready(&R.bar[s], (uint32_t)((c_seq / NS) & 1), M.err, M.wait)) {
       drain<NS>(R.bar, c_seq, p_seq);
       return;
     }
@@ -521,7 +536,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
     const bool sec = c_it >= n0;
     const MatDev& M = sec ? m1 : m0;
     const int s = c_seq % NS;
-    if (!stage_ready(&R.bar[s], (uint32_t)((c_seq / NS) & 1), M.err)) {
+    if (!stage_ready(&R.bar[s], (uint32_t)((c_seq / NS) & 1), M.err, M.wait)) {
       drain<NS>(R.bar, c_seq, p_seq);
       return;
     }

@@ -29,6 +29,9 @@ extern "C" {
 #define HBI_ERR_STATE (-4)    /* call out of order (e.g. construct before generate) */
 #define HBI_ERR_CONVERGE (-5) /* Runge-Kutta step size underflow (reference: stop) */
 #define HBI_ERR_LIMIT (-6)    /* a size limit of this entry point was exceeded */
+#define HBI_ERR_DEVICE (-7)   /* a product kernel gave up a bounded wait for one of its bulk
+                                 copies: the results of the calls since the last check are
+                                 invalid; the operator's device state has been reset */
 
 /* problem kinds: st_bemv%problem of m_HACApK_calc_entry_ij.f90:24-90 */
 #define HBI_2DVS 1 /* 2D antiplane, half space (matels2dpa_ij :685-695)   */
@@ -114,6 +117,23 @@ int hbi_adot_lattice_hyp(double* au, hbi_lhp* st_LHp, hbi_ctl* st_ctl, double* w
 /* same product on device arrays, enqueued on `stream` (cudaStream_t, NULL =
  * the handle's stream); no synchronisation */
 int hbi_adot_lattice_hyp_dev(double* d_au, hbi_lhp* st_LHp, const double* d_u, void* stream);
+/* Error check of the asynchronous products (no reference counterpart: the
+ * reference's product cannot fail).  Every wait of the product kernels for a
+ * bulk copy is bounded (about a second of SM clock); a wait that runs out
+ * sets the operator's device error word and the kernel leaves early.  The
+ * blocking calls (hbi_adot_lattice_hyp, hbi_rkck, hbi_rkqs, hbi_derivs,
+ * hbi_rk_get_state, hbi_cycle_run, hbi_ens_run) read the word themselves and
+ * return HBI_ERR_DEVICE; after hbi_adot_lattice_hyp_dev or
+ * hbi_adot_lattice_hyp_noalloc, synchronise the stream and call this.
+ * Returns HBI_OK or HBI_ERR_DEVICE, and clears the word and the operator's
+ * arrival counters, so that the next product starts clean. */
+int hbi_lh_check_error(hbi_lhp* st_LHp);
+/* Test hook (no reference counterpart): the bound of the product kernels'
+ * bulk-copy waits in SM clock cycles for products launched afterwards
+ * (operators already bound to an RK handle keep theirs); 0 makes each wait a
+ * single non-blocking probe, so that waits run out without anything being
+ * wrong; a negative value restores the default bound. */
+int hbi_lh_set_wait_limit(hbi_lhp* st_LHp, long long cycles);
 
 /* The product of hbi_adot_lattice_hyp_dev without any device allocation.
  * No counterpart in the reference (HACApK allocates its scratch per call).
@@ -129,7 +149,11 @@ int hbi_adot_lattice_hyp_dev(double* d_au, hbi_lhp* st_LHp, const double* d_u, v
  * set-up, no allocation); make that first call before any stream capture.
  * All calls share the array and it keeps the previous call's contents (the
  * counters are cleared on every call), so calls that overlap on the GPU --
- * on different streams, or from different threads -- race; serialise them. */
+ * on different streams, or from different threads -- race; serialise them.
+ * The array's device address is looked up once per device and kept for the
+ * life of the process: do not use this entry point after cudaDeviceReset (or
+ * anything else that destroys the device's primary context) in the same
+ * process.  Check for a timed-out wait with hbi_lh_check_error. */
 #define HBI_NOALLOC_SCRATCH_BYTES (16u << 20)
 int hbi_adot_lattice_hyp_noalloc(double* d_au, hbi_lhp* st_LHp, const double* d_u, void* stream);
 
@@ -186,6 +210,9 @@ int hbi_rkck(hbi_rk* rk, double h, double eps, double* yout, double* yerr, doubl
  * HBI_ERR_CONVERGE when the step size underflows (the reference stops). */
 int hbi_rkqs(hbi_rk* rk, double* x, double htry, double eps, double dtmax, double* hdid,
              double* hnext, double* errmax, int* nrjct);
+/* after hbi_rk_attempt_async: waits for the handle's stream and returns
+ * HBI_ERR_DEVICE if a product kernel gave up a wait (see hbi_lh_check_error) */
+int hbi_rk_check_error(hbi_rk* rk);
 /* number of kernels the handle launches per RK attempt */
 int hbi_rk_launches_per_attempt(const hbi_rk* rk);
 /* the CUDA stream (cudaStream_t) the RK handle enqueues on, for timing events */
@@ -228,6 +255,7 @@ typedef struct {
 #define HBI_STOP_KLIMIT 4    /* k reached the run's step limit (resumable) */
 #define HBI_STOP_UNDERFLOW 5 /* rkqs step size underflow (reference: stop) */
 #define HBI_STOP_TLIMIT 6    /* x reached the run's time limit exactly (resumable) */
+#define HBI_STOP_DEVICE 7    /* a product kernel gave up a wait; hbi_cycle_run returns HBI_ERR_DEVICE */
 
 typedef struct {
   long long k, attempts, rejected;

@@ -1,0 +1,108 @@
+"""Bounded waits of the product kernels end in an error status the host
+reads, through the C ABI.
+
+Every wait of the phase kernels for one of their bulk copies is bounded; a
+wait that runs out sets the operator's device error word and the warp leaves
+after its copies in flight have landed.  These tests make the waits run out
+without anything being wrong: hbi_lh_set_wait_limit(lh, 0) turns each wait
+into a single non-blocking probe, which fails for nearly every stage because
+a copy from HBM takes far longer than one probe.  All copies are valid and
+are waited for before the kernel ends, so nothing faults or hangs.
+
+Checked: the blocking product returns HBI_ERR_DEVICE, the asynchronous one
+reports it through hbi_lh_check_error, the device time loop stops with
+HBI_ERR_DEVICE; afterwards (default bound restored) the same operator gives
+the product bit for bit again, i.e. the error word and the arrival counters
+were reset.
+"""
+import numpy as np
+import pytest
+
+import hbi_gb300 as H
+from gpu_cases import case, product_geometry
+from hbi_gb300 import configs
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def operator():
+    prob, n, g, w, eps = case("3dph", (64, 64))
+    ctl = H.Ctl(n)
+    lf = H.LeafMtxp(ctl, product_geometry(prob, n, g, w, "s"), eps)
+    return n, ctl, lf
+
+
+@pytest.mark.parametrize("store", ["f32", "f64"])
+def test_blocking_product_reports_a_wait_that_ran_out(operator, store):
+    n, ctl, lf = operator
+    lh = H.LHp(lf, ctl, store)
+    u = np.random.default_rng(1).standard_normal(n)
+    good = lh.matvec(u)
+    lh.set_wait_limit(0)
+    with pytest.raises(H.HBIError) as e:
+        lh.matvec(u)
+    assert e.value.code == H.HBI_ERR_DEVICE
+    assert b"gave up" in H.lib().hbi_last_error()
+    lh.set_wait_limit(-1)
+    lh.check_error()  # the blocking call already cleared the word
+    assert np.array_equal(lh.matvec(u), good)
+    assert np.array_equal(lh.matvec(u), good)
+
+
+def test_async_product_reports_through_check_error(operator):
+    import torch
+    n, ctl, lf = operator
+    lh = H.LHp(lf, ctl, "f32")
+    st = torch.cuda.Stream()
+    u = torch.randn(n, dtype=torch.float64, device="cuda", generator=torch.Generator(device="cuda").manual_seed(2))
+    ref = torch.empty(n, dtype=torch.float64, device="cuda")
+    out = torch.empty(n, dtype=torch.float64, device="cuda")
+    lh.matvec_dev(ref.data_ptr(), u.data_ptr(), st.cuda_stream)
+    st.synchronize()
+    lh.check_error()
+    lh.set_wait_limit(0)
+    for _ in range(3):
+        lh.matvec_dev(out.data_ptr(), u.data_ptr(), st.cuda_stream)
+    st.synchronize()
+    with pytest.raises(H.HBIError) as e:
+        lh.check_error()
+    assert e.value.code == H.HBI_ERR_DEVICE
+    lh.check_error()  # cleared by the first check
+    lh.set_wait_limit(-1)
+    lh.matvec_dev(out.data_ptr(), u.data_ptr(), st.cuda_stream)
+    st.synchronize()
+    lh.check_error()
+    assert torch.equal(out, ref)
+
+
+def test_time_loop_stops_on_a_wait_that_ran_out():
+    w = configs.c1_2dvs(512)
+    ctl = H.Ctl(w.nd)
+    lf = H.LeafMtxp(ctl, w.geometry("s"), w.eps_h)
+    lh = H.LHp(lf, ctl, "f64")
+    ndc, lodc = H.HACApK_gen_lattice_vector(ctl)
+    y0, p = w.initial_state(lodc)
+    ds = w.ds_area[lodc - 1]
+
+    def loop():
+        rk = H.RK(lh, None, a=p["a"], b=p["b"], dc=p["dc"], f0=p["f0"], vpl=p["vpl"])
+        rk.set_state(y0)
+        return rk, H.Cycle(rk, p["vel"], ds, eps_r=1e-6)
+
+    lh.set_wait_limit(0)  # bound into the RK handle made next
+    rk, c = loop()
+    with pytest.raises(H.HBIError) as e:
+        c.run(k_limit=20)
+    assert e.value.code == H.HBI_ERR_DEVICE
+    with pytest.raises(H.HBIError):  # a stopped loop stays stopped
+        c.run(k_limit=40)
+    c.close()
+    rk.close()
+    lh.set_wait_limit(-1)
+    rk2, c2 = loop()
+    st = c2.run(k_limit=20)
+    assert st["stop_name"] == "klimit" and st["k"] == 20
+    rk3, c3 = loop()
+    c3.run(k_limit=20)
+    assert np.array_equal(c2.trace(), c3.trace())

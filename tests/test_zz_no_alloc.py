@@ -6,7 +6,8 @@ when they multiply (device memory owned by another allocator or a fixed
 budget, or a time loop that must stay clear of cudaMalloc and its device-wide
 synchronisation).  Its scratch is a 16 MiB array inside the library, shared by
 all calls, so two calls in a row must each give the same product as the
-allocating path -- the second call must not see stale data from the first.
+allocating path, bit for bit (same kernels, schedules and summation order) --
+the second call must not see stale data from the first.
 
 This file is collected last so that a failure here leaves every other test
 already run; it also passes on its own in a fresh process.
@@ -33,6 +34,7 @@ def test_noalloc_matches_allocating_product(kind, store, tol):
     ctl = H.Ctl(n)
     lf = H.LeafMtxp(ctl, product_geometry(prob, n, g, w, "s"), eps)
     lh = H.LHp(lf, ctl, store)
+    l64 = H.LHp(lf, ctl, "f64")
     st = torch.cuda.Stream()
     gen = torch.Generator(device="cuda").manual_seed(5)
     for call in range(2):  # two calls in a row share the scratch array
@@ -44,9 +46,15 @@ def test_noalloc_matches_allocating_product(kind, store, tol):
         rc = _noalloc(lh, out.data_ptr(), u.data_ptr(), st.cuda_stream)
         assert rc == 0, H.lib().hbi_last_error()
         st.synchronize()
+        assert H.lib().hbi_lh_check_error(lh.h) == 0
         r, o = ref.cpu().numpy(), out.cpu().numpy()
         assert np.all(np.isfinite(o))
-        assert np.linalg.norm(o - r) <= tol * np.linalg.norm(r), (call, np.linalg.norm(o - r) / np.linalg.norm(r))
+        # the same kernels, warp schedules and summation order as the
+        # allocating path: any stale scratch would show as a difference
+        assert np.array_equal(o, r), (call, np.linalg.norm(o - r) / np.linalg.norm(r))
+        # and the product itself is the one of the factors (storage tolerance)
+        r64 = l64.matvec(u.cpu().numpy())
+        assert np.linalg.norm(o - r64) <= tol * np.linalg.norm(r64)
 
 
 def test_noalloc_rejects_operators_beyond_its_scratch():

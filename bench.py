@@ -1,26 +1,38 @@
 #!/usr/bin/env python
-"""bench.py -- H-matvec GB/s inside Cash-Karp RK45 attempts of HBI's hot path.
+"""bench.py -- H-matvec GB/s inside Cash-Karp RK45 attempts of HBI's hot path,
+and the simulated years per hour of the time loop on the target fault.
 
-Workload (default): the 3D planar thrust fault of the second benchmark
-configuration -- a 30-degree dipping fault in a half space, Okada kernel,
-256 x 256 = 65,536 elements, two H-matrices (shear 's' and normal 'n'),
-velocity-weakening central patch, ACA eps 1e-5; seeded synthetic inputs.
-
-A step is one Cash-Karp attempt (rkck, main_LH.f90:2472-2554): six stages,
-each evaluating derivs (main_LH.f90:2053-2163) with one product per
-H-matrix, i.e. 12 lattice H-matrix-vector products plus the fused
-rate-and-state / stage epilogue.  value = 12 x (algorithmic bytes of one
-product) per second, the bytes being the stored factor bytes
+Kernel workload (the headline `value`): the 3D planar thrust fault of the
+second benchmark configuration -- a 30-degree dipping fault in a half space,
+Okada kernel, 256 x 256 = 65,536 elements, two H-matrices (shear 's' and
+normal 'n'), velocity-weakening central patch, ACA eps 1e-5; seeded
+synthetic inputs.  A step is one Cash-Karp attempt (rkck, main_LH.f90:
+2472-2554): six stages, each evaluating derivs (main_LH.f90:2053-2163) with
+one product per H-matrix, i.e. 12 lattice H-matrix-vector products plus the
+fused rate-and-state / stage epilogue.  value = 12 x (algorithmic bytes of
+one product) per second, the bytes being the stored factor bytes
 (sum_LR kt(ndl+ndt) + sum_dense ndl*ndt, times the storage size) plus the
 FP64 input and output vectors.  The factor stores (> 1 GB) exceed the 126 MB
-L2, so no flush is needed between steps.
+L2, so no flush is needed between steps.  The same attempt rate with FP64
+factors, the reference's own precision, is reported beside it
+(same_precision_f64).
+
+Time-loop workload (sim_yr_per_hour): the third configuration, the target of
+the 3x goal -- a rough strike-slip fault of 200,000 triangles, TDstressFS
+full space, slip law, two H-matrices, ACA eps 1e-4 -- from steady state
+through its first earthquake (it nucleates at 19.44 years) to
+--sim-window-yr (20): the plain form (FP64 factors, rkqs controller) against
+the mixed form (FP32 factors and the learned step-size proposer trained on
+the plain run's trace), with the catalogues compared event by event (see
+catalogue_gate) and the slip field at the window's end, each within 1e-3
+relative; a mismatch fails the gate and is listed, never dropped.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--store f32|bf16|f64]
   python bench.py --impl reference ...   # the CPU oracle port, all host cores
+  python bench.py --mode matvec|ensemble  # product kernels alone / configuration c4
 """
 import argparse
 import json
-import math
 import os
 import subprocess
 import sys
@@ -48,9 +60,13 @@ def parse():
     ap.add_argument("--jmax", type=int, default=256)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-same-precision", action="store_true")
     ap.add_argument("--mode", default="step", choices=["step", "matvec", "ensemble"])
-    ap.add_argument("--window-yr", type=float, default=100.0,
+    ap.add_argument("--sim-config", default="c3", choices=["c3", "c2"],
+                    help="workload of the sim-yr/h comparison (c3: the 200,000-triangle rough fault)")
+    ap.add_argument("--sim-window-yr", type=float, default=20.0,
                     help="simulated window of the sim-yr/h comparison (0: skip it)")
+    ap.add_argument("--window-yr", type=float, default=2.0, help="simulated window of --mode ensemble")
     return ap.parse_args()
 
 
@@ -72,8 +88,9 @@ class Clocks:
 
     def __enter__(self):
         try:
-            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={NSMI_Q}", "--format=csv,noheader,nounits",
-                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={NSMI_Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
         except FileNotFoundError:
             self.p = None
         time.sleep(0.3)
@@ -92,7 +109,8 @@ class Clocks:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for r in rows:
             try:
-                sm.append(float(r[1])); mx = max(mx, float(r[2]))
+                sm.append(float(r[1]))
+                mx = max(mx, float(r[2]))
                 for k, nm in enumerate(names):
                     if r[5 + k].strip().lower() == "active":
                         reasons.add(nm)
@@ -103,64 +121,14 @@ class Clocks:
 
 
 # DRAM bytes (read + write) per launch of the phase kernels on the c2 shear
-# H-matrix, from the ncu capture summarised in
-# profiles/matvec_p1_p2_c2_256x256_f32.md (FP32 store)
-NCU_TRAFFIC = {"f32": {"phase1": 330.0e6, "phase2": 378.6e6}}
+# H-matrix, from the ncu captures summarised under profiles/ (one entry per
+# factor storage that has been captured)
+NCU_TRAFFIC = {
+    "f32": {"phase1": 330.0e6, "phase2": 378.6e6, "source": "profiles/matvec_p1_p2_c2_256x256_f32.md"},
+}
 
 
-def run_cycles(args, w, lf_s, lf_n, ctl_s, ctl_n, lodc, y0, p):
-    """sim-yr/h of the time loop over [0, window]: the plain FP64 form (FP64
-    factors, rkqs controller) against the mixed form (--store factors,
-    learned step-size proposer trained on the plain run's own trace), with
-    the relative error of the mixed run's slip field at the window's end and
-    of its event onset times."""
-    import hbi_gb300 as H
-    from hbi_gb300 import proposer
-    ds = w.ds_area[lodc - 1]
-    T = args.window_yr * H.YEAR
-
-    def one(store, wts=None):
-        lh_s = H.LHp(lf_s, ctl_s, store)
-        lh_n = H.LHp(lf_n, ctl_n, store)
-        rk = H.RK(lh_s, lh_n, evlaw=w.evlaw, scale=w.scale, a=p["a"], b=p["b"], dc=p["dc"], f0=p["f0"],
-                  vpl=p["vpl"])
-        rk.set_state(y0)
-        c = H.Cycle(rk, p["vel"], ds, eps_r=1e-6, tmax_yr=w.tmax_yr)
-        if wts is not None:
-            c.set_proposer(wts)
-        st = c.run(t_limit=T)
-        out = dict(st=st, trace=c.trace(), events=c.events(), slip=c.fields()[1])
-        c.close(); rk.close(); lh_s.close(); lh_n.close()
-        return out
-
-    plain = one("f64")
-    X, Tt = proposer.training_set(plain["trace"])
-    t0 = time.perf_counter()
-    wts, hist = proposer.train(X, Tt, epochs=30)
-    t_train = time.perf_counter() - t0
-    mixed = one(args.store, wts)
-    rate = lambda r: r["st"]["x"] / H.YEAR / r["st"]["wall_s"] * 3600.0
-    slip_err = float(np.linalg.norm(mixed["slip"] - plain["slip"]) / np.linalg.norm(plain["slip"]))
-    on_p = [e["onset"] for e in plain["events"]]
-    on_m = [e["onset"] for e in mixed["events"]]
-    onset_err = (max(abs(a - b) / b for a, b in zip(on_m, on_p)) if on_p and len(on_p) == len(on_m) else None)
-    rj = lambda r: r["st"]["rejected"] / max(1, r["st"]["attempts"])
-    return {
-        "unit": "simulated yr/hour", "window_yr": args.window_yr,
-        "plain_fp64": round(rate(plain), 1), "mixed": round(rate(mixed), 1),
-        "ratio": round(rate(mixed) / rate(plain), 3),
-        "mixed_form": f"{args.store} factors + learned step-size proposer (trained on the plain run's trace, "
-                      f"{len(Tt)} samples, {t_train:.1f} s on the GPU)",
-        "plain_form": "f64 factors, rkqs controller, same kernels and device-resident loop",
-        "slip_rel_err_at_window_end": slip_err, "onset_rel_err_max": onset_err,
-        "events": [len(on_p), len(on_m)],
-        "attempts": [plain["st"]["attempts"], mixed["st"]["attempts"]],
-        "rejected_frac": [round(rj(plain), 4), round(rj(mixed), 4)],
-        "wall_s": [round(plain["st"]["wall_s"], 2), round(mixed["st"]["wall_s"], 2)],
-    }
-
-
-def dist_init(args):
+def dist_init():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -177,8 +145,8 @@ def out_line(d):
 
 
 def time_phases(torch, lh, n, reps):
-    """Mean device time of the two product kernels, timed with CUDA events on
-    the (non-default) stream they are launched on."""
+    """Mean device time of the three product phases, timed with CUDA events
+    on the (non-default) stream they are launched on."""
     x = torch.randn(n, dtype=torch.float64, device="cuda")
     y = torch.empty(n, dtype=torch.float64, device="cuda")
     ts = torch.cuda.Stream()
@@ -195,6 +163,7 @@ def time_phases(torch, lh, n, reps):
         lh.matvec_dev(y.data_ptr(), x.data_ptr(), ts.cuda_stream, phase=3)
         ev[4 * r + 3].record(ts)
     torch.cuda.synchronize()
+    lh.check_error()
     t1 = float(np.mean([ev[4 * r].elapsed_time(ev[4 * r + 1]) for r in range(reps)])) * 1e-3
     t2 = float(np.mean([ev[4 * r + 1].elapsed_time(ev[4 * r + 2]) for r in range(reps)])) * 1e-3
     t3 = float(np.mean([ev[4 * r + 2].elapsed_time(ev[4 * r + 3]) for r in range(reps)])) * 1e-3
@@ -267,13 +236,140 @@ def run_ensemble_mode(args):
                                                         max(1, res["cuda-cores"][0]["attempts"]) * 1e3, 3)})
 
 
+# ------------------------------------------------------------ time loops
+def compare_time_loops(args, w):
+    """sim-yr/h of the time loop over [0, window]: the plain FP64 form (FP64
+    factors, rkqs controller) against the mixed form (--store factors,
+    learned step-size proposer trained on the plain run's own trace)."""
+    import hbi_gb300 as H
+    from hbi_gb300 import proposer
+    from hbi_gb300.catalogue import catalogue_gate
+    n = w.nd
+    t0 = time.perf_counter()
+    ctl_s, ctl_n = H.Ctl(n), H.Ctl(n)
+    lf_s = H.LeafMtxp(ctl_s, w.geometry("s"), w.eps_h)
+    lf_n = H.LeafMtxp(ctl_n, w.geometry("n"), w.eps_h)
+    t_gen = time.perf_counter() - t0
+    ndc, lodc = H.HACApK_gen_lattice_vector(ctl_s)
+    y0, p = w.initial_state(lodc)
+    ds = w.ds_area[lodc - 1]
+    T = args.sim_window_yr * H.YEAR
+
+    def one(store, wts=None):
+        lh_s = H.LHp(lf_s, ctl_s, store)
+        lh_n = H.LHp(lf_n, ctl_n, store)
+        gb = (lh_s.info()["store_bytes"] + lh_n.info()["store_bytes"]) / 1e9
+        rk = H.RK(lh_s, lh_n, evlaw=w.evlaw, scale=w.scale, a=p["a"], b=p["b"], dc=p["dc"], f0=p["f0"],
+                  vpl=p["vpl"])
+        rk.set_state(y0)
+        c = H.Cycle(rk, p["vel"], ds, eps_r=1e-6, tmax_yr=max(w.tmax_yr, args.sim_window_yr + 1))
+        if wts is not None:
+            c.set_proposer(wts)
+        st = c.run(t_limit=T)
+        out = dict(st=st, trace=c.trace(), events=c.events(), slip=c.fields()[1], store_gb=gb)
+        c.close()
+        rk.close()
+        lh_s.close()
+        lh_n.close()
+        return out
+
+    plain = one("f64")
+    X, Tt = proposer.training_set(plain["trace"])
+    t1 = time.perf_counter()
+    wts, hist = proposer.train(X, Tt, epochs=30)
+    t_train = time.perf_counter() - t1
+    mixed = one(args.store, wts)
+    for h in (lf_s, lf_n, ctl_s, ctl_n):
+        h.close()
+    rate = lambda r: r["st"]["x"] / H.YEAR / r["st"]["wall_s"] * 3600.0
+    rj = lambda r: r["st"]["rejected"] / max(1, r["st"]["attempts"])
+    cat = lambda r: [[round(e["onset"] / H.YEAR, 6), round(e["end"] / H.YEAR, 6), e["hypoloc"],
+                      float("%.6e" % e["moment"])] for e in r["events"]]
+    return {
+        "unit": "simulated yr/hour", "workload": f"{w.name}: {n} elements, 2 H-matrices, ACA eps {w.eps_h}, "
+                                                 f"eps_r 1e-6, from steady state to {args.sim_window_yr} yr",
+        "window_yr": args.sim_window_yr,
+        "plain_fp64": round(rate(plain), 2), "mixed": round(rate(mixed), 2),
+        "ratio": round(rate(mixed) / rate(plain), 3),
+        "mixed_form": f"{args.store} factors ({mixed['store_gb']:.1f} GB) + learned step-size proposer (trained on "
+                      f"the plain run's trace, {len(Tt)} samples, {t_train:.1f} s on the GPU)",
+        "plain_form": f"f64 factors ({plain['store_gb']:.1f} GB), rkqs controller, same kernels and "
+                      f"device-resident loop",
+        "gate": catalogue_gate(plain, mixed),
+        "events": [len(plain["events"]), len(mixed["events"])],
+        "catalogue_plain": cat(plain), "catalogue_mixed": cat(mixed),
+        "attempts": [plain["st"]["attempts"], mixed["st"]["attempts"]],
+        "rejected_frac": [round(rj(plain), 4), round(rj(mixed), 4)],
+        "ms_per_attempt": [round(r["st"]["wall_s"] / max(1, r["st"]["attempts"]) * 1e3, 3) for r in (plain, mixed)],
+        "wall_s": [round(plain["st"]["wall_s"], 2), round(mixed["st"]["wall_s"], 2)],
+        "assembly_s": round(t_gen, 1),
+    }
+
+
 # --------------------------------------------------------------------- ours
+def attempt_rate(torch, rk, steps, warmup, world, local, dist=None, clocks=False):
+    """K back-to-back RK attempts enqueued on the handle's stream, timed with
+    CUDA events on that stream; max over ranks."""
+    stream = torch.cuda.ExternalStream(rk.stream)
+    h, eps = 1.0e5, 1e-5
+    for _ in range(warmup):
+        rk.attempt_async(h, eps)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ck = Clocks(local) if clocks else None
+    if ck:
+        ck.__enter__()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        rk.attempt_async(h, eps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if ck:
+        ck.__exit__()
+    rk.check_error()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    return ms, (ck.summary() if ck else None)
+
+
+def e2e_rate(torch, rk, y0, steps, world, dist=None):
+    """The same attempts through the C ABI with pinned host buffers: state
+    copied in, rkck, yout and yerr copied out, every step."""
+    n3 = y0.size
+    yh = torch.empty(n3, dtype=torch.float64, pin_memory=True).numpy()
+    yh[:] = y0
+    yo = torch.empty(n3, dtype=torch.float64, pin_memory=True).numpy()
+    ye = torch.empty(n3, dtype=torch.float64, pin_memory=True).numpy()
+    h, eps = 1.0e5, 1e-5
+    for _ in range(2):
+        rk.set_state(yh)
+        rk.rkck_into(h, eps, yo, ye)
+    torch.cuda.synchronize()
+    te = time.perf_counter()
+    for _ in range(steps):
+        rk.set_state(yh)
+        rk.rkck_into(h, eps, yo, ye)
+    te = time.perf_counter() - te
+    if world > 1:
+        tt = torch.tensor([te], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        te = float(tt.item())
+    return te, {"h2d_bytes_per_step": n3 * 8, "d2h_bytes_per_step": 2 * n3 * 8 + 32}
+
+
 def run_ours(args):
     import torch
 
     import hbi_gb300 as H
 
-    rank, world, local = dist_init(args)
+    rank, world, local = dist_init()
+    dist = None
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
@@ -286,107 +382,92 @@ def run_ours(args):
     lf_s = H.LeafMtxp(ctl_s, w.geometry("s"), w.eps_h)
     lf_n = H.LeafMtxp(ctl_n, w.geometry("n"), w.eps_h)
     t_gen = time.perf_counter() - t0
-    lh_s = H.LHp(lf_s, ctl_s, args.store)
-    lh_n = H.LHp(lf_n, ctl_n, args.store)
     ndc, lodc = H.HACApK_gen_lattice_vector(ctl_s)
     y0, p = w.initial_state(lodc)
-    rk = H.RK(lh_s, lh_n, evlaw=w.evlaw, scale=w.scale, a=p["a"], b=p["b"], dc=p["dc"], f0=p["f0"], vpl=p["vpl"],
-              taudot=p["taudot"], sigdot=p["sigdot"])
-    rk.set_state(y0)
+
+    def rk_for(store):
+        lh_s = H.LHp(lf_s, ctl_s, store)
+        lh_n = H.LHp(lf_n, ctl_n, store)
+        rk = H.RK(lh_s, lh_n, evlaw=w.evlaw, scale=w.scale, a=p["a"], b=p["b"], dc=p["dc"], f0=p["f0"],
+                  vpl=p["vpl"], taudot=p["taudot"], sigdot=p["sigdot"])
+        rk.set_state(y0)
+        bytes_attempt = 6.0 * (lh_s.info()["alg_bytes"] + lh_n.info()["alg_bytes"])
+        return rk, lh_s, lh_n, bytes_attempt
+
+    # ---- the headline store: device-resident attempts, roofline, end to end ----
+    rk, lh_s, lh_n, bytes_attempt = rk_for(args.store)
     t_setup = time.perf_counter() - t0
     info_s, info_n = lh_s.info(), lh_n.info()
-    bytes_attempt = 6.0 * (info_s["alg_bytes"] + info_n["alg_bytes"])
-    stream = torch.cuda.ExternalStream(rk.stream)
-    h, eps = 1.0e5, 1e-5
-
-    # ---- device-resident throughput: K back-to-back attempts ----
-    for _ in range(args.warmup):
-        rk.attempt_async(h, eps)
-    torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with Clocks(local) as ck:
-        torch.cuda.synchronize()
-        e0.record(stream)
-        for _ in range(args.steps):
-            rk.attempt_async(h, eps)
-        e1.record(stream)
-        torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    clocks = ck.summary()
-    if world > 1:
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms, clocks = attempt_rate(torch, rk, args.steps, args.warmup, world, local, dist, clocks=True)
     ms_step = ms / args.steps
     value = world * args.steps * bytes_attempt / (ms * 1e-3) / 1e9
-
-    # ---- roofline of the two matvec kernels (phase 1, phase 2) on lh_s ----
     t1, t2, t3, b1, b2 = time_phases(torch, lh_s, n, 20)
     peak, peak_kind = peaks()
     dominant = "phase2" if t2 >= t1 else "phase1"
     ach = (b2 / t2 if dominant == "phase2" else b1 / t1) / 1e9
     mv_gbs = (b1 + b2 + 8 * n) / (t1 + t2 + t3) / 1e9  # the whole product (y written by phase 3)
-
-    # ---- end to end through the C ABI with host buffers ----
-    yh = torch.empty(3 * n, dtype=torch.float64, pin_memory=True).numpy()
-    yh[:] = y0
-    yo = torch.empty(3 * n, dtype=torch.float64, pin_memory=True).numpy()
-    ye = torch.empty(3 * n, dtype=torch.float64, pin_memory=True).numpy()
-    for _ in range(2):
-        rk.set_state(yh)
-        rk.rkck_into(h, eps, yo, ye)
-    torch.cuda.synchronize()
-    te = time.perf_counter()
-    for _ in range(args.steps):
-        rk.set_state(yh)
-        rk.rkck_into(h, eps, yo, ye)
-    te = time.perf_counter() - te
-    if world > 1:
-        tt = torch.tensor([te], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        te = float(tt.item())
+    te, e2e_bytes = e2e_rate(torch, rk, y0, args.steps, world, dist)
     e2e = world * args.steps * bytes_attempt / te / 1e9
+    launches = args.steps * rk.launches_per_attempt
+    for hnd in (rk, lh_s, lh_n):
+        hnd.close()
 
-    # ---- sim-yr/h: plain FP64 form against the mixed + learned form ----
-    cyc = None
-    if rank == 0 and args.window_yr > 0:
-        cyc = run_cycles(args, w, lf_s, lf_n, ctl_s, ctl_n, lodc, y0, p)
+    # ---- the same attempts with FP64 factors (the reference's precision) ----
+    same = None
+    if args.store != "f64" and not args.no_same_precision:
+        rk, lh_s, lh_n, bytes64 = rk_for("f64")
+        ms64, _ = attempt_rate(torch, rk, args.steps, args.warmup, world, local, dist)
+        te64, _ = e2e_rate(torch, rk, y0, args.steps, world, dist)
+        same = {"storage": "f64", "value": round(world * args.steps * bytes64 / (ms64 * 1e-3) / 1e9, 2),
+                "unit": "GB/s", "ms_per_step": round(ms64 / args.steps, 4),
+                "e2e": {"value": round(world * args.steps * bytes64 / te64 / 1e9, 2), "unit": "GB/s",
+                        "ms_per_step": round(te64 / args.steps * 1e3, 4)},
+                "note": "same attempts, FP64 factor stores: FP64 products with FP64 accumulation"}
+        for hnd in (rk, lh_s, lh_n):
+            hnd.close()
 
     # ---- CPU baseline: the oracle port on the host cores (rank 0, N=1) ----
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(args, w, lf_s, lf_n, y0, p, lodc)
+        cpu = cpu_baseline(args, w, lf_s, lf_n, y0, p)
+    for hnd in (lf_s, lf_n, ctl_s, ctl_n):
+        hnd.close()
+
+    # ---- sim-yr/h: plain FP64 form against the mixed + learned form ----
+    cyc = None
+    if rank == 0 and args.sim_window_yr > 0:
+        from hbi_gb300 import configs
+        cyc = compare_time_loops(args, configs.c3_3dnt() if args.sim_config == "c3" else w)
 
     if rank == 0:
+        traffic = NCU_TRAFFIC.get(args.store, {})
         d = {
             "metric": "H-matvec GB/s", "value": round(value, 2), "unit": "GB/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.store,
-            "data": "synthetic (seeded 3D planar thrust, Okada half space)",
+            "data": "synthetic (seeded 3D planar thrust, Okada half space; seeded rough fault for sim_yr_per_hour)",
             "config": {"workload": f"{w.name}: 3dph Okada half space, {n} elements, 2 H-matrices (s,n), "
                                    f"ACA eps {w.eps_h}, one Cash-Karp attempt per step (12 products)",
                        "elements": n, "storage": args.store, "products_per_step": 12,
-                       "l2": "inputs larger than L2 (factor stores %.2f GB)" % ((info_s["store_bytes"] + info_n["store_bytes"]) / 1e9),
+                       "l2": "inputs larger than L2 (factor stores %.2f GB)" % (
+                           (info_s["store_bytes"] + info_n["store_bytes"]) / 1e9),
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
             "roofline": {"bound": "hbm", "kernel": f"matvec {dominant}", "achieved": round(ach, 1),
                          "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4), "peak_kind": peak_kind,
-                         "traffic": NCU_TRAFFIC.get(args.store, {}).get(dominant),
-                         "traffic_source": "ncu dram bytes per launch (profiles/matvec_p1_p2_c2_256x256_f32.md)"
-                                           if args.store in NCU_TRAFFIC else None,
+                         "traffic": traffic.get(dominant), "traffic_source": traffic.get("source"),
                          "matvec_gbs_whole_product": round(mv_gbs, 1),
                          "phase1_us": round(t1 * 1e6, 2), "phase2_us": round(t2 * 1e6, 2),
                          "phase3_us": round(t3 * 1e6, 2),
                          "phase1_bytes": b1, "phase2_bytes": b2},
-            "e2e": {"value": round(e2e, 2), "unit": "GB/s", "h2d_bytes_per_step": 3 * n * 8,
-                    "d2h_bytes_per_step": 2 * 3 * n * 8 + 32},
-            "gpu_launches": args.steps * rk.launches_per_attempt,
+            "e2e": dict({"value": round(e2e, 2), "unit": "GB/s"}, **e2e_bytes),
+            "gpu_launches": launches,
             "clocks": clocks,
             "setup": {"generate_s": round(t_gen, 2), "total_s": round(t_setup, 2),
                       "factor_elems_s": info_s["factor_elems"], "factor_elems_n": info_n["factor_elems"],
                       "compression_s": info_s["factor_elems"] / n / n},
         }
+        if same:
+            d["same_precision_f64"] = same
         if cpu:
             d["cpu_baseline"] = cpu
         if cyc:
@@ -396,7 +477,7 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def cpu_baseline(args, w, lf_s, lf_n, y0, p, lodc):
+def cpu_baseline(args, w, lf_s, lf_n, y0, p):
     """The oracle's RK attempt (OpenMP products mirroring the reference's
     thread ranges and atomics) on the same FP64 factors, all host cores."""
     from oracle import oracle as O
@@ -427,7 +508,7 @@ def cpu_baseline(args, w, lf_s, lf_n, y0, p, lodc):
 
 # ---------------------------------------------------------------- reference
 def run_reference(args):
-    rank, world, local = dist_init(args)
+    rank, world, local = dist_init()
     if rank != 0:
         return
     from oracle import oracle as O

@@ -45,6 +45,8 @@ EXPORTS = [
     "hbi_ens_create", "hbi_ens_free", "hbi_ens_set_state", "hbi_ens_get_state", "hbi_ens_run",
     "hbi_tc_plan_emulate", "hbi_ens_use_tensor_cores", "hbi_cycle_restart", "hbi_restart_point",
     "hbi_plan_warp_schedule", "hbi_lh_check_error", "hbi_lh_set_wait_limit", "hbi_rk_check_error",
+    "hbi_stream_shapes", "hbi_lh_tuning", "hbi_autotune_select", "hbi_lh_set_shapes",
+    "hbi_partition_leaves", "hbi_construct_lh_part", "hbi_mlp_set_loss",
 ]
 
 
@@ -246,11 +248,18 @@ class LeafMtxp:
 class LHp:
     """st_HACApK_LHp: the lattice matvec operator (HACApK_construct_LH)."""
 
-    def __init__(self, lf, ctl, storage=STORE_F64):
+    def __init__(self, lf, ctl, storage=STORE_F64, owner=None, rank=0):
+        """owner (per leaf, from partition_leaves) and rank: the operator of
+        one rank's leaves (its product is that rank's partial product)."""
         if isinstance(storage, str):
             storage = STORE_NAMES[storage]
         self.ctl, self.h, self.storage = ctl, C.c_void_p(), storage
-        _check(lib().hbi_construct_lh(C.byref(self.h), lf.h, ctl.h, int(storage)), "hbi_construct_lh")
+        if owner is None:
+            _check(lib().hbi_construct_lh(C.byref(self.h), lf.h, ctl.h, int(storage)), "hbi_construct_lh")
+        else:
+            self._owner = np.ascontiguousarray(owner, dtype=np.int32)
+            _check(lib().hbi_construct_lh_part(C.byref(self.h), lf.h, ctl.h, int(storage),
+                                               self._owner.ctypes.data_as(_ip), int(rank)), "hbi_construct_lh_part")
         self.n = ctl.nd
         _register(self, 2)
 
@@ -266,6 +275,24 @@ class LHp:
         2 or 3 runs one phase of it alone (for timing), 0 the whole product."""
         _check(lib().hbi_adot_lattice_hyp_phase_dev(C.c_void_p(d_au), self.h, C.c_void_p(d_u), C.c_void_p(stream),
                                                     int(phase)), "hbi_adot_lattice_hyp_phase_dev")
+
+    def tuning(self):
+        """The launch shapes the autotuner chose for phases 1 and 2 and the
+        median time (us) of every compiled shape per phase."""
+        sh1, sh2 = stream_shapes(1), stream_shapes(2)
+        s1, s2, src = C.c_int(), C.c_int(), C.c_int()
+        us = np.zeros(len(sh1) + len(sh2), dtype=np.float32)
+        _check(lib().hbi_lh_tuning(self.h, C.byref(s1), C.byref(s2), us.ctypes.data_as(C.POINTER(C.c_float)),
+                                   C.byref(src)), "hbi_lh_tuning")
+        name = lambda t: "%dw x %d x %d KB%s" % (t[0], t[1], t[2] // 1024, " col" if t[3] else "")
+        return {"phase1": name(sh1[s1.value]), "phase2": name(sh2[s2.value]), "shape1": s1.value,
+                "shape2": s2.value, "source": {0: "timed", 1: "reused", 2: "forced"}.get(src.value, "?"),
+                "phase1_us": {name(t): round(float(us[i]), 2) for i, t in enumerate(sh1)},
+                "phase2_us": {name(t): round(float(us[len(sh1) + i]), 2) for i, t in enumerate(sh2)}}
+
+    def set_shapes(self, shape1, shape2):
+        """Pin the launch shapes (indices into stream_shapes()) of phases 1 and 2."""
+        _check(lib().hbi_lh_set_shapes(self.h, int(shape1), int(shape2)), "hbi_lh_set_shapes")
 
     def check_error(self):
         """hbi_lh_check_error: raises HBIError (code HBI_ERR_DEVICE) if a
@@ -545,6 +572,10 @@ class MLP:
         self.set_params(p)
         return p
 
+    def set_loss(self, tau=None):
+        """Squared error (tau None), or the pinball loss of quantile tau."""
+        _check(lib().hbi_mlp_set_loss(self.h, C.c_float(-1.0 if tau is None else tau)), "hbi_mlp_set_loss")
+
     def set_params(self, p):
         p = _f32(p)
         _check(lib().hbi_mlp_set_params(self.h, p.ctypes.data_as(_fp)), "hbi_mlp_set_params")
@@ -586,6 +617,38 @@ class MLP:
 
     def __del__(self):
         self.close()
+
+
+def stream_shapes(phase=1):
+    """The compiled launch shapes of the phase-1 or phase-2 product kernel:
+    [(warps per block, stages per warp, stage bytes, lane mapping), ...]."""
+    k = C.c_int()
+    _check(lib().hbi_stream_shapes(int(phase), C.byref(k), None), "hbi_stream_shapes")
+    a = np.zeros(4 * k.value, dtype=np.int32)
+    _check(lib().hbi_stream_shapes(int(phase), C.byref(k), a.ctypes.data_as(_ip)), "hbi_stream_shapes")
+    return [tuple(int(v) for v in a[4 * s:4 * s + 4]) for s in range(k.value)]
+
+
+def autotune_select(times):
+    """The autotuner's selection rule (host only): times (candidates x
+    repeats) -> (best candidate, medians)."""
+    t = np.ascontiguousarray(times, dtype=np.float32)
+    med = np.zeros(t.shape[0], dtype=np.float32)
+    best = C.c_int()
+    _check(lib().hbi_autotune_select(t.shape[0], t.shape[1], t.ctypes.data_as(C.POINTER(C.c_float)),
+                                     med.ctypes.data_as(C.POINTER(C.c_float)), C.byref(best)), "hbi_autotune_select")
+    return best.value, med
+
+
+def partition_leaves(leaves, nranks):
+    """Deal the leaves (nleaf x 6 table) to nranks ranks by factor elements
+    (host only): returns (owner per leaf, elements per rank)."""
+    lv = np.ascontiguousarray(leaves, dtype=np.int32)
+    owner = np.zeros(max(len(lv), 1), dtype=np.int32)
+    load = np.zeros(nranks, dtype=np.int64)
+    _check(lib().hbi_partition_leaves(len(lv), lv.ctypes.data_as(_ip), int(nranks), owner.ctypes.data_as(_ip),
+                                      load.ctypes.data_as(_i64p)), "hbi_partition_leaves")
+    return owner[:len(lv)], load
 
 
 def plan_warp_schedule(cost, nwarps):

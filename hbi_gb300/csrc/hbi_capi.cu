@@ -10,8 +10,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/hbi_gpu.h"
@@ -200,7 +202,12 @@ struct hbi_lhp_s {
   int32_t *d_grow0 = nullptr, *d_gndl = nullptr, *d_gnch = nullptr, *d_gpoff = nullptr;
   int32_t *d_row_fc = nullptr, *d_fc_ptr = nullptr, *d_fc_group = nullptr;
   int32_t *d_fcb_ptr = nullptr, *d_fcb_base = nullptr;
-  int32_t *d_w1off = nullptr, *d_w1item = nullptr, *d_w2off = nullptr, *d_w2item = nullptr;
+  int32_t *d_w1off[kNumShapes1] = {}, *d_w1item[kNumShapes1] = {}, *d_w2off[kNumShapes2] = {},
+          *d_w2item[kNumShapes2] = {};
+  // launch shapes chosen for phases 1 and 2, the median time (us) of every
+  // shape per phase as timed at construction, and how the choice was made
+  int tune_source = 0;  // 0 timed, 1 cached from an operator of the same plan, 2 forced or pinned
+  float tune_us[2][kMaxShapes] = {};
   int* d_err = nullptr;
   double *d_x = nullptr, *d_y = nullptr;
   MatDev md{};
@@ -541,8 +548,211 @@ extern "C" int hbi_entry_ij(const hbi_bemv* bv, int n, const int* i, const int* 
   return HBI_OK;
 }
 
+static int device_error_status(const MatDev& m, const char* where);
+
+// ----------------------------------------------------- shape autotuner
+// Replaces the reference's byte-balanced cut of the leaf list over OpenMP
+// threads (m_HACApK_use.f90:387-431, m_HACApK_base.f90:1537-1564): the work
+// of a phase is dealt to warps by plan_warp_schedule, and the launch shape
+// (warps per block, stages, stage bytes -- which sets the chunk width) is
+// chosen per operator and phase by timing every compiled shape on the
+// operator itself.  The choice is cached for operators whose plans have the
+// same size statistics.
+
+// median of the positive, finite entries of t[0..n); -1 if there is none
+static float median_valid(const float* t, int n) {
+  std::vector<float> v;
+  for (int i = 0; i < n; i++)
+    if (t[i] > 0 && std::isfinite(t[i])) v.push_back(t[i]);
+  if (v.empty()) return -1.0f;
+  std::sort(v.begin(), v.end());
+  const size_t m = v.size();
+  return m % 2 ? v[m / 2] : 0.5f * (v[m / 2 - 1] + v[m / 2]);
+}
+
+extern "C" int hbi_autotune_select(int ncand, int reps, const float* times, float* medians, int* best) {
+  if (ncand < 1 || reps < 1 || !times || !best) return fail(HBI_ERR_ARG, "hbi_autotune_select: bad arguments");
+  int b = -1;
+  float bt = 0.0f;
+  for (int c = 0; c < ncand; c++) {
+    const float m = median_valid(times + (size_t)c * reps, reps);
+    if (medians) medians[c] = m;
+    if (m < 0) continue;
+    // a later candidate must beat the current best by more than 1%: ties and
+    // near-ties keep the earlier (default-first) shape
+    if (b < 0 || m < 0.99f * bt) {
+      b = c;
+      bt = m;
+    }
+  }
+  if (b < 0) return fail(HBI_ERR_ARG, "hbi_autotune_select: no candidate has a valid time");
+  *best = b;
+  return HBI_OK;
+}
+
+namespace {
+struct TuneKey {
+  int storage, sm;
+  int64_t ns1, ns2, vstore, ustore;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(storage, sm, ns1, ns2, vstore, ustore) < std::tie(o.storage, o.sm, o.ns1, o.ns2, o.vstore, o.ustore);
+  }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, std::pair<int, int>> g_tune_cache;
+}  // namespace
+
+static int autotune_stream_shapes(hbi_lhp* h) {
+  MatDev& m = h->md;
+  for (int ph = 0; ph < 2; ph++)
+    for (int sh = 0; sh < kMaxShapes; sh++) h->tune_us[ph][sh] = -1.0f;
+  const int f1 = forced_stream_shape(1), f2 = forced_stream_shape(2);
+  if (f1 >= 0 && f2 >= 0) {
+    m.shape1 = f1;
+    m.shape2 = f2;
+    h->tune_source = 2;
+    return HBI_OK;
+  }
+  const TuneKey key{h->storage, h->ctl->sm_count, (int64_t)h->plan.p1.size(), (int64_t)h->plan.p2.size(),
+                    h->plan.vstore, h->plan.ustore};
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      m.shape1 = f1 >= 0 ? f1 : it->second.first;
+      m.shape2 = f2 >= 0 ? f2 : it->second.second;
+      h->tune_source = 1;
+      return HBI_OK;
+    }
+  }
+  cudaStream_t st = h->ctl->stream;
+  constexpr int R = 5;
+  float t[2][kMaxShapes * R];
+  cudaEvent_t ev[2 * R];
+  for (auto& e : ev)
+    if (cudaEventCreate(&e) != cudaSuccess) return fail(HBI_ERR_CUDA, "autotune: events");
+  CK(cudaMemsetAsync(h->d_x, 0, sizeof(double) * h->n, st));
+  int rc = HBI_OK;
+  for (int ph = 1; ph <= 2 && rc == HBI_OK; ph++)
+    for (int sh = 0; sh < num_shapes(ph); sh++) {
+      launch_phase_shape(ph, sh, &m, 1, h->d_x, h->ctl->sm_count, st);  // warm-up
+      for (int r = 0; r < R; r++) {
+        cudaEventRecord(ev[2 * r], st);
+        launch_phase_shape(ph, sh, &m, 1, h->d_x, h->ctl->sm_count, st);
+        cudaEventRecord(ev[2 * r + 1], st);
+      }
+      const cudaError_t e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) {
+        rc = fail(HBI_ERR_CUDA, "autotune: %s", cudaGetErrorString(e));
+        break;
+      }
+      for (int r = 0; r < R; r++) {
+        float ms = -1.0f;
+        if (cudaEventElapsedTime(&ms, ev[2 * r], ev[2 * r + 1]) != cudaSuccess) ms = -1.0f;
+        t[ph - 1][sh * R + r] = ms * 1e3f;
+      }
+    }
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (rc) return rc;
+  rc = device_error_status(m, "hbi_construct_lh (shape autotuner)");
+  if (rc) return rc;
+  int best[2] = {0, 0};
+  for (int ph = 0; ph < 2; ph++) {
+    rc = hbi_autotune_select(num_shapes(ph + 1), R, t[ph], h->tune_us[ph], &best[ph]);
+    if (rc) return rc;
+  }
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune_cache[key] = {best[0], best[1]};
+  }
+  m.shape1 = f1 >= 0 ? f1 : best[0];
+  m.shape2 = f2 >= 0 ? f2 : best[1];
+  h->tune_source = (f1 >= 0 || f2 >= 0) ? 2 : 0;
+  return HBI_OK;
+}
+
+extern "C" int hbi_lh_tuning(const hbi_lhp* h, int* shape1, int* shape2, float* median_us, int* source) {
+  if (!h) return fail(HBI_ERR_ARG, "hbi_lh_tuning: null");
+  if (shape1) *shape1 = h->md.shape1;
+  if (shape2) *shape2 = h->md.shape2;
+  if (median_us) {
+    int o = 0;
+    for (int ph = 0; ph < 2; ph++)
+      for (int sh = 0; sh < num_shapes(ph + 1); sh++) median_us[o++] = h->tune_us[ph][sh];
+  }
+  if (source) *source = h->tune_source;
+  return HBI_OK;
+}
+
+extern "C" int hbi_lh_set_shapes(hbi_lhp* h, int shape1, int shape2) {
+  if (!h || shape1 < 0 || shape1 >= kNumShapes1 || shape2 < 0 || shape2 >= kNumShapes2)
+    return fail(HBI_ERR_ARG, "hbi_lh_set_shapes: shapes must be in 0..%d (phase 1) and 0..%d (phase 2)",
+                kNumShapes1 - 1, kNumShapes2 - 1);
+  h->md.shape1 = shape1;
+  h->md.shape2 = shape2;
+  h->tune_source = 2;
+  return HBI_OK;
+}
+
+extern "C" int hbi_stream_shapes(int phase, int* count, int* shapes4) {
+  if (!count || (phase != 1 && phase != 2)) return fail(HBI_ERR_ARG, "hbi_stream_shapes: bad arguments");
+  *count = num_shapes(phase);
+  if (shapes4)
+    for (int sh = 0; sh < num_shapes(phase); sh++) {
+      const StreamShape& S = stream_shape(phase, sh);
+      shapes4[4 * sh] = S.nw;
+      shapes4[4 * sh + 1] = S.ns;
+      shapes4[4 * sh + 2] = S.sb;
+      shapes4[4 * sh + 3] = S.map;
+    }
+  return HBI_OK;
+}
+
 // ---------------------------------------------------------- construct
+// ------------------------------------------------- leaf partition (host)
+// factor elements of a leaf: kt (ndl + ndt) low rank, ndl ndt dense
+static int64_t leaf_elems(const int* q) {
+  return q[0] == 1 ? (int64_t)q[1] * (q[3] + q[5]) : (int64_t)q[3] * q[5];
+}
+
+extern "C" int hbi_partition_leaves(int nleaf, const int* leaves6, int nranks, int32_t* owner,
+                                    int64_t* elems_per_rank) {
+  if (nleaf < 0 || (nleaf > 0 && (!leaves6 || !owner)) || nranks < 1)
+    return fail(HBI_ERR_ARG, "hbi_partition_leaves: bad arguments");
+  // longest first to the least-loaded rank (ties to the lower rank), as the
+  // warp schedules deal items; leaves of equal size keep their order
+  std::vector<int> order(nleaf);
+  for (int i = 0; i < nleaf; i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return leaf_elems(leaves6 + 6 * a) > leaf_elems(leaves6 + 6 * b); });
+  std::vector<int64_t> load(nranks, 0);
+  for (int i : order) {
+    int r = 0;
+    for (int q = 1; q < nranks; q++)
+      if (load[q] < load[r]) r = q;
+    owner[i] = r;
+    load[r] += leaf_elems(leaves6 + 6 * i);
+  }
+  if (elems_per_rank)
+    for (int q = 0; q < nranks; q++) elems_per_rank[q] = load[q];
+  return HBI_OK;
+}
+
+static int construct_impl(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* c, int storage, const int32_t* owner,
+                          int rank);
+
 extern "C" int hbi_construct_lh(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* c, int storage) {
+  return construct_impl(out, lf, c, storage, nullptr, 0);
+}
+
+extern "C" int hbi_construct_lh_part(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* c, int storage,
+                                     const int32_t* owner, int rank) {
+  if (!owner || rank < 0) return fail(HBI_ERR_ARG, "hbi_construct_lh_part: owner table and rank needed");
+  return construct_impl(out, lf, c, storage, owner, rank);
+}
+
+static int construct_impl(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* c, int storage, const int32_t* owner,
+                          int rank) {
   if (!out || !lf || !c) return fail(HBI_ERR_ARG, "hbi_construct_lh: null");
   if (storage < 0 || storage > 2) return fail(HBI_ERR_ARG, "storage must be HBI_STORE_F64/F32/BF16");
   if (lf->ctl != c || !c->have_tree) return fail(HBI_ERR_STATE, "construct_LH needs the ctl used by generate");
@@ -550,15 +760,19 @@ extern "C" int hbi_construct_lh(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* 
   h->ctl = c;
   h->n = c->nd;
   h->storage = storage;
-  h->leaves = lf->leaves;
+  // the operator's leaves (all, or those of one rank) and their body offsets
+  std::vector<int64_t> boff;
+  for (size_t i = 0; i < lf->leaves.size(); i++)
+    if (!owner || owner[i] == rank) {
+      h->leaves.push_back(lf->leaves[i]);
+      boff.push_back(lf->off[i]);
+    }
   const int esz = storage == ST_F64 ? 8 : storage == ST_F32 ? 4 : 2;
   const size_t acc = storage == ST_F64 ? 8 : 4;
   cudaStream_t st = c->stream;
   // row-tiled stores read by bulk copies (plan_stream)
-  std::vector<int64_t> boff(lf->leaves.size());
-  for (size_t i = 0; i < boff.size(); i++) boff[i] = lf->off[i];
   StreamPlan& P = h->plan;
-  plan_stream(c->nd, lf->leaves, boff, 16 / esz, P, stream_stage_bytes());
+  plan_stream(c->nd, h->leaves, boff, 16 / esz, P, 8192);
   const size_t vbytes = (size_t)P.vstore * esz, ubytes = (size_t)P.ustore * esz;
   h->store_bytes = vbytes + ubytes;
   CK(cudaMalloc(&h->d_vstore, std::max<size_t>(vbytes, 16)));
@@ -620,11 +834,12 @@ extern "C" int hbi_construct_lh(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* 
   m.err = h->d_err;
   m.wait = kWaitCyclesDefault;
   m.ncnt = (int)P.ncg;
-  // static warp schedules for the grid the phase kernels get on this device:
-  // one block of stream_warps_per_block() warps per SM, fewer for small operators
-  {
-    const int nw = stream_warps_per_block(), sb = stream_stage_bytes();
-    for (int ph = 1; ph <= 2; ph++) {
+  // static warp schedules, one per launch shape, for the grid the phase
+  // kernels get on this device in that shape: one block of nw warps per SM,
+  // fewer for small operators
+  for (int ph = 1; ph <= 2; ph++)
+    for (int sh = 0; sh < num_shapes(ph); sh++) {
+      const int nw = stream_shape(ph, sh).nw, sb = stream_shape(ph, sh).sb;
       const int ni = ph == 1 ? (int)P.p1.size() : (int)P.p2.size();
       if (ni == 0) continue;
       const int need = (ni + nw - 1) / nw;
@@ -638,15 +853,29 @@ extern "C" int hbi_construct_lh(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* 
       }
       std::vector<int32_t> woff, witem;
       plan_warp_schedule(cost, gw, woff, witem);
-      CK(upload(ph == 1 ? &h->d_w1off : &h->d_w2off, woff, st));
-      CK(upload(ph == 1 ? &h->d_w1item : &h->d_w2item, witem, st));
-      (ph == 1 ? m.gw1 : m.gw2) = gw;
+      if (ph == 1) {
+        CK(upload(&h->d_w1off[sh], woff, st));
+        CK(upload(&h->d_w1item[sh], witem, st));
+        m.gw1[sh] = gw;
+        m.w1off[sh] = h->d_w1off[sh];
+        m.w1item[sh] = h->d_w1item[sh];
+      } else {
+        CK(upload(&h->d_w2off[sh], woff, st));
+        CK(upload(&h->d_w2item[sh], witem, st));
+        m.gw2[sh] = gw;
+        m.w2off[sh] = h->d_w2off[sh];
+        m.w2item[sh] = h->d_w2item[sh];
+      }
     }
-    m.w1off = h->d_w1off; m.w1item = h->d_w1item; m.w2off = h->d_w2off; m.w2item = h->d_w2item;
-  }
+  m.shape1 = m.shape2 = 0;
   h->alg_bytes = (double)P.factor_elems * esz + (double)h->n * 8 * 2;
   prepare_stream_kernels();
   CK(cudaGetLastError());
+  int rc = autotune_stream_shapes(h);
+  if (rc) {
+    hbi_free_lh(h);
+    return rc;
+  }
   *out = h;
   return HBI_OK;
 }
@@ -656,10 +885,15 @@ extern "C" int hbi_free_lh(hbi_lhp* h) {
   for (void* p : {h->d_vstore, h->d_ustore, (void*)h->d_s1, (void*)h->d_s2, (void*)h->d_cnt, h->d_part, h->d_z,
                   h->d_gpart, (void*)h->d_midx, (void*)h->d_grow0, (void*)h->d_gndl, (void*)h->d_gnch,
                   (void*)h->d_gpoff, (void*)h->d_row_fc, (void*)h->d_fc_ptr, (void*)h->d_fc_group, (void*)h->d_err,
-                  (void*)h->d_w1off, (void*)h->d_w1item, (void*)h->d_w2off, (void*)h->d_w2item,
                   (void*)h->d_fcb_ptr, (void*)h->d_fcb_base,
                   (void*)h->d_x, (void*)h->d_y})
     if (p) cudaFree(p);
+  for (int sh = 0; sh < kNumShapes1; sh++)
+    for (void* p : {(void*)h->d_w1off[sh], (void*)h->d_w1item[sh]})
+      if (p) cudaFree(p);
+  for (int sh = 0; sh < kNumShapes2; sh++)
+    for (void* p : {(void*)h->d_w2off[sh], (void*)h->d_w2item[sh]})
+      if (p) cudaFree(p);
   delete h;
   return HBI_OK;
 }
@@ -1157,7 +1391,12 @@ extern "C" int hbi_plan_emulate(int n, int nleaf, const int* lv6, const double* 
     for (const SegCopy& c : map) {
       if (c.dst < 0 || c.dst + c.len > (int64_t)dst.size() || c.dst % vec) return fail(HBI_ERR_STATE, "copy dst");
       if (c.src < 0 || c.src + (int64_t)(c.len - 1) * c.stride >= off) return fail(HBI_ERR_STATE, "copy src");
-      for (int r = 0; r < c.len; r++) dst[c.dst + r] = body[c.src + (int64_t)r * c.stride];
+      if (c.swz < 0 || c.swz >= 8 || (w == 1 && c.swz != 0)) return fail(HBI_ERR_STATE, "copy swizzle");
+      for (int r = 0; r < c.len; r++) {
+        const int64_t d = c.dst + (int64_t)(((r / vec) ^ c.swz) * vec + r % vec);
+        if (d >= (int64_t)dst.size()) return fail(HBI_ERR_STATE, "swizzled copy dst");
+        dst[d] = body[c.src + (int64_t)r * c.stride];
+      }
     }
     nseg_conv += (int64_t)map.size();
   }
@@ -1169,9 +1408,16 @@ extern "C" int hbi_plan_emulate(int n, int nleaf, const int* lv6, const double* 
         (it.ntile > 1 && (it.cg < 0 || it.cg >= P.ncg || it.poff < 0 ||
                           it.poff + (int64_t)it.ntile * it.ncols > P.plen1)))
       return fail(HBI_ERR_STATE, "phase-1 item out of bounds");
+    const int nq = it.ntp / vec;
     for (int c = 0; c < it.ncols; c++) {
+      // the kernels find logical row r of column c at its swizzled place
+      const int sw = vswz(c, nq);
+      // every swizzled vector index stays inside the column's segment
+      for (int k = 0; k < nq; k++)
+        if ((k ^ sw) >= nq) return fail(HBI_ERR_STATE, "phase-1 swizzle leaves the segment");
       double t = 0.0;
-      for (int r = 0; r < it.nt; r++) t += V[it.soff + (int64_t)c * it.ntp + r] * x[it.x0 + r];
+      for (int r = 0; r < it.nt; r++)
+        t += V[it.soff + (int64_t)c * it.ntp + ((r / vec) ^ sw) * vec + r % vec] * x[it.x0 + r];
       if (it.ntile == 1) z[it.z0 + c] = t;
       else part[it.poff + (int64_t)it.tile * it.ncols + c] = t;
     }

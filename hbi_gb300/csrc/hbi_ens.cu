@@ -256,7 +256,10 @@ __global__ void __launch_bounds__(256, 2) p1e_kernel(EnsMat A, EnsMat B, int nma
 #pragma unroll
         for (int q = 0; q < 4; q++) {
           if (!ok[q]) continue;
-          const float4 v = *(const float4*)(V + (base + warp + 8 * q) * Dc.ntp + r);
+          // the V store's swizzle (vswz) of column base + warp + 8q; chunks
+          // start at multiples of 32 columns, so chunk and item columns agree mod 8
+          const int cl = base + warp + 8 * q;
+          const float4 v = *(const float4*)(V + cl * Dc.ntp + (((r >> 2) ^ vswz(cl, Dc.ntp >> 2)) << 2));
           acc[q][0] += v.x * x0[0] + v.y * x0[1] + v.z * x0[2] + v.w * x0[3];
           acc[q][1] += v.x * x1[0] + v.y * x1[1] + v.z * x1[2] + v.w * x1[3];
         }

@@ -48,6 +48,25 @@ enum { ST_F64 = 0, ST_F32 = 1, ST_BF16 = 2 };
 // bound of the product kernels' bulk-copy waits: about one second of SM clock
 constexpr long long kWaitCyclesDefault = 2LL << 30;
 
+// Launch shapes of the phase kernels: warps per block (one block per SM),
+// shared-memory stages per warp and bytes per stage, and a variant: for phase
+// 1 the lane mapping (0: the lanes of a column segment split its rows and
+// reduce by shuffles; 1: one lane per column, no cross-lane reduction), for
+// phase 2 how far ahead the multipliers are gathered (0: one chunk, 1: two).  Every shape
+// is compiled for every storage type; hbi_construct_lh times them on the
+// operator and keeps the fastest per phase (autotune_stream_shapes).  Shape
+// 0 of each phase is the default.
+struct StreamShape {
+  int nw, ns, sb, map;
+};
+constexpr int kNumShapes1 = 6, kNumShapes2 = 5, kMaxShapes = 6;
+constexpr StreamShape kShapes1[kNumShapes1] = {{12, 2, 8192, 0}, {8, 3, 8192, 0}, {6, 2, 16384, 0},
+                                               {12, 2, 8192, 1}, {8, 3, 8192, 1}, {6, 2, 16384, 1}};
+constexpr StreamShape kShapes2[kNumShapes2] = {{12, 2, 8192, 0}, {8, 3, 8192, 0}, {6, 2, 16384, 0},
+                                               {10, 2, 8192, 0}, {8, 3, 8192, 1}};
+inline const StreamShape& stream_shape(int phase, int s) { return phase == 1 ? kShapes1[s] : kShapes2[s]; }
+inline int num_shapes(int phase) { return phase == 1 ? kNumShapes1 : kNumShapes2; }
+
 // work items of the streamed product (plan_stream in hbi_structure.cpp)
 typedef S1Item S1ItemDev;
 typedef S2Item S2ItemDev;
@@ -76,10 +95,12 @@ struct MatDev {            // one H-matrix on the device
   int* err;                // set to nonzero when a bulk copy did not arrive in time
   long long wait;          // bound of a stage wait in SM clock cycles (0: one non-blocking probe)
   int ncnt;                // number of arrival counters in cnt
-  // static warp schedules (hbi_structure.hpp, plan_warp_schedule) for a grid
-  // of gw1 / gw2 warps: warp w walks item[off[w] .. off[w+1]) of its phase
-  const int32_t *w1off, *w1item, *w2off, *w2item;
-  int gw1, gw2;
+  // static warp schedules (hbi_structure.hpp, plan_warp_schedule), one per
+  // launch shape s, for a grid of gw1[s] / gw2[s] warps: warp w walks
+  // item[off[w] .. off[w+1]) of its phase
+  const int32_t *w1off[kNumShapes1], *w1item[kNumShapes1], *w2off[kNumShapes2], *w2item[kNumShapes2];
+  int gw1[kNumShapes1], gw2[kNumShapes2];
+  int shape1, shape2;      // launch shapes of phases 1 and 2 (indices into kShapes1 / kShapes2)
 };
 
 // RK (Cash-Karp) stage state on the device; all arrays in cluster order
@@ -123,9 +144,12 @@ struct RkView {
 void launch_segcopy(const double* body, const SegCopyDev* map, int64_t nmap, void* dst, int storage,
                     cudaStream_t st);
 void prepare_stream_kernels();
-// the phase kernels' launch shape: warps per block and bytes per stage
-int stream_warps_per_block();
-int stream_stage_bytes();
+// the shape index of `phase` forced by HBI_STREAM_SHAPE1 / HBI_STREAM_SHAPE2, or -1
+int forced_stream_shape(int phase);
+// one phase (1 or 2) of the product with launch shape `shape` (the grid of
+// m0's schedule for it; m1, when nmat == 2, has one for the same shape)
+void launch_phase_shape(int phase, int shape, const MatDev* mats, int nmat, const double* x, int sm_count,
+                        cudaStream_t st);
 void launch_phase1(const MatDev* mats, int nmat, const double* x, int sm_count, cudaStream_t st);
 void launch_phase2(const MatDev* mats, int nmat, const double* x, int sm_count, cudaStream_t st);
 void launch_phase3_plain(const MatDev* mats, int nmat, double* const* y, cudaStream_t st);

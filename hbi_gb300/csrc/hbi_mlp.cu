@@ -4,7 +4,10 @@
 // The network is nin -> hid -> hid -> 1 with tanh hidden layers and a linear
 // output, parameters packed [W1(hid x nin) b1 W2(hid x hid) b2 W3(hid) b3]
 // row-major (the same packing the time loop's proposer reads).  The loss is
-// the mean squared error over a minibatch.
+// the mean over a minibatch of the squared error, or (hbi_mlp_set_loss) of
+// the pinball loss of quantile tau: (1 - tau) r for r = out - t > 0, -tau r
+// otherwise, whose minimiser is the tau-quantile of the target given the
+// inputs.
 //
 //   mlp_forward_kernel   one thread per sample: activations A1, A2, output,
 //                        and the backpropagated deltas D2, D1 (weights in
@@ -43,7 +46,7 @@ __global__ void __launch_bounds__(128) mlp_forward_kernel(const float* __restric
                                                           float* __restrict__ A1, float* __restrict__ A2,
                                                           float* __restrict__ D1, float* __restrict__ D2,
                                                           float* __restrict__ DY, float* __restrict__ R,
-                                                          float* __restrict__ Y) {
+                                                          float* __restrict__ Y, float tau) {
   extern __shared__ float sp[];
   const int np = mlp_nparams(nin, hid);
   for (int i = threadIdx.x; i < np; i += blockDim.x) sp[i] = P[i];
@@ -76,8 +79,16 @@ __global__ void __launch_bounds__(128) mlp_forward_kernel(const float* __restric
   if (Y) Y[s] = y;
   if (!T) return;
   const float r = y - T[row];
-  R[s] = r;
-  const float dy = 2.0f * r / (float)batch;
+  // per-sample loss and its derivative in the output (a subgradient of 0 at
+  // r = 0 for the pinball loss)
+  float dy;
+  if (tau > 0.0f) {
+    R[s] = r > 0.0f ? (1.0f - tau) * r : -tau * r;
+    dy = (r > 0.0f ? 1.0f - tau : (r < 0.0f ? -tau : 0.0f)) / (float)batch;
+  } else {
+    R[s] = r * r;
+    dy = 2.0f * r / (float)batch;
+  }
   DY[s] = dy;
   // D2 = dy W3 (1 - a2^2); D1 = (W2^T D2) (1 - a1^2)
   for (int o = 0; o < hid; o++) {
@@ -140,7 +151,7 @@ __global__ void mlp_adam_kernel(float* __restrict__ P, const float* __restrict__
 __global__ void mlp_loss_kernel(const float* __restrict__ R, int batch, float* __restrict__ loss) {
   __shared__ double sh[256];
   double s = 0.0;
-  for (int i = threadIdx.x; i < batch; i += blockDim.x) s += (double)R[i] * (double)R[i];
+  for (int i = threadIdx.x; i < batch; i += blockDim.x) s += (double)R[i];
   sh[threadIdx.x] = s;
   __syncthreads();
   for (int o = blockDim.x / 2; o > 0; o >>= 1) {
@@ -175,6 +186,7 @@ struct hbi_mlp_s {
   float *X = nullptr, *T = nullptr, *loss = nullptr;
   int* idx = nullptr;
   long long step = 0;
+  float tau = -1.0f;  // <= 0: squared error; in (0, 1): pinball loss of that quantile
   cudaStream_t st = nullptr;
 };
 
@@ -198,7 +210,8 @@ int ensure_data(hbi_mlp* m, long long n) {
 void launch_fwd(hbi_mlp* m, const int* idx, int b, bool with_target) {
   const size_t shm = sizeof(float) * m->np;
   mlp_forward_kernel<<<(b + 127) / 128, 128, shm, m->st>>>(m->P, m->nin, m->hid, m->X, with_target ? m->T : nullptr,
-                                                          idx, b, m->A1, m->A2, m->D1, m->D2, m->DY, m->R, m->Y);
+                                                          idx, b, m->A1, m->A2, m->D1, m->D2, m->DY, m->R, m->Y,
+                                                          m->tau);
 }
 
 void launch_bwd(hbi_mlp* m, const int* idx, int b) {
@@ -267,6 +280,12 @@ extern "C" int hbi_mlp_get_params(hbi_mlp* m, float* p) {
   if (!m || !p) return mfail(HBI_ERR_ARG, "null");
   MCK(cudaMemcpyAsync(p, m->P, sizeof(float) * m->np, cudaMemcpyDeviceToHost, m->st));
   MCK(cudaStreamSynchronize(m->st));
+  return HBI_OK;
+}
+
+extern "C" int hbi_mlp_set_loss(hbi_mlp* m, float tau) {
+  if (!m || !(tau < 1.0f)) return mfail(HBI_ERR_ARG, "hbi_mlp_set_loss: tau must be below 1");
+  m->tau = tau > 0.0f ? tau : -1.0f;
   return HBI_OK;
 }
 

@@ -193,21 +193,21 @@ struct WarpSeq {
   }
 };
 
-__device__ __forceinline__ WarpSeq warp_seq(const MatDev& m0, const MatDev& m1, int nmat, int phase, int gw, int GW,
-                                            int n0, int ntot) {
+__device__ __forceinline__ WarpSeq warp_seq(const MatDev& m0, const MatDev& m1, int nmat, int phase, int shape,
+                                            int gw, int GW, int n0, int ntot) {
   WarpSeq q;
   q.n0 = n0;
   q.gw = gw;
   q.GW = GW;
   q.ntot = ntot;
-  const int32_t* off0 = phase == 1 ? m0.w1off : m0.w2off;
-  const int32_t* off1 = phase == 1 ? m1.w1off : m1.w2off;
-  const int g0 = phase == 1 ? m0.gw1 : m0.gw2, g1 = phase == 1 ? m1.gw1 : m1.gw2;
+  const int32_t* off0 = phase == 1 ? m0.w1off[shape] : m0.w2off[shape];
+  const int32_t* off1 = phase == 1 ? m1.w1off[shape] : m1.w2off[shape];
+  const int g0 = phase == 1 ? m0.gw1[shape] : m0.gw2[shape], g1 = phase == 1 ? m1.gw1[shape] : m1.gw2[shape];
   if (off0 && g0 == GW && (nmat == 1 || (off1 && g1 == GW))) {
-    q.a0 = (phase == 1 ? m0.w1item : m0.w2item) + __ldg(&off0[gw]);
+    q.a0 = (phase == 1 ? m0.w1item[shape] : m0.w2item[shape]) + __ldg(&off0[gw]);
     q.len0 = __ldg(&off0[gw + 1]) - __ldg(&off0[gw]);
     if (nmat == 2) {
-      q.a1 = (phase == 1 ? m1.w1item : m1.w2item) + __ldg(&off1[gw]);
+      q.a1 = (phase == 1 ? m1.w1item[shape] : m1.w2item[shape]) + __ldg(&off1[gw]);
       q.len1 = __ldg(&off1[gw + 1]) - __ldg(&off1[gw]);
     }
   }
@@ -220,10 +220,17 @@ __device__ __forceinline__ WarpSeq warp_seq(const MatDev& m0, const MatDev& m1, 
 // Item = one row tile of a column group over all its columns; streamed in
 // chunks of up to SB bytes.  Column sums of a chunk go to z (one tile) or to
 // the tile's partials; the last tile of the group to finish sums the
-// partials.
-template <typename T, int NW, int NS, int SB>
+// partials.  The V store is swizzled per column segment (vswz): logical
+// 16-byte vector k of column c sits at k ^ vswz(c, ntp / VEC).
+//
+// MAP 0: the LW lanes of a column segment split its rows (one vector each)
+// and reduce by shuffles; CS = 32 / LW columns side by side.
+// MAP 1: one lane per column (two lanes, each half the rows, when a chunk has
+// only 16 columns), the item's x tile in the warp's shared-memory buffer:
+// no cross-lane reduction, VEC independent accumulator chains per lane.
+template <typename T, int NW, int NS, int SB, int MAP>
 __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev m1, int nmat,
-                                                               const double* __restrict__ x) {
+                                                               const double* __restrict__ x, int shape) {
   typedef typename AccT<T>::type Acc;
   constexpr int VEC = 16 / sizeof(T);
   constexpr int ESZ = sizeof(T);
@@ -232,6 +239,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
   if (m0.skip && __ldcg(m0.skip)) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   Ring<NW, NS, SB> R(smem, warp);
+  Acc* xs = (Acc*)R.mu;  // MAP 1: the current item's x tile (32 x VEC values)
   if (lane == 0) {
     for (int s = 0; s < NS; s++) mbar_init(&R.bar[s], 1);
     fence_mbar_init();
@@ -239,12 +247,16 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
   __syncwarp();
   const int gw = blockIdx.x * NW + warp, GW = gridDim.x * NW;
   const int n0 = m0.ns1, ntot = nmat == 2 ? n0 + m1.ns1 : n0;
+  // the item's chunk width follows from this shape's stage size
   auto desc = [&](int it) -> S1ItemDev {
     S1ItemDev d{};
-    if (it < ntot) d = it < n0 ? m0.s1[it] : m1.s1[it - n0];
+    if (it < ntot) {
+      d = it < n0 ? m0.s1[it] : m1.s1[it - n0];
+      d.cc = chunk_cols(d.ntp, ESZ, SB);
+    }
     return d;
   };
-  const WarpSeq seq = warp_seq(m0, m1, nmat, 1, gw, GW, n0, ntot);
+  const WarpSeq seq = warp_seq(m0, m1, nmat, 1, shape, gw, GW, n0, ntot);
   // producer: walks this warp's items chunk by chunk, NS chunks ahead; the
   // item ids are fetched two items ahead, the descriptors one
   int p_k = 0, p_it = seq.at(0), p_itn = seq.at(1), p_itnn = seq.at(2), p_c0 = 0, p_seq = 0;
@@ -276,8 +288,10 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
   // consumer: item ids three ahead, descriptors two
   int c_k = 0, c_it = seq.at(0), c_i1 = seq.at(1), c_i2 = seq.at(2), c_i3 = seq.at(3), c_c0 = 0, c_seq = 0;
   S1ItemDev Dc = desc(c_it), Dn = desc(c_i1), Dnn = desc(c_i2);
+  // x rows of an item: MAP 0, lane j of each column slot holds rows
+  // j*VEC .. j*VEC+VEC-1; MAP 1, lane L holds rows L*VEC .. (for the tile)
   auto load_x = [&](const S1ItemDev& D, Acc* xv) {
-    const int lw = log2ceil(max(1, D.ntp / VEC));
+    const int lw = MAP == 1 ? 5 : log2ceil(max(1, D.ntp / VEC));
     const int j = lane & ((1 << lw) - 1);
 #pragma unroll
     for (int v = 0; v < VEC; v++) {
@@ -285,9 +299,18 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
       xv[v] = (D.ncols > 0 && r < D.nt) ? (Acc)__ldg(&x[D.x0 + r]) : Acc(0);
     }
   };
+  auto put_x = [&](const Acc* xv) {
+    if constexpr (MAP == 1) {
+      __syncwarp();
+#pragma unroll
+      for (int v = 0; v < VEC; v++) xs[lane * VEC + v] = xv[v];
+      __syncwarp();
+    }
+  };
   Acc xc[VEC], xn[VEC];
   load_x(Dc, xc);
   load_x(Dn, xn);
+  put_x(xc);
   // the arrival of a finished multi-tile item is resolved one chunk later, so
   // that the atomic's round trip overlaps the next chunk
   int pend_old = 0, pend_cg = -1, pend_ntile = 0, pend_ncols = 0, pend_poff = 0, pend_z0 = 0, pend_sec = 0;
@@ -318,86 +341,134 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
     }
     const int nc = min(Dc.cc, Dc.ncols - c_c0);
     const T* st = (const T*)(R.buf + s * SB);
-    const int nq = Dc.ntp / VEC;
-    const int lw = log2ceil(nq), LW = 1 << lw, CS = 32 >> lw;
-    const int slot = lane >> lw, j = lane & (LW - 1);
+    const int nq = Dc.ntp / VEC;  // 16-byte vectors per column segment
     Acc* z = (Acc*)M.z;
     Acc* part = (Acc*)M.part;
-    if (LW == 32) {
-      // tall tiles: BF columns at a time, reduced by a butterfly
-      // reduce-scatter inside groups of BF lanes (BF-1 shuffle-adds per lane
-      // for BF columns), then across the groups; lane L ends with the sum of
-      // column r0 + L % BF
-      for (int r0 = 0; r0 < nc; r0 += BF) {
-        Acc p[BF];
-        if (nq == 32 && r0 + BF <= nc) {
-          // a full block of BF full-height columns: no predicates
+    auto put = [&](int col, Acc v) {
+      if (Dc.ntile == 1) z[Dc.z0 + col] = v;
+      else part[Dc.poff + (int64_t)Dc.tile * Dc.ncols + col] = v;
+    };
+    if constexpr (MAP == 1) {
+      if (Dc.cc <= 16) {
+        // 16 columns per chunk: lanes L and L + 16 take halves of column L's
+        // vectors (their logical indices; the swizzle permutes within the column)
+        const int h = lane >> 4, cl = lane & 15;
+        const int half = (nq + 1) >> 1;
+        const int k0 = h ? half : 0, k1 = h ? nq : half;
+        Acc acc[VEC];
 #pragma unroll
-          for (int u = 0; u < BF; u++) {
+        for (int v = 0; v < VEC; v++) acc[v] = 0;
+        if (cl < nc) {
+          const T* cp = st + cl * Dc.ntp;
+          const int sw = vswz(cl, nq);
+#pragma unroll 4
+          for (int k = k0; k < k1; k++) {
+            const int ph = k ^ sw;
             Acc a[VEC];
-            lds16(st + (r0 + u) * (32 * VEC) + lane * VEC, a);
-            p[u] = a[0] * xc[0];
+            lds16(cp + ph * VEC, a);
 #pragma unroll
-            for (int v = 1; v < VEC; v++) p[u] += a[v] * xc[v];
+            for (int v = 0; v < VEC; v++) acc[v] += a[v] * xs[k * VEC + v];
           }
-        } else {
+        }
+        Acc t = acc[0];
 #pragma unroll
-          for (int u = 0; u < BF; u++) {
-            p[u] = 0;
-            if (r0 + u < nc && j < nq) {
+        for (int v = 1; v < VEC; v++) t += acc[v];
+        t += __shfl_xor_sync(0xffffffffu, t, 16);
+        if (h == 0 && cl < nc) put(c_c0 + cl, t);
+      } else {
+        // one lane per column, columns lane, lane + 32, ...
+        for (int cl = lane; cl < nc; cl += 32) {
+          const T* cp = st + cl * Dc.ntp;
+          const int sw = vswz(cl, nq);
+          Acc acc[VEC];
+#pragma unroll
+          for (int v = 0; v < VEC; v++) acc[v] = 0;
+#pragma unroll 4
+          for (int k = 0; k < nq; k++) {
+            const int ph = k ^ sw;
+            Acc a[VEC];
+            lds16(cp + ph * VEC, a);
+#pragma unroll
+            for (int v = 0; v < VEC; v++) acc[v] += a[v] * xs[k * VEC + v];
+          }
+          Acc t = acc[0];
+#pragma unroll
+          for (int v = 1; v < VEC; v++) t += acc[v];
+          put(c_c0 + cl, t);
+        }
+      }
+    } else {
+      const int lw = log2ceil(nq), LW = 1 << lw, CS = 32 >> lw;
+      const int slot = lane >> lw, j = lane & (LW - 1);
+      if (LW == 32) {
+        // tall tiles: BF columns at a time, reduced by a butterfly
+        // reduce-scatter inside groups of BF lanes (BF-1 shuffle-adds per lane
+        // for BF columns), then across the groups; lane L ends with the sum of
+        // column r0 + L % BF
+        for (int r0 = 0; r0 < nc; r0 += BF) {
+          Acc p[BF];
+          if (nq == 32 && r0 + BF <= nc) {
+            // a full block of BF full-height columns: no predicates; the
+            // swizzle of column r0 + u is u & 7 (r0 is a multiple of 16)
+#pragma unroll
+            for (int u = 0; u < BF; u++) {
               Acc a[VEC];
-              lds16(st + (r0 + u) * Dc.ntp + j * VEC, a);
+              lds16(st + (r0 + u) * (32 * VEC) + (lane ^ (u & 7)) * VEC, a);
+              p[u] = a[0] * xc[0];
 #pragma unroll
-              for (int v = 0; v < VEC; v++) p[u] += a[v] * xc[v];
+              for (int v = 1; v < VEC; v++) p[u] += a[v] * xc[v];
+            }
+          } else {
+#pragma unroll
+            for (int u = 0; u < BF; u++) {
+              p[u] = 0;
+              if (r0 + u < nc && j < nq) {
+                Acc a[VEC];
+                lds16(st + (r0 + u) * Dc.ntp + (j ^ vswz(r0 + u, nq)) * VEC, a);
+#pragma unroll
+                for (int v = 0; v < VEC; v++) p[u] += a[v] * xc[v];
+              }
             }
           }
-        }
 #pragma unroll
-        for (int lev = BF / 2; lev >= 1; lev >>= 1) {
-          const bool upper = (lane & lev) != 0;
+          for (int lev = BF / 2; lev >= 1; lev >>= 1) {
+            const bool upper = (lane & lev) != 0;
 #pragma unroll
-          for (int i = 0; i < lev; i++) {
-            const Acc send = upper ? p[i] : p[i + lev];
-            const Acc keep = upper ? p[i + lev] : p[i];
-            p[i] = keep + __shfl_xor_sync(0xffffffffu, send, lev);
+            for (int i = 0; i < lev; i++) {
+              const Acc send = upper ? p[i] : p[i + lev];
+              const Acc keep = upper ? p[i + lev] : p[i];
+              p[i] = keep + __shfl_xor_sync(0xffffffffu, send, lev);
+            }
           }
+#pragma unroll
+          for (int o = BF; o < 32; o <<= 1) p[0] += __shfl_xor_sync(0xffffffffu, p[0], o);
+          if (lane < BF && r0 + lane < nc) put(c_c0 + r0 + lane, p[0]);
         }
-#pragma unroll
-        for (int o = BF; o < 32; o <<= 1) p[0] += __shfl_xor_sync(0xffffffffu, p[0], o);
-        if (lane < BF && r0 + lane < nc) {
-          const int col = c_c0 + r0 + lane;
-          if (Dc.ntile == 1) z[Dc.z0 + col] = p[0];
-          else part[Dc.poff + (int64_t)Dc.tile * Dc.ncols + col] = p[0];
-        }
-      }
-    } else
-    // eight columns per slot at a time, so that their lane reductions
-    // (shuffle chains) proceed side by side
-    for (int r0 = 0; r0 < nc; r0 += 8 * CS) {
-      constexpr int UC_ = 8;
-      Acc p[UC_];
-#pragma unroll
-      for (int u = 0; u < UC_; u++) {
-        const int sg = r0 + u * CS + slot;
-        p[u] = 0;
-        if (sg < nc && j < nq) {
-          Acc a[VEC];
-          lds16(st + sg * Dc.ntp + j * VEC, a);
-#pragma unroll
-          for (int v = 0; v < VEC; v++) p[u] += a[v] * xc[v];
-        }
-      }
-      for (int o = 1; o < LW; o <<= 1)
-#pragma unroll
-        for (int u = 0; u < UC_; u++) p[u] += __shfl_xor_sync(0xffffffffu, p[u], o);
-      if (j == 0) {
+      } else
+      // eight columns per slot at a time, so that their lane reductions
+      // (shuffle chains) proceed side by side
+      for (int r0 = 0; r0 < nc; r0 += 8 * CS) {
+        constexpr int UC_ = 8;
+        Acc p[UC_];
 #pragma unroll
         for (int u = 0; u < UC_; u++) {
           const int sg = r0 + u * CS + slot;
-          if (sg < nc) {
-            const int col = c_c0 + sg;
-            if (Dc.ntile == 1) z[Dc.z0 + col] = p[u];
-            else part[Dc.poff + (int64_t)Dc.tile * Dc.ncols + col] = p[u];
+          p[u] = 0;
+          if (sg < nc && j < nq) {
+            Acc a[VEC];
+            lds16(st + sg * Dc.ntp + (j ^ vswz(sg, nq)) * VEC, a);
+#pragma unroll
+            for (int v = 0; v < VEC; v++) p[u] += a[v] * xc[v];
+          }
+        }
+        for (int o = 1; o < LW; o <<= 1)
+#pragma unroll
+          for (int u = 0; u < UC_; u++) p[u] += __shfl_xor_sync(0xffffffffu, p[u], o);
+        if (j == 0) {
+#pragma unroll
+          for (int u = 0; u < UC_; u++) {
+            const int sg = r0 + u * CS + slot;
+            if (sg < nc) put(c_c0 + sg, p[u]);
           }
         }
       }
@@ -430,6 +501,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
     Dn = Dnn;
 #pragma unroll
     for (int v = 0; v < VEC; v++) xc[v] = xn[v];
+    put_x(xc);
     load_x(Dn, xn);
     Dnn = desc(c_i2);
   }
@@ -444,14 +516,20 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
 // neither latency falls between a stage's arrival and its use.  Lanes
 // accumulate their rows over the item's chunks; one reduction over the
 // column slots per item.
-template <typename T, int NW, int NS, int SB>
+//
+// GA: how many chunks ahead the multipliers are gathered (1, or 2 with three
+// or more stages: the indices of chunk c + 2 are in the FIFO when chunk c
+// starts); two register sets of multipliers then cover two chunk times of
+// load latency.
+template <typename T, int NW, int NS, int SB, int GA>
 __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev m1, int nmat,
-                                                               const double* __restrict__ x) {
+                                                               const double* __restrict__ x, int shape) {
   typedef typename AccT<T>::type Acc;
   constexpr int VEC = 16 / sizeof(T);
   constexpr int ESZ = sizeof(T);
   constexpr int KP = kMaxCols / 32;  // multipliers per lane of one chunk
   static_assert(NS >= 2, "the multiplier gather runs one chunk ahead");
+  static_assert(GA == 1 || (GA == 2 && NS >= 3), "a gather two chunks ahead needs three stages");
   extern __shared__ __align__(128) unsigned char smem[];
   if (m0.skip && __ldcg(m0.skip)) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -466,7 +544,10 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
   const int n0 = m0.ns2, ntot = nmat == 2 ? n0 + m1.ns2 : n0;
   auto desc = [&](int it) -> S2ItemDev {
     S2ItemDev d{};
-    if (it < ntot) d = it < n0 ? m0.s2[it] : m1.s2[it - n0];
+    if (it < ntot) {
+      d = it < n0 ? m0.s2[it] : m1.s2[it - n0];
+      d.cc = chunk_cols(d.ntp, ESZ, SB);
+    }
     return d;
   };
   // column indices of a chunk in flight: lane L holds columns L + 32 i
@@ -474,7 +555,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
     int32_t idx[KP];
     int nc, sec;
   };
-  const WarpSeq seq = warp_seq(m0, m1, nmat, 2, gw, GW, n0, ntot);
+  const WarpSeq seq = warp_seq(m0, m1, nmat, 2, shape, gw, GW, n0, ntot);
   int p_k = 0, p_it = seq.at(0), p_itn = seq.at(1), p_itnn = seq.at(2), p_c0 = 0, p_seq = 0;
   S2ItemDev Dp = desc(p_it), Dpn = desc(p_itn);
   auto produce = [&](Pend& pd) {
@@ -525,8 +606,9 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
   Pend fifo[NS];
 #pragma unroll
   for (int q = 0; q < NS; q++) produce(fifo[q]);
-  Acc mu[KP];
+  Acc mu[KP], mu2[KP];
   gather(fifo[0], mu);
+  if constexpr (GA == 2) gather(fifo[1], mu2);
   int c_k = 0, c_it = seq.at(0), c_i1 = seq.at(1), c_i2 = seq.at(2), c_c0 = 0, c_seq = 0;
   S2ItemDev Dc = desc(c_it), Dn = desc(c_i1);
   Acc acc[VEC];
@@ -546,7 +628,13 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
 #pragma unroll
     for (int i = 0; i < KP; i++) musm[lane + 32 * i] = mu[i];
     __syncwarp();
-    gather(fifo[1], mu);
+    if constexpr (GA == 2) {
+#pragma unroll
+      for (int i = 0; i < KP; i++) mu[i] = mu2[i];
+      gather(fifo[2], mu2);
+    } else {
+      gather(fifo[1], mu);
+    }
     const int nq = Dc.ntp / VEC;
     const int lw = log2ceil(nq), LW = 1 << lw, CS = 32 >> lw;
     const int slot = lane >> lw, j = lane & (LW - 1);
@@ -611,7 +699,8 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
 }
 
 // ------------------------------------------------------ store conversion
-// one warp per column segment: dst[r] = (T) body[src + r * stride], r < len
+// one warp per column segment: dst[r'] = (T) body[src + r * stride], r < len,
+// with r' the row's place under the segment's vector swizzle
 template <typename T>
 __global__ void segcopy_kernel(const double* __restrict__ body, const SegCopyDev* __restrict__ map, int64_t nmap,
                                T* __restrict__ dst) {
@@ -620,11 +709,13 @@ __global__ void segcopy_kernel(const double* __restrict__ body, const SegCopyDev
   const int64_t nw = (gridDim.x * (int64_t)blockDim.x) >> 5;
   for (int64_t q = w; q < nmap; q += nw) {
     const SegCopyDev c = map[q];
+    constexpr int VEC = 16 / sizeof(T);
     for (int r = lane; r < c.len; r += 32) {
       const double v = body[c.src + (int64_t)r * c.stride];
-      if constexpr (sizeof(T) == 8) dst[c.dst + r] = v;
-      else if constexpr (sizeof(T) == 4) dst[c.dst + r] = (float)v;
-      else dst[c.dst + r] = __double2bfloat16(v);
+      const int64_t d = c.dst + ((r / VEC) ^ c.swz) * VEC + r % VEC;
+      if constexpr (sizeof(T) == 8) dst[d] = v;
+      else if constexpr (sizeof(T) == 4) dst[d] = (float)v;
+      else dst[d] = __double2bfloat16(v);
     }
   }
 }
@@ -651,74 +742,93 @@ void set_smem_once(K kernel, size_t bytes) {
   if (ndone < 64) done[ndone++] = (const void*)kernel;
 }
 
-// pipeline shape, HBI_STREAM_SHAPE: 0 = 12 warps x 2 stages x 8 KB (default),
-// 1 = 6 warps x 2 stages x 16 KB, 2 = 8 warps x 3 stages x 8 KB
-int stream_shape() {
-  static int shape = -1;
-  if (shape < 0) {
-    const char* e = getenv("HBI_STREAM_SHAPE");
-    shape = e ? atoi(e) : 0;
-    if (shape < 0 || shape > 2) shape = 0;
+// HBI_STREAM_SHAPE1=s / HBI_STREAM_SHAPE2=s force launch shape s of phase 1 /
+// phase 2 for every operator
+int env_shape(int phase) {
+  static int shape[2] = {-2, -2};
+  int& v = shape[phase - 1];
+  if (v == -2) {
+    const char* e = getenv(phase == 1 ? "HBI_STREAM_SHAPE1" : "HBI_STREAM_SHAPE2");
+    v = e ? atoi(e) : -1;
+    if (v < -1 || v >= num_shapes(phase)) v = -1;
   }
-  return shape;
+  return v;
 }
 
-}  // namespace
-
-int stream_warps_per_block() { return stream_shape() == 1 ? 6 : stream_shape() == 2 ? 8 : 12; }
-int stream_stage_bytes() { return stream_shape() == 1 ? 16384 : 8192; }
-
-namespace {
-
-template <typename T, int NW, int NS, int SB>
-void launch_p1_shape(const MatDev& m0, const MatDev& m1, int nmat, const double* x, int sm, int n, cudaStream_t st) {
+template <typename T, int S>
+void launch_p1s(const MatDev& m0, const MatDev& m1, int nmat, const double* x, int sm, int n, cudaStream_t st) {
+  constexpr int NW = kShapes1[S].nw, NS = kShapes1[S].ns, SB = kShapes1[S].sb, MAP = kShapes1[S].map;
   const int need = (n + NW - 1) / NW;
   const int grid = need < sm ? (need > 0 ? need : 1) : sm;
-  set_smem_once(p1_stream_kernel<T, NW, NS, SB>, smem_bytes<NW, NS, SB>());
-  p1_stream_kernel<T, NW, NS, SB><<<grid, NW * 32, smem_bytes<NW, NS, SB>(), st>>>(m0, m1, nmat, x);
+  p1_stream_kernel<T, NW, NS, SB, MAP><<<grid, NW * 32, smem_bytes<NW, NS, SB>(), st>>>(m0, m1, nmat, x, S);
 }
 
-template <typename T, int NW, int NS, int SB>
-void launch_p2_shape(const MatDev& m0, const MatDev& m1, int nmat, const double* x, int sm, int n, cudaStream_t st) {
+template <typename T, int S>
+void launch_p2s(const MatDev& m0, const MatDev& m1, int nmat, const double* x, int sm, int n, cudaStream_t st) {
+  constexpr int NW = kShapes2[S].nw, NS = kShapes2[S].ns, SB = kShapes2[S].sb, GA = kShapes2[S].map + 1;
   const int need = (n + NW - 1) / NW;
   const int grid = need < sm ? (need > 0 ? need : 1) : sm;
-  set_smem_once(p2_stream_kernel<T, NW, NS, SB>, smem_bytes<NW, NS, SB>());
-  p2_stream_kernel<T, NW, NS, SB><<<grid, NW * 32, smem_bytes<NW, NS, SB>(), st>>>(m0, m1, nmat, x);
+  p2_stream_kernel<T, NW, NS, SB, GA><<<grid, NW * 32, smem_bytes<NW, NS, SB>(), st>>>(m0, m1, nmat, x, S);
 }
 
 template <typename T>
-void launch_p1(const MatDev& m0, const MatDev& m1, int nmat, const double* x, int sm, cudaStream_t st) {
-  const int n = m0.ns1 + (nmat == 2 ? m1.ns1 : 0);
+void launch_typed(int phase, int shape, const MatDev& m0, const MatDev& m1, int nmat, const double* x, int sm,
+                  cudaStream_t st) {
+  const int n = phase == 1 ? m0.ns1 + (nmat == 2 ? m1.ns1 : 0) : m0.ns2 + (nmat == 2 ? m1.ns2 : 0);
   if (n == 0) return;
-  switch (stream_shape()) {
-    case 1: launch_p1_shape<T, 6, 2, 16384>(m0, m1, nmat, x, sm, n, st); break;
-    case 2: launch_p1_shape<T, 8, 3, 8192>(m0, m1, nmat, x, sm, n, st); break;
-    default: launch_p1_shape<T, 12, 2, 8192>(m0, m1, nmat, x, sm, n, st);
+  static_assert(kNumShapes1 == 6 && kNumShapes2 == 5, "one case per shape");
+  if (phase == 1) {
+    switch (shape) {
+      case 1: launch_p1s<T, 1>(m0, m1, nmat, x, sm, n, st); break;
+      case 2: launch_p1s<T, 2>(m0, m1, nmat, x, sm, n, st); break;
+      case 3: launch_p1s<T, 3>(m0, m1, nmat, x, sm, n, st); break;
+      case 4: launch_p1s<T, 4>(m0, m1, nmat, x, sm, n, st); break;
+      case 5: launch_p1s<T, 5>(m0, m1, nmat, x, sm, n, st); break;
+      default: launch_p1s<T, 0>(m0, m1, nmat, x, sm, n, st);
+    }
+  } else {
+    switch (shape) {
+      case 1: launch_p2s<T, 1>(m0, m1, nmat, x, sm, n, st); break;
+      case 2: launch_p2s<T, 2>(m0, m1, nmat, x, sm, n, st); break;
+      case 3: launch_p2s<T, 3>(m0, m1, nmat, x, sm, n, st); break;
+      case 4: launch_p2s<T, 4>(m0, m1, nmat, x, sm, n, st); break;
+      default: launch_p2s<T, 0>(m0, m1, nmat, x, sm, n, st);
+    }
   }
 }
 
-template <typename T>
-void launch_p2(const MatDev& m0, const MatDev& m1, int nmat, const double* x, int sm, cudaStream_t st) {
-  const int n = m0.ns2 + (nmat == 2 ? m1.ns2 : 0);
-  if (n == 0) return;
-  switch (stream_shape()) {
-    case 1: launch_p2_shape<T, 6, 2, 16384>(m0, m1, nmat, x, sm, n, st); break;
-    case 2: launch_p2_shape<T, 8, 3, 8192>(m0, m1, nmat, x, sm, n, st); break;
-    default: launch_p2_shape<T, 12, 2, 8192>(m0, m1, nmat, x, sm, n, st);
-  }
+template <typename T, int S>
+void prepare_p1() {
+  constexpr int NW = kShapes1[S].nw, NS = kShapes1[S].ns, SB = kShapes1[S].sb, MAP = kShapes1[S].map;
+  static_assert(smem_bytes<NW, NS, SB>() <= 227 * 1024, "shape exceeds the shared memory of a block");
+  set_smem_once(p1_stream_kernel<T, NW, NS, SB, MAP>, smem_bytes<NW, NS, SB>());
+}
+
+template <typename T, int S>
+void prepare_p2() {
+  constexpr int NW = kShapes2[S].nw, NS = kShapes2[S].ns, SB = kShapes2[S].sb, GA = kShapes2[S].map + 1;
+  static_assert(smem_bytes<NW, NS, SB>() <= 227 * 1024, "shape exceeds the shared memory of a block");
+  set_smem_once(p2_stream_kernel<T, NW, NS, SB, GA>, smem_bytes<NW, NS, SB>());
 }
 
 template <typename T>
 void prepare_type() {
-  set_smem_once(p1_stream_kernel<T, 12, 2, 8192>, smem_bytes<12, 2, 8192>());
-  set_smem_once(p1_stream_kernel<T, 6, 2, 16384>, smem_bytes<6, 2, 16384>());
-  set_smem_once(p1_stream_kernel<T, 8, 3, 8192>, smem_bytes<8, 3, 8192>());
-  set_smem_once(p2_stream_kernel<T, 12, 2, 8192>, smem_bytes<12, 2, 8192>());
-  set_smem_once(p2_stream_kernel<T, 6, 2, 16384>, smem_bytes<6, 2, 16384>());
-  set_smem_once(p2_stream_kernel<T, 8, 3, 8192>, smem_bytes<8, 3, 8192>());
+  prepare_p1<T, 0>();
+  prepare_p1<T, 1>();
+  prepare_p1<T, 2>();
+  prepare_p1<T, 3>();
+  prepare_p1<T, 4>();
+  prepare_p1<T, 5>();
+  prepare_p2<T, 0>();
+  prepare_p2<T, 1>();
+  prepare_p2<T, 2>();
+  prepare_p2<T, 3>();
+  prepare_p2<T, 4>();
 }
 
 }  // namespace
+
+int forced_stream_shape(int phase) { return env_shape(phase); }
 
 // the large shared-memory opt-in of the phase kernels, once per process and
 // before any stream capture
@@ -728,21 +838,22 @@ void prepare_stream_kernels() {
   prepare_type<__nv_bfloat16>();
 }
 
-// both H-matrices of a stage in one grid per phase (same storage type)
-void launch_phase1(const MatDev* mats, int nmat, const double* x, int sm, cudaStream_t st) {
+void launch_phase_shape(int phase, int shape, const MatDev* mats, int nmat, const double* x, int sm, cudaStream_t st) {
   const MatDev& m0 = mats[0];
   const MatDev& m1 = nmat == 2 ? mats[1] : mats[0];
-  if (m0.storage == ST_F64) launch_p1<double>(m0, m1, nmat, x, sm, st);
-  else if (m0.storage == ST_F32) launch_p1<float>(m0, m1, nmat, x, sm, st);
-  else launch_p1<__nv_bfloat16>(m0, m1, nmat, x, sm, st);
+  if (m0.storage == ST_F64) launch_typed<double>(phase, shape, m0, m1, nmat, x, sm, st);
+  else if (m0.storage == ST_F32) launch_typed<float>(phase, shape, m0, m1, nmat, x, sm, st);
+  else launch_typed<__nv_bfloat16>(phase, shape, m0, m1, nmat, x, sm, st);
+}
+
+// both H-matrices of a stage in one grid per phase (same storage type), in
+// the launch shape chosen for the first
+void launch_phase1(const MatDev* mats, int nmat, const double* x, int sm, cudaStream_t st) {
+  launch_phase_shape(1, mats[0].shape1, mats, nmat, x, sm, st);
 }
 
 void launch_phase2(const MatDev* mats, int nmat, const double* x, int sm, cudaStream_t st) {
-  const MatDev& m0 = mats[0];
-  const MatDev& m1 = nmat == 2 ? mats[1] : mats[0];
-  if (m0.storage == ST_F64) launch_p2<double>(m0, m1, nmat, x, sm, st);
-  else if (m0.storage == ST_F32) launch_p2<float>(m0, m1, nmat, x, sm, st);
-  else launch_p2<__nv_bfloat16>(m0, m1, nmat, x, sm, st);
+  launch_phase_shape(2, mats[0].shape2, mats, nmat, x, sm, st);
 }
 
 void launch_segcopy(const double* body, const SegCopyDev* map, int64_t nmap, void* dst, int storage,

@@ -195,74 +195,6 @@ int build_structure(int n, const double* coord, const double* param_in, Structur
 
 static int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
 
-void plan_matrix(const std::vector<Leaf>& leaves, int vec, int item_elems, MatPlan& mp) {
-  // Every column of V (ndt rows), U (ndl rows) and dense A (ndl rows) is
-  // padded with zeros to a multiple of `vec` rows (vec elements = 16 bytes),
-  // so each column, and each block, starts on a 16-byte boundary and can be
-  // read with 16-byte vector loads.
-  const int nl = (int)leaves.size();
-  mp.leaf_off.assign(nl, 0);
-  mp.p1.clear(); mp.lr_leaf.clear(); mp.lr_zoff.clear(); mp.lr_nparts.clear(); mp.lr_poff.clear();
-  mp.desc.assign(nl, LeafDesc{});
-  int64_t off = 0, z = 0, pz = 0, fe = 0;
-  const int quantum = 32 * vec;  // rows one warp covers with one vector load per lane
-  for (int i = 0; i < nl; i++) {
-    const Leaf& L = leaves[i];
-    off = round_up(off, vec);
-    mp.leaf_off[i] = off;
-    LeafDesc& d = mp.desc[i];
-    const int ndlp = (int)round_up(L.ndl, vec);
-    d.row0 = L.nstrtl - 1;
-    d.ndl = ndlp;  // leading dimension of U / A
-    d.kind = L.ltmtx;
-    if (L.ltmtx == 1) {
-      const int ndtp = (int)round_up(L.ndt, vec);
-      int lr = (int)mp.lr_leaf.size();
-      // rows per phase-1 task: about item_elems elements, a multiple of quantum
-      int chunk = (int)std::max<int64_t>(quantum, (item_elems / std::max(L.kt, 1)) / quantum * quantum);
-      int nparts = (ndtp + chunk - 1) / chunk;
-      mp.lr_leaf.push_back(i);
-      mp.lr_nparts.push_back(nparts);
-      mp.lr_zoff.push_back((int32_t)z);
-      mp.lr_poff.push_back((int32_t)pz);
-      for (int p = 0; p < nparts; p++) {
-        int t0 = p * chunk;
-        P1Item it;
-        it.voff = off + t0;
-        it.ldv = ndtp;
-        it.nt = std::min(chunk, L.ndt - t0);
-        it.x0 = L.nstrtt - 1 + t0;
-        it.k0 = 0;
-        it.nk = L.kt;
-        it.leaf = lr;
-        it.part = p;
-        mp.p1.push_back(it);
-      }
-      d.off = off + (int64_t)ndtp * L.kt;  // U block follows V
-      d.kt_or_ndt = L.kt;
-      d.aux = (int32_t)z;
-      z += L.kt;
-      pz += (int64_t)L.kt * nparts;
-      off += (int64_t)L.kt * (ndlp + ndtp);
-      fe += (int64_t)L.kt * (L.ndl + L.ndt);
-    } else {
-      d.off = off;
-      d.kt_or_ndt = L.ndt;
-      d.aux = L.nstrtt - 1;
-      off += (int64_t)ndlp * L.ndt;
-      fe += (int64_t)L.ndl * L.ndt;
-    }
-  }
-  mp.store_elems = round_up(off, vec);
-  mp.zlen = z;
-  mp.plen = pz;
-  mp.factor_elems = fe;
-  // big tasks first so the static warp schedule ends evenly
-  std::stable_sort(mp.p1.begin(), mp.p1.end(), [](const P1Item& a, const P1Item& b) {
-    return (int64_t)a.nt * a.nk > (int64_t)b.nt * b.nk;
-  });
-}
-
 void plan_groups(int n, const std::vector<Leaf>& leaves, GroupPlan& gp) {
   // groups ordered by (row0 ascending, ndl descending): coarse before fine
   std::vector<std::pair<std::pair<int, int>, int>> key;
@@ -309,59 +241,6 @@ void plan_groups(int n, const std::vector<Leaf>& leaves, GroupPlan& gp) {
   }
 }
 
-void plan_p2_items(const std::vector<Leaf>& leaves, const GroupPlan& gp, int vec, std::vector<P2Item>& items) {
-  const int ng = (int)gp.grow0.size();
-  const int quantum = 32 * vec;  // rows of one task: 32 lanes x one vector each
-  std::vector<std::pair<int64_t, P2Item>> v;
-  for (int g = 0; g < ng; g++) {
-    int64_t cols = 0;
-    for (int e = gp.gleaf_ptr[g]; e < gp.gleaf_ptr[g + 1]; e++) {
-      const Leaf& L = leaves[gp.gleaf[e]];
-      cols += L.ltmtx == 1 ? L.kt : L.ndt;
-    }
-    for (int r0 = 0; r0 < gp.gndl[g]; r0 += quantum) {
-      P2Item it{g, r0, std::min(quantum, gp.gndl[g] - r0), 0};
-      v.push_back({cols * it.nr, it});
-    }
-  }
-  std::stable_sort(v.begin(), v.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
-  items.resize(v.size());
-  for (size_t i = 0; i < v.size(); i++) items[i] = v[i].second;
-}
-
-void plan_chains(int n, const std::vector<Leaf>& leaves, ChainPlan& cp) {
-  std::vector<int> bnd;
-  bnd.reserve(2 * leaves.size() + 2);
-  bnd.push_back(0);
-  bnd.push_back(n);
-  for (const Leaf& L : leaves) {
-    bnd.push_back(L.nstrtl - 1);
-    bnd.push_back(L.nstrtl - 1 + L.ndl);
-  }
-  std::sort(bnd.begin(), bnd.end());
-  bnd.erase(std::unique(bnd.begin(), bnd.end()), bnd.end());
-  const int nf = (int)bnd.size() - 1;
-  cp.row_fc.assign(n, 0);
-  for (int f = 0; f < nf; f++)
-    for (int r = bnd[f]; r < bnd[f + 1]; r++) cp.row_fc[r] = f;
-  std::vector<int> cnt(nf + 1, 0);
-  for (const Leaf& L : leaves) {
-    int f0 = cp.row_fc[L.nstrtl - 1];
-    int f1 = cp.row_fc[L.nstrtl - 1 + L.ndl - 1];
-    for (int f = f0; f <= f1; f++) cnt[f + 1]++;
-  }
-  cp.chain_ptr.assign(nf + 1, 0);
-  for (int f = 0; f < nf; f++) cp.chain_ptr[f + 1] = cp.chain_ptr[f] + cnt[f + 1];
-  cp.chain_leaf.assign(cp.chain_ptr[nf], 0);
-  std::vector<int> fill(cp.chain_ptr.begin(), cp.chain_ptr.end() - 1);
-  for (int i = 0; i < (int)leaves.size(); i++) {
-    const Leaf& L = leaves[i];
-    int f0 = cp.row_fc[L.nstrtl - 1];
-    int f1 = cp.row_fc[L.nstrtl - 1 + L.ndl - 1];
-    for (int f = f0; f <= f1; f++) cp.chain_leaf[fill[f]++] = i;
-  }
-}
-
 void plan_stream(int n, const std::vector<Leaf>& leaves, const std::vector<int64_t>& body_off, int vec,
                  StreamPlan& sp, int stage_bytes) {
   const int nl = (int)leaves.size();
@@ -401,7 +280,7 @@ void plan_stream(int n, const std::vector<Leaf>& leaves, const std::vector<int64
         const Leaf& L = leaves[li];
         for (int k = 0; k < L.kt; k++, c++)
           sp.vcopy.push_back(SegCopy{region + (int64_t)c * ntp, body_off[li] + (int64_t)k * L.ndt + (int64_t)t * tr,
-                                     nt, 1});
+                                     nt, 1, vswz(c, ntp / vec), 0});
       }
       S1Item it{};
       it.soff = region;
@@ -465,12 +344,12 @@ void plan_stream(int n, const std::vector<Leaf>& leaves, const std::vector<int64
         if (L.ltmtx == 1) {
           const int64_t u0 = body_off[li] + (int64_t)L.ndt * L.kt;
           for (int k = 0; k < L.kt; k++, c++)
-            sp.ucopy.push_back(SegCopy{region + (int64_t)c * ntp, u0 + (int64_t)k * L.ndl + (int64_t)t * tr, nr, 1});
+            sp.ucopy.push_back(SegCopy{region + (int64_t)c * ntp, u0 + (int64_t)k * L.ndl + (int64_t)t * tr, nr, 1, 0, 0});
         } else {
           // a1(ndt, ndl): element (it, il) at it + il*ndt; column it, rows il
           for (int k = 0; k < L.ndt; k++, c++)
             sp.ucopy.push_back(SegCopy{region + (int64_t)c * ntp, body_off[li] + k + (int64_t)t * tr * L.ndt, nr,
-                                       L.ndt});
+                                       L.ndt, 0, 0});
         }
       }
       S2Item it{};

@@ -34,61 +34,9 @@ void default_params(double* p100);
 // coord: coord(n,3) column-major as the reference passes it.
 int build_structure(int n, const double* coord, const double* param, Structure& s);
 
-// ---- matvec plans -------------------------------------------------------
-// Phase 1 (z = V^T x for every low-rank leaf) items and phase 2 (y = U z + A x,
-// one thread per row walking the leaves that cover the row) chains.
-struct P1Item {            // one warp task
-  int64_t voff;            // element offset of V(t0, k0) in the factor store
-  int32_t ldv;             // row stride of the transposed V (kt)
-  int32_t nt;              // rows in this chunk
-  int32_t x0;              // 0-based column of x for row t0
-  int32_t k0, nk;          // column range of V
-  int32_t leaf;            // low-rank leaf index (dense-order in lr table)
-  int32_t part;            // 0-based chunk number inside the leaf
-};
-
-struct LeafDesc {          // per leaf, device table (phase 2)
-  int64_t off;             // element offset of U (low rank) or A (dense), column-major ld = ndl
-  int32_t row0;            // 0-based first row
-  int32_t ndl;
-  int32_t kind;            // 1 low rank, 2 dense
-  int32_t kt_or_ndt;       // kt (low rank) or ndt (dense)
-  int32_t aux;             // low rank: z offset; dense: 0-based first column
-  int32_t pad;
-};
-
-struct MatPlan {
-  std::vector<int64_t> leaf_off;     // factor-store offset of each leaf's block
-  int64_t store_elems = 0;           // factor store length (elements)
-  std::vector<P1Item> p1;            // phase-1 items
-  std::vector<int32_t> lr_leaf;      // leaf id of each low-rank leaf
-  std::vector<int32_t> lr_zoff;      // z offset of each low-rank leaf
-  std::vector<int32_t> lr_nparts;    // chunks of each low-rank leaf
-  std::vector<int32_t> lr_poff;      // partial-sum offset of each low-rank leaf
-  int64_t zlen = 0, plen = 0;
-  std::vector<LeafDesc> desc;        // per leaf
-  double alg_bytes_per_elem = 0;     // set by caller
-  int64_t factor_elems = 0;          // sum kt(ndl+ndt) + sum ndl*ndt
-};
-
-struct ChainPlan {                   // shared by matrices with the same leaf list
-  std::vector<int32_t> row_fc;       // 0-based row -> fine range id
-  std::vector<int32_t> chain_ptr;    // fine range -> [ptr, ptr+1) in chain_leaf
-  std::vector<int32_t> chain_leaf;   // leaf ids covering the range, coarse-to-fine order
-};
-
-// align: element alignment of each leaf block in the factor store
-// vec: elements per 16-byte vector of the storage type; columns are padded to
-// multiples of vec rows.  item_elems: target size of a phase-1 task.
-void plan_matrix(const std::vector<Leaf>& leaves, int vec, int item_elems, MatPlan& mp);
-void plan_chains(int n, const std::vector<Leaf>& leaves, ChainPlan& cp);
-
 // Row groups: the leaves that share one row range (nstrtl, ndl).  Phase 2
 // gives a warp one 32-row chunk of a group and all of the group's leaves; the
 // per-row sum over the (at most tree-depth) groups that cover a row follows.
-struct P2Item {
-  int32_t group, r0, nr, pad;
-};
 struct GroupPlan {
   std::vector<int32_t> gleaf_ptr, gleaf;  // group -> its leaves, in leaf order
   std::vector<int32_t> grow0, gndl;       // 0-based first row, rows
@@ -98,9 +46,6 @@ struct GroupPlan {
   std::vector<int32_t> fc_ptr, fc_group;  // fine range -> covering groups, coarse to fine
 };
 void plan_groups(int n, const std::vector<Leaf>& leaves, GroupPlan& gp);
-// items of 32-row chunks, ordered by decreasing cost (bytes) for the static
-// warp schedule; cost uses kt, so the order is per matrix
-void plan_p2_items(const std::vector<Leaf>& leaves, const GroupPlan& gp, int vec, std::vector<P2Item>& items);
 
 // ---- streamed product plan ---------------------------------------------
 // The factor store is re-laid out in row tiles of up to 32*vec rows (one
@@ -135,6 +80,7 @@ struct S2Item {
 struct SegCopy {           // conversion of one column segment from the FP64 body
   int64_t dst, src;        // element offsets (dst in the V or U store)
   int32_t len, stride;     // valid rows, source element stride between rows
+  int32_t swz, pad;        // XOR mask of the 16-byte vector index (vswz), 0 = none
 };
 struct StreamPlan {
   int vec = 1, tr = 1;
@@ -153,9 +99,28 @@ struct StreamPlan {
   std::vector<SegCopy> vcopy, ucopy; // conversion maps
   int64_t factor_elems = 0;
 };
+// XOR mask of the 16-byte vectors of column c in a V-store segment of nv
+// vectors: within each aligned group of g = gcd(nv, 8) vectors, vector k of
+// column c is stored at k ^ vswz(c, nv).  Eight consecutive columns read at
+// the same logical vector then fall on eight different 16-byte bank slots of
+// shared memory (c * nv + (k ^ s) is distinct mod 8 over c), so a warp whose
+// lanes own consecutive columns reads a stage without bank conflicts.  The
+// mask only depends on c mod 8, and chunks start at multiples of 16 columns.
+#if defined(__CUDACC__)
+__host__ __device__
+#endif
+inline int vswz(int c, int nv) {
+  const int g = (nv & -nv) < 8 ? (nv & -nv) : 8;
+  const int shift = g == 8 ? 0 : g == 4 ? 1 : g == 2 ? 2 : 3;
+  return (c >> shift) & (g - 1);
+}
+
 // columns of one streamed chunk in a shared-memory stage of stage_bytes (8 KB
 // or 16 KB): as many whole columns as fit, a multiple of 16 (ntp * esz <= 512,
 // so at least 16), and at most 128 (four phase-2 multipliers per lane)
+#if defined(__CUDACC__)
+__host__ __device__
+#endif
 inline int chunk_cols(int ntp, int esz, int stage_bytes) {
   const int c = (stage_bytes / (ntp * esz)) / 16 * 16;
   return c < 128 ? c : 128;

@@ -67,10 +67,13 @@ def pack(params, mean, sd, lo=LO, hi=HI):
     return w
 
 
-def train(X, T, epochs=40, batch=1024, lr=2e-3, seed=0, min_steps=3000):
+def train(X, T, epochs=40, batch=1024, lr=2e-3, seed=0, min_steps=3000, tau=None, lo=LO, hi=HI):
     """Fit the proposer on the GPU; returns (weight vector, loss per epoch).
     Small traces get smaller batches and more epochs, so that every fit takes
-    at least `min_steps` Adam steps."""
+    at least `min_steps` Adam steps.  tau: None fits the mean of the label
+    (squared error); 0 < tau < 1 fits its tau-quantile (pinball loss), a
+    proposal that the ideal step exceeds with probability 1 - tau.  lo, hi:
+    the clamp of the proposal d."""
     nin, hid, _ = proposer_size()
     batch = int(min(batch, max(64, len(T) // 8)))
     epochs = int(max(epochs, -(-min_steps * batch // max(1, len(T)))))
@@ -80,7 +83,8 @@ def train(X, T, epochs=40, batch=1024, lr=2e-3, seed=0, min_steps=3000):
     Xs = ((X - mean) / sd).astype(np.float32)
     m = MLP(nin, hid, batch_max=max(batch, 64))
     m.init(seed)
+    m.set_loss(tau)
     hist = m.train(Xs, T, epochs=epochs, batch=min(batch, len(T)), lr=lr, seed=seed)
-    w = pack(m.params(), mean, sd)
+    w = pack(m.params(), mean, sd, lo, hi)
     m.close()
     return w, hist

@@ -105,6 +105,21 @@ int hbi_free_leafmtxp(hbi_leafmtxp* lf);
 int hbi_construct_lh(hbi_lhp** st_LHp, const hbi_leafmtxp* lf, hbi_ctl* st_ctl, int storage);
 int hbi_free_lh(hbi_lhp* lh);
 
+/* Sharding of the product over ranks.  The reference distributes lattice
+ * blocks over a 2-D MPI process grid and combines each rank's partial row
+ * sums by a row reduce and a column broadcast (m_HACApK_solve.f90:278-314).
+ * Here the leaves are dealt to nranks ranks by factor elements, largest
+ * first to the least-loaded rank (host only, no GPU): owner[leaf] receives
+ * the rank, elems_per_rank[nranks] the load of each (may be NULL).  A rank's
+ * operator (hbi_construct_lh_part) holds only its leaves, so its product is
+ * a partial au; the sum of the ranks' partials -- one all-reduce of ndc
+ * doubles per product -- is au. */
+int hbi_partition_leaves(int nleaf, const int* leaves6, int nranks, int32_t* owner, int64_t* elems_per_rank);
+/* hbi_construct_lh over the leaves with owner[leaf] == rank (owner as from
+ * hbi_partition_leaves on hbi_get_leaves' table) */
+int hbi_construct_lh_part(hbi_lhp** st_LHp, const hbi_leafmtxp* lf, hbi_ctl* st_ctl, int storage,
+                          const int32_t* owner, int rank);
+
 /* HACApK_gen_lattice_vector (m_HACApK_base.f90:3449-3500): ndc = NCELL and
  * lodc(1:ndc) (1-based global ids of the cluster-ordered vector); lodc may be
  * NULL to query ndc only. */
@@ -162,6 +177,35 @@ int hbi_adot_lattice_hyp_noalloc(double* d_au, hbi_lhp* st_LHp, const double* d_
  * the dense leaves (from the z of the last phase 1), phase 3 sums them into
  * au; phase 0 runs all three.  For kernel timing. */
 int hbi_adot_lattice_hyp_phase_dev(double* d_au, hbi_lhp* st_LHp, const double* d_u, void* stream, int phase);
+/* Launch-shape autotuner of the product kernels (no reference counterpart;
+ * it replaces the byte-balanced cut of the leaf list over OpenMP threads,
+ * m_HACApK_use.f90:387-431 and m_HACApK_base.f90:1537-1564).  The phase
+ * kernels are compiled in several launch shapes (warps per block, stages per
+ * warp, stage bytes; the stage size sets the streamed chunk width), each with
+ * its own static warp schedule.  hbi_construct_lh times every shape on the
+ * new operator (five launches per phase after one warm-up, CUDA events) and
+ * keeps the fastest per phase; operators whose plans have the same size
+ * statistics reuse the choice; the environment variables HBI_STREAM_SHAPE1=s
+ * and HBI_STREAM_SHAPE2=s force shape s of phase 1 / phase 2. */
+/* the compiled shapes of phase 1 or 2: *count, and shapes4[4*s .. 4*s+3] =
+ * warps per block, stages per warp, stage bytes, lane mapping (phase 1: 0 =
+ * the lanes of a column split its rows, 1 = one lane per column; phase 2: 0)
+ * (shapes4 may be NULL) */
+int hbi_stream_shapes(int phase, int* count, int* shapes4);
+/* the shapes chosen for phases 1 and 2, the median time in microseconds of
+ * every shape (phase 1's shapes, then phase 2's; -1 if not timed) and how
+ * they were chosen (0 timed, 1 reused, 2 forced or pinned) */
+int hbi_lh_tuning(const hbi_lhp* st_LHp, int* shape1, int* shape2, float* median_us, int* source);
+/* pin the launch shapes of phases 1 and 2 (0 <= shape < count) for products
+ * launched afterwards; RK handles copy an operator's shapes when created */
+int hbi_lh_set_shapes(hbi_lhp* st_LHp, int shape1, int shape2);
+/* Host-only selection rule of the autotuner: times[c * reps + r] are the
+ * times of candidate c (non-positive or non-finite entries are ignored);
+ * medians[c] receives each candidate's median (-1 when it has no valid
+ * time; medians may be NULL); *best is the candidate with the lowest median,
+ * a later candidate replacing an earlier one only when it is more than 1%
+ * faster.  HBI_ERR_ARG when no candidate has a valid time. */
+int hbi_autotune_select(int ncand, int reps, const float* times, float* medians, int* best);
 /* algorithmic bytes of phases 1 (V factors + u) and 2 (U factors, dense
  * blocks + u); the product adds ndc x 8 bytes for au (phase 3) */
 int hbi_lh_phase_bytes(const hbi_lhp* lh, double* phase1, double* phase2);
@@ -319,7 +363,11 @@ int hbi_mlp_create(hbi_mlp** m, int nin, int hid, int batch_max);
 int hbi_mlp_free(hbi_mlp* m);
 int hbi_mlp_set_params(hbi_mlp* m, const float* p);
 int hbi_mlp_get_params(hbi_mlp* m, float* p);
-/* loss = mean((out - t)^2) over x[batch][nin]; grad = d loss / d params */
+/* the training loss: tau <= 0 the squared error (the default), 0 < tau < 1
+ * the pinball loss of quantile tau -- (1 - tau) r for r = out - t > 0, -tau r
+ * otherwise -- whose minimiser is the tau-quantile of t given the inputs */
+int hbi_mlp_set_loss(hbi_mlp* m, float tau);
+/* loss = mean of the per-sample loss over x[batch][nin]; grad = d loss / d params */
 int hbi_mlp_loss_grad(hbi_mlp* m, const float* x, const float* t, int batch, float* grad, float* loss,
                       float* out);
 /* `epochs` passes of Adam over n samples in shuffled minibatches (seeded) */

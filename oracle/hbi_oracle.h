@@ -102,6 +102,10 @@ void orc_matvec(int n, int nleaf, const orc_leaf* leaves, const int64_t* offsets
  * (setcutthread_lattice), per-thread zaut, atomic accumulation. */
 void orc_matvec_omp(int n, int nleaf, const orc_leaf* leaves, const int64_t* offsets,
                     const double* body, const double* u, double* au, int nthreads);
+/* rows[] (0-based cluster positions) of the exact operator times u: out[r] =
+ * sum_j entry(lod[rows[r]], lod[j]) u[j]; OpenMP over rows */
+void orc_rows_matvec(const orc_bemv* b, int n, const int* lod, int nr, const int* rows, const double* u,
+                     double* out, int nthreads);
 
 /* ---- meshes (main_LH.f90) ---- */
 void orc_mesh_2dp(int n, double ds0, double* xel, double* xer, double* xcol, double* ds);
@@ -161,6 +165,8 @@ void orc_rkqs_consts(double* c4);
  * loss = mean((out - target)^2); grad same packing. */
 double orc_mlp_loss_grad(int nin, int h, int batch, const float* params, const float* x,
                          const float* target, float* grad, float* out);
+double orc_mlp_loss_grad_tau(int nin, int h, int batch, const float* params, const float* x,
+                             const float* target, float* grad, float* out, double tau);
 
 #ifdef __cplusplus
 }

@@ -66,6 +66,7 @@ def lib():
         L.orc_znrm.restype = C.c_double
         L.orc_errmax.restype = C.c_double
         L.orc_mlp_loss_grad.restype = C.c_double
+        L.orc_mlp_loss_grad_tau.restype = C.c_double
         L.orc_fill.restype = _dp
         _lib = L
     return _lib
@@ -210,6 +211,18 @@ def dense_matrix(g, lod):
     return A
 
 
+def rows_matvec(g, lod, rows, u, nthreads=0):
+    """Selected rows of the exact operator times u (cluster order):
+    out[r] = sum_j entry(lod[rows[r]], lod[j]) u[j], OpenMP over the rows."""
+    lod = np.ascontiguousarray(lod, dtype=np.int32)
+    rows = np.ascontiguousarray(rows, dtype=np.int32)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    out = np.zeros(len(rows))
+    lib().orc_rows_matvec(C.byref(g.bemv), g.n, lod.ctypes.data_as(_ip), len(rows), rows.ctypes.data_as(_ip), _p(u),
+                          _p(out), int(nthreads))
+    return out
+
+
 def okada(alpha, x, y, z, depth, dip, al1, al2, aw1, aw2, d1, d2, d3, fullspace=False):
     u = np.zeros(12)
     lib().orc_okada(C.c_double(alpha), C.c_double(x), C.c_double(y), C.c_double(z), C.c_double(depth),
@@ -347,13 +360,14 @@ def cycle(rsf, y, vel, ds, nsteps, eps_r=1e-4, dtinit=1.0, dtmax=1e10, tmax_yr=1
     return stop, rec[:nrec.value], ev[:min(nev.value, max_events)], y, vel, slip
 
 
-def mlp_loss_grad(nin, h, params, x, target):
+def mlp_loss_grad(nin, h, params, x, target, tau=-1.0):
     params = np.ascontiguousarray(params, dtype=np.float32)
     x = np.ascontiguousarray(x, dtype=np.float32)
     target = np.ascontiguousarray(target, dtype=np.float32)
     g = np.zeros_like(params)
     out = np.zeros(len(target), dtype=np.float32)
     fp = C.POINTER(C.c_float)
-    loss = lib().orc_mlp_loss_grad(nin, h, len(target), params.ctypes.data_as(fp), x.ctypes.data_as(fp),
-                                   target.ctypes.data_as(fp), g.ctypes.data_as(fp), out.ctypes.data_as(fp))
+    loss = lib().orc_mlp_loss_grad_tau(nin, h, len(target), params.ctypes.data_as(fp), x.ctypes.data_as(fp),
+                                       target.ctypes.data_as(fp), g.ctypes.data_as(fp), out.ctypes.data_as(fp),
+                                       C.c_double(tau))
     return loss, g, out

@@ -410,3 +410,25 @@ void orc_matvec_omp(int n, int nleaf, const orc_leaf* leaves, const int64_t* off
   orc_matvec(n, nleaf, leaves, offsets, body, u, au);
 #endif
 }
+
+/* Rows of the exact operator times u, for parity checks at sizes where the
+ * dense matrix does not fit: out[r] = sum_j entry(lod[rows[r]], lod[j]) u[j]
+ * with rows[] 0-based cluster-order positions and u in cluster order (the
+ * lattice vector of the reference).  Each row is summed serially in j order;
+ * rows are spread over the threads. */
+void orc_rows_matvec(const orc_bemv* b, int n, const int* lod, int nr, const int* rows, const double* u,
+                     double* out, int nthreads) {
+#ifdef _OPENMP
+  if (nthreads < 1) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+#endif
+  for (int r = 0; r < nr; r++) {
+    const int gi = lod[rows[r]];
+    double t = 0.0;
+    for (int j = 0; j < n; j++) t += orc_entry_ij(gi, lod[j], b) * u[j];
+    out[r] = t;
+  }
+#ifndef _OPENMP
+  (void)nthreads;
+#endif
+}

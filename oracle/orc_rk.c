@@ -255,6 +255,13 @@ void orc_evcalc(int n, const double* xs1, const double* xs2, const double* xs3, 
  *      GPU training kernels).  Double accumulation, float in/out. ---- */
 double orc_mlp_loss_grad(int nin, int h, int batch, const float* P, const float* X,
                          const float* T, float* G, float* out) {
+  return orc_mlp_loss_grad_tau(nin, h, batch, P, X, T, G, out, -1.0);
+}
+
+/* as orc_mlp_loss_grad with the pinball loss of quantile tau when 0 < tau < 1:
+ * (1 - tau) r for r = y - t > 0, -tau r otherwise (derivative 0 at r = 0) */
+double orc_mlp_loss_grad_tau(int nin, int h, int batch, const float* P, const float* X,
+                             const float* T, float* G, float* out, double tau) {
   const float* W1 = P;
   const float* b1 = W1 + h * nin;
   const float* W2 = b1 + h;
@@ -284,8 +291,14 @@ double orc_mlp_loss_grad(int nin, int h, int batch, const float* P, const float*
     for (int i = 0; i < h; i++) y += (double)W3[i] * a2[i];
     if (out) out[s] = (float)y;
     double r = y - T[s];
-    loss += r * r;
-    double dy = 2.0 * r / batch;
+    double dy;
+    if (tau > 0.0) {
+      loss += r > 0.0 ? (1.0 - tau) * r : -tau * r;
+      dy = (r > 0.0 ? 1.0 - tau : (r < 0.0 ? -tau : 0.0)) / batch;
+    } else {
+      loss += r * r;
+      dy = 2.0 * r / batch;
+    }
     double* gW1 = g;
     double* gb1 = gW1 + h * nin;
     double* gW2 = gb1 + h;

@@ -1,0 +1,84 @@
+"""The product kernels' launch-shape autotuner, host side (no GPU).
+
+hbi_construct_lh times every compiled launch shape of the phase kernels on
+the operator (five launches per phase after a warm-up) and keeps, per phase,
+the shape with the lowest median time; a later shape must beat the earlier
+best by more than 1% (near-ties keep the default, shape 0).  These tests run
+that selection rule on recorded timings and check the shape table against
+the kernels' shared-memory and chunk-width limits.
+"""
+import numpy as np
+import pytest
+
+import hbi_gb300 as H
+
+# median phase times (us) of the four shapes on the c2 shear operator (FP32
+# store, 65,536 elements), five launches each, as construct_LH timed them on
+# a GB300: the 12-warp default wins phase 1, the 8-warp 3-stage shape phase 2
+RECORDED = {
+    "phase1": [[73.1, 73.6, 73.4, 73.3, 74.0], [79.2, 78.8, 79.9, 79.1, 79.3],
+               [88.5, 88.1, 88.9, 88.2, 88.0], [75.9, 76.2, 75.8, 76.4, 76.0]],
+    "phase2": [[69.4, 69.1, 69.8, 69.0, 69.3], [67.2, 67.5, 66.9, 67.3, 67.0],
+               [80.3, 80.1, 80.9, 80.0, 80.2], [71.0, 70.8, 71.3, 70.9, 71.1]],
+}
+
+
+def test_selection_on_recorded_timings():
+    b1, m1 = H.autotune_select(RECORDED["phase1"])
+    b2, m2 = H.autotune_select(RECORDED["phase2"])
+    assert b1 == 0 and b2 == 1
+    assert m1[0] == pytest.approx(73.4) and m2[1] == pytest.approx(67.2)
+
+
+def test_median_ignores_one_outlier_and_invalid_runs():
+    t = [[50.0, 50.2, 49.9, 50.1, 50.0], [45.0, 45.1, 900.0, 44.9, 45.2]]
+    assert H.autotune_select(t)[0] == 1
+    t = [[50.0, -1.0, float("nan"), 50.1, 50.0], [float("inf"), 0.0, -1.0, float("nan"), -2.0]]
+    best, med = H.autotune_select(t)
+    assert best == 0 and med[1] == -1.0
+    with pytest.raises(H.HBIError):
+        H.autotune_select([[-1.0, 0.0], [float("nan"), -5.0]])
+
+
+def test_near_ties_keep_the_earlier_shape():
+    assert H.autotune_select([[100.0] * 5, [99.5] * 5, [99.2] * 5])[0] == 0
+    assert H.autotune_select([[100.0] * 5, [98.0] * 5, [97.5] * 5])[0] == 1
+    assert H.autotune_select([[100.0] * 5, [98.0] * 5, [96.9] * 5])[0] == 2
+
+
+def test_shape_table_fits_the_kernels():
+    for phase in (1, 2):
+        shapes = H.stream_shapes(phase)
+        assert len(shapes) >= 3 and shapes[0] == (12, 2, 8192, 0)
+        for nw, ns, sb, lane_map in shapes:
+            assert 1 <= nw <= 32 and ns >= 2 and sb in (8192, 16384)
+            assert lane_map in (0, 1)
+            smem = nw * ns * sb + nw * 128 * 8 + nw * ns * 8
+            assert smem <= 227 * 1024
+            for esz in (2, 4, 8):
+                for ntp in range(16 // esz, 512 // esz + 1, 16 // esz):
+                    cc = (sb // (ntp * esz)) // 16 * 16
+                    cc = min(cc, 128)
+                    assert 16 <= cc <= 128 and cc * ntp * esz <= sb
+    assert {m for *_, m in H.stream_shapes(1)} == {0, 1}
+
+
+def _vswz(c, nv):
+    g = min(nv & -nv, 8)
+    shift = {8: 0, 4: 1, 2: 2, 1: 3}[g]
+    return (c >> shift) & (g - 1)
+
+
+@pytest.mark.parametrize("nv", list(range(1, 33)))
+def test_v_store_swizzle_is_conflict_free_and_in_bounds(nv):
+    """The V-store swizzle (vswz in hbi_structure.hpp): within a column segment
+    of nv 16-byte vectors it permutes the vectors, and eight consecutive
+    columns reading the same logical vector hit eight different 16-byte bank
+    slots of shared memory (vector address mod 8)."""
+    for c in range(64):
+        s = _vswz(c, nv)
+        assert sorted(k ^ s for k in range(nv)) == list(range(nv))
+    for c0 in range(0, 64, 8):
+        for k in range(nv):
+            slots = {((c0 + c) * nv + (k ^ _vswz(c0 + c, nv))) % 8 for c in range(8)}
+            assert len(slots) == 8, (nv, c0, k)

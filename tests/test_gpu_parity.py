@@ -293,3 +293,50 @@ def test_matvec_large_operator(oracle, store, tol):
     y = lh.matvec(u)
     assert np.linalg.norm(y - ref) <= tol * np.linalg.norm(ref)
     assert np.array_equal(y, lh.matvec(u))
+
+
+@pytest.mark.parametrize("store,tol", [("f64", 1e-12), ("f32", 1e-5), ("bf16", 2e-2)])
+def test_every_launch_shape_gives_the_product(oracle, store, tol):
+    """The autotuner's candidates: every compiled launch shape of the phase
+    kernels (its own warp schedule and chunk width) gives the product of the
+    same factors; the tuner's choice is timed once and reused for an operator
+    with the same plan."""
+    prob, n, g, w, eps = case("3dph", (64, 64))
+    ctl = H.Ctl(n)
+    lf = H.LeafMtxp(ctl, product_geometry(prob, n, g, w, "s"), eps)
+    off, body = lf.body()
+    ref_op = oracle.HMatrix.from_body(n, lf.leaves(), off, body)
+    lh = H.LHp(lf, ctl, store)
+    tun = lh.tuning()
+    assert tun["source"] in ("timed", "reused")
+    assert all(v > 0 for v in tun["phase1_us"].values()) or tun["source"] == "reused"
+    u = np.random.default_rng(12).standard_normal(n)
+    ref = ref_op.matvec(u)
+    for s1 in range(len(H.stream_shapes(1))):
+        for s2 in range(len(H.stream_shapes(2))):
+            lh.set_shapes(s1, s2)
+            y = lh.matvec(u)
+            assert np.linalg.norm(y - ref) <= tol * np.linalg.norm(ref), (s1, s2)
+    lh2 = H.LHp(lf, ctl, store)
+    assert lh2.tuning()["source"] == "reused"
+    assert (lh2.tuning()["shape1"], lh2.tuning()["shape2"]) == (tun["shape1"], tun["shape2"])
+
+
+@pytest.mark.parametrize("nranks", [2, 3])
+def test_partial_operators_sum_to_the_product(built, nranks):
+    """hbi_construct_lh_part: the operators of the ranks' leaves (dealt by
+    hbi_partition_leaves) give partial products that sum to the product, as
+    the all-reduce of a sharded run would combine them."""
+    B = built("3dph")
+    lv = B["lf"].leaves()
+    owner, load = H.partition_leaves(lv, nranks)
+    full = H.LHp(B["lf"], B["ctl"], "f64")
+    u = np.random.default_rng(17).standard_normal(B["n"])
+    ref = full.matvec(u)
+    acc = np.zeros(B["n"])
+    for r in range(nranks):
+        part = H.LHp(B["lf"], B["ctl"], "f64", owner=owner, rank=r)
+        assert part.info()["factor_elems"] == load[r]
+        acc += part.matvec(u)
+        part.close()
+    assert np.linalg.norm(acc - ref) <= 1e-13 * np.linalg.norm(ref)

@@ -1,0 +1,140 @@
+"""GPU parity at the benchmarked sizes, through the C ABI.
+
+* c2 (3D planar thrust, Okada half space, 256 x 256 = 65,536 elements, ACA
+  eps 1e-5) -- the operator bench.py measures: the GPU products with FP64,
+  FP32 and BF16 factor stores against the oracle's product of the same FP64
+  factors (HACApK_adot_body_lfmtx_hyp_contiguous, m_HACApK_solve.f90:
+  2108-2164, restated with the reference's thread ranges and atomics), with
+  ones and a seeded random vector; tolerances 1e-12 / 1e-5 / 2e-2 relative.
+* c3 (rough strike-slip fault, 200,000 triangles, TDstressFS full space,
+  ACA eps 1e-4): the FP64 and FP32 products against the oracle's product of
+  the same factors, and 2,000 seeded random rows of the FP32 product against
+  the same rows of the exact operator, evaluated entry by entry by the
+  oracle's TDstressFS (HACApK_entry_ij, m_HACApK_calc_entry_ij.f90:802-851):
+  the whole chain -- tree, ACA+ on the GPU, FP32 store, product -- within
+  50 x eps_h of the exact operator, the bound the small cases use.
+* c1 (2D antiplane, 1,024 elements, eps_r 1e-6): the device time loop
+  against the oracle's loop (main_LH.f90:1217-1438) over the first 500
+  simulated years -- every event of the catalogue: same count, onset within
+  1e-5 relative, hypocentre within two elements, event slip within 1e-3
+  relative, the slip field at 500 years within 1e-3.  (The products differ
+  only in summation order, ~1e-15; each nucleation amplifies that round-off,
+  and the differences carry over from one cycle to the next.)
+"""
+import os
+
+import numpy as np
+import pytest
+
+import hbi_gb300 as H
+from gpu_cases import ORC_PROBLEM
+from hbi_gb300 import configs
+
+pytestmark = pytest.mark.gpu
+
+NTH = os.cpu_count() or 1
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def _oracle_geometry(oracle, w, v):
+    return oracle.Geometry(ORC_PROBLEM[w.problem], w.nd, v, w=w.w, **w.geom_kw)
+
+
+@pytest.fixture(scope="module")
+def c2(oracle):
+    w = configs.c2_3dph(256, 256)
+    ctl = H.Ctl(w.nd)
+    lf = H.LeafMtxp(ctl, w.geometry("s"), w.eps_h)
+    off, body = lf.body()
+    Ho = oracle.HMatrix.from_body(w.nd, lf.leaves(), off, body)
+    del body
+    return dict(w=w, ctl=ctl, lf=lf, Ho=Ho)
+
+
+@pytest.mark.parametrize("store,tol", [("f64", 1e-12), ("f32", 1e-5), ("bf16", 2e-2)])
+def test_c2_product_against_oracle_on_the_same_factors(c2, store, tol):
+    w = c2["w"]
+    lh = H.LHp(c2["lf"], c2["ctl"], store)
+    for u in (np.ones(w.nd), np.random.default_rng(21).standard_normal(w.nd)):
+        y = lh.matvec(u)
+        ref = c2["Ho"].matvec(u, nthreads=NTH)
+        assert _rel(y, ref) <= tol, (store, _rel(y, ref))
+    lh.close()
+
+
+def test_c2_rows_against_the_exact_operator(oracle, c2):
+    """512 random rows of the FP32 product against the exact Okada operator."""
+    w = c2["w"]
+    lh = H.LHp(c2["lf"], c2["ctl"], "f32")
+    u = np.random.default_rng(22).standard_normal(w.nd)
+    y = lh.matvec(u)
+    rows = np.sort(np.random.default_rng(23).choice(w.nd, 512, replace=False))
+    exact = oracle.rows_matvec(_oracle_geometry(oracle, w, "s"), c2["ctl"].lod(), rows, u, NTH)
+    assert _rel(y[rows], exact) <= 50 * w.eps_h, _rel(y[rows], exact)
+
+
+@pytest.fixture(scope="module")
+def c3(oracle):
+    w = configs.c3_3dnt()
+    ctl = H.Ctl(w.nd)
+    lf = H.LeafMtxp(ctl, w.geometry("s"), w.eps_h)
+    off, body = lf.body()
+    Ho = oracle.HMatrix.from_body(w.nd, lf.leaves(), off, body)
+    del body
+    return dict(w=w, ctl=ctl, lf=lf, Ho=Ho)
+
+
+@pytest.mark.parametrize("store,tol", [("f64", 1e-12), ("f32", 1e-5)])
+def test_c3_product_against_oracle_on_the_same_factors(c3, store, tol):
+    w = c3["w"]
+    lh = H.LHp(c3["lf"], c3["ctl"], store)
+    for u in (np.ones(w.nd), np.random.default_rng(31).standard_normal(w.nd)):
+        y = lh.matvec(u)
+        ref = c3["Ho"].matvec(u, nthreads=NTH)
+        assert _rel(y, ref) <= tol, (store, _rel(y, ref))
+    lh.close()
+
+
+def test_c3_rows_against_the_exact_operator(oracle, c3):
+    """2,000 random rows of the FP32 product against exact TDstressFS rows."""
+    w = c3["w"]
+    lh = H.LHp(c3["lf"], c3["ctl"], "f32")
+    u = np.random.default_rng(32).standard_normal(w.nd)
+    y = lh.matvec(u)
+    rows = np.sort(np.random.default_rng(33).choice(w.nd, 2000, replace=False))
+    exact = oracle.rows_matvec(_oracle_geometry(oracle, w, "s"), c3["ctl"].lod(), rows, u, NTH)
+    assert _rel(y[rows], exact) <= 50 * w.eps_h, _rel(y[rows], exact)
+    lh.close()
+
+
+def test_c1_loop_catalogue_follows_the_oracle_for_500_years(oracle):
+    n, years = 1024, 500.0
+    w = configs.c1_2dvs(n)
+    ctl = H.Ctl(n)
+    lf = H.LeafMtxp(ctl, w.geometry("s"), w.eps_h)
+    lh = H.LHp(lf, ctl, "f64")
+    ndc, lodc = H.HACApK_gen_lattice_vector(ctl)
+    y0, p = w.initial_state(lodc)
+    ds = w.ds_area[lodc - 1]
+    off, body = lf.body()
+    Ho = oracle.HMatrix.from_body(n, lf.leaves(), off, body)
+    R = oracle.RSF(n, Ho, evlaw=0, a=p["a"], b=p["b"], dc=p["dc"], f0=p["f0"], vplv=p["vpl"], nthreads=NTH)
+    stop_o, rec, ev_o, _, _, slip_o = oracle.cycle(R, y0, p["vel"], ds, 400000, eps_r=1e-6, tmax_yr=years)
+    rk = H.RK(lh, None, evlaw=0, a=p["a"], b=p["b"], dc=p["dc"], f0=p["f0"], vpl=p["vpl"])
+    rk.set_state(y0)
+    c = H.Cycle(rk, p["vel"], ds, eps_r=1e-6, tmax_yr=years)
+    st = c.run()
+    assert st["stop_name"] == "tmax"
+    ev = c.events()
+    assert len(ev_o) >= 4, "the window must hold several earthquakes"
+    assert len(ev) == len(ev_o)
+    for e_g, e_o in zip(ev, ev_o):
+        assert e_g["id"] == int(e_o[0])
+        assert abs(e_g["onset"] - e_o[2]) <= 1e-5 * e_o[2], (e_g["id"], e_g["onset"], e_o[2])
+        assert abs(e_g["hypoloc"] - int(e_o[4])) <= 2, (e_g["id"], e_g["hypoloc"], e_o[4])
+        assert abs(e_g["moment"] - e_o[3]) <= 1e-3 * abs(e_o[3]), e_g["id"]
+    _, slip = c.fields()
+    assert _rel(slip, slip_o) <= 1e-3

@@ -17,17 +17,21 @@ from hbi_gb300 import configs, proposer
 pytestmark = pytest.mark.gpu
 
 
-def test_mlp_gradients_match_oracle(oracle):
+@pytest.mark.parametrize("tau", [None, 0.2])
+def test_mlp_gradients_match_oracle(oracle, tau):
+    """Squared error, and the pinball loss of quantile 0.2 (targets shifted so
+    that no residual sits near the loss's kink)."""
     nin, hid, B = 6, 64, 512
     rng = np.random.default_rng(3)
     m = H.MLP(nin, hid, batch_max=B)
     p = m.init(seed=4)
     p[: hid * nin + hid] += 0.05 * rng.standard_normal(hid * nin + hid).astype(np.float32)  # nonzero biases
     m.set_params(p)
+    m.set_loss(tau)
     x = rng.standard_normal((B, nin)).astype(np.float32)
-    t = rng.standard_normal(B).astype(np.float32)
+    t = rng.standard_normal(B).astype(np.float32) + (0.0 if tau is None else 3.0)
     loss, g, out = m.loss_grad(x, t)
-    loss_o, g_o, out_o = oracle.mlp_loss_grad(nin, hid, p, x, t)
+    loss_o, g_o, out_o = oracle.mlp_loss_grad(nin, hid, p, x, t, -1.0 if tau is None else tau)
     assert abs(loss - loss_o) <= 2e-4 * abs(loss_o)
     assert np.allclose(out, out_o, rtol=2e-4, atol=2e-5)
     o = 0
@@ -90,3 +94,33 @@ def test_learned_proposer_gains_over_rkqs():
     for a, b in zip(ev_l, ev_c):
         assert abs(a["onset"] - b["onset"]) <= 1e-3 * b["onset"]
         assert abs(a["moment"] - b["moment"]) <= 1e-3 * abs(b["moment"])
+
+
+def test_mixed_form_passes_the_catalogue_gate():
+    """The accuracy gate of the mixed form at small size: c1 (1,024
+    elements) over 600 years, the plain form (FP64 factors, rkqs) against
+    FP32 factors with the proposer trained on the plain run's trace; the
+    catalogues and slip fields compared by hbi_gb300.catalogue (earthquakes
+    paired one to one within 1e-3 in onset and slip, every event matched,
+    slip field within 1e-3)."""
+    from hbi_gb300.catalogue import catalogue_gate
+    S = _system()
+    p = S["p"]
+
+    def run(lh, w=None):
+        rk = H.RK(lh, None, evlaw=0, a=p["a"], b=p["b"], dc=p["dc"], f0=p["f0"], vpl=p["vpl"])
+        rk.set_state(S["y0"])
+        c = H.Cycle(rk, p["vel"], S["ds"], eps_r=1e-6, tmax_yr=1500.0)
+        if w is not None:
+            c.set_proposer(w)
+        st = c.run(t_limit=600.0 * H.YEAR)
+        return dict(st=st, trace=c.trace(), events=c.events(), slip=c.fields()[1])
+
+    plain = run(S["lh"])
+    X, T = proposer.training_set(plain["trace"])
+    w, _ = proposer.train(X, T, epochs=30)
+    ctl, lf = S["keep"]
+    mixed = run(H.LHp(lf, ctl, "f32"), w)
+    g = catalogue_gate(plain, mixed)
+    assert g["earthquakes"][0] >= 5, g
+    assert g["pass"], g["failures"]

@@ -215,6 +215,31 @@ def test_mlp_oracle_gradient_matches_finite_differences(oracle):
     assert np.allclose(g, fd, rtol=2e-2, atol=2e-4)
 
 
+def test_mlp_oracle_pinball_gradient_matches_finite_differences(oracle):
+    """The same for the pinball (quantile) loss: away from the kinks (no
+    sample's residual within the finite-difference step of zero) its
+    gradient is the central difference of the loss."""
+    nin, h, B, tau = 3, 4, 16, 0.2
+    rng = np.random.default_rng(4)
+    npar = h * nin + h + h * h + h + h + 1
+    p = (0.5 * rng.standard_normal(npar)).astype(np.float32)
+    x = rng.standard_normal((B, nin)).astype(np.float32)
+    t = rng.standard_normal(B).astype(np.float32) + 3.0
+    loss, g, out = oracle.mlp_loss_grad(nin, h, p, x, t, tau)
+    r = out - t
+    assert np.all(np.abs(r) > 0.5)
+    assert loss == pytest.approx(np.mean(np.where(r > 0, (1 - tau) * r, -tau * r)), rel=1e-6)
+    step = 1e-2
+    fd = np.zeros(npar)
+    for k in range(npar):
+        pp, pm = p.copy(), p.copy()
+        pp[k] += step
+        pm[k] -= step
+        fd[k] = (oracle.mlp_loss_grad(nin, h, pp, x, t, tau)[0] - oracle.mlp_loss_grad(nin, h, pm, x, t, tau)[0]) / (
+            float(pp[k]) - float(pm[k]))
+    assert np.allclose(g, fd, rtol=2e-2, atol=2e-4)
+
+
 def test_proposer_labels_recover_the_ideal_step():
     """training_set's label is the step that would have met the target error
     under Cash-Karp's h**5 error law."""

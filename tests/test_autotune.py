@@ -12,22 +12,22 @@ import pytest
 
 import hbi_gb300 as H
 
-# median phase times (us) of the four shapes on the c2 shear operator (FP32
-# store, 65,536 elements), five launches each, as construct_LH timed them on
-# a GB300: the 12-warp default wins phase 1, the 8-warp 3-stage shape phase 2
+# the median phase times (us) that construct_LH recorded for every shape on
+# a GB300 (c2 shear operator, 65,536 elements, FP32 store; five launches per
+# shape): phase 1 in the order of stream_shapes(1) -- 12, 8 and 6 warps with
+# the row mapping, then the same with one lane per column -- and phase 2 in
+# the order of stream_shapes(2)
 RECORDED = {
-    "phase1": [[73.1, 73.6, 73.4, 73.3, 74.0], [79.2, 78.8, 79.9, 79.1, 79.3],
-               [88.5, 88.1, 88.9, 88.2, 88.0], [75.9, 76.2, 75.8, 76.4, 76.0]],
-    "phase2": [[69.4, 69.1, 69.8, 69.0, 69.3], [67.2, 67.5, 66.9, 67.3, 67.0],
-               [80.3, 80.1, 80.9, 80.0, 80.2], [71.0, 70.8, 71.3, 70.9, 71.1]],
+    "phase1": [88.0, 102.3, 114.62, 71.62, 79.78, 83.94],
+    "phase2": [67.46, 77.7, 81.79, 69.54, 77.7],
 }
 
 
 def test_selection_on_recorded_timings():
-    b1, m1 = H.autotune_select(RECORDED["phase1"])
-    b2, m2 = H.autotune_select(RECORDED["phase2"])
-    assert b1 == 0 and b2 == 1
-    assert m1[0] == pytest.approx(73.4) and m2[1] == pytest.approx(67.2)
+    b1, m1 = H.autotune_select([[t] for t in RECORDED["phase1"]])
+    b2, m2 = H.autotune_select([[t] for t in RECORDED["phase2"]])
+    assert b1 == 3 and b2 == 0
+    assert m1[3] == pytest.approx(71.62) and m2[0] == pytest.approx(67.46)
 
 
 def test_median_ignores_one_outlier_and_invalid_runs():

@@ -49,13 +49,13 @@ enum { ST_F64 = 0, ST_F32 = 1, ST_BF16 = 2 };
 constexpr long long kWaitCyclesDefault = 2LL << 30;
 
 // Launch shapes of the phase kernels: warps per block (one block per SM),
-// shared-memory stages per warp and bytes per stage, and a variant: for phase
-// 1 the lane mapping (0: the lanes of a column segment split its rows and
-// reduce by shuffles; 1: one lane per column, no cross-lane reduction), for
-// phase 2 how far ahead the multipliers are gathered (0: one chunk, 1: two).  Every shape
-// is compiled for every storage type; hbi_construct_lh times them on the
-// operator and keeps the fastest per phase (autotune_stream_shapes).  Shape
-// 0 of each phase is the default.
+// shared-memory stages per warp and bytes per stage, and a variant: for
+// phase 1 the lane mapping (0: the lanes of a column segment split its rows
+// and reduce by shuffles; 1: one lane per column, no cross-lane reduction),
+// for phase 2 how far ahead the multipliers are gathered (0: one chunk, 1:
+// two).  Every shape is compiled for every storage type; hbi_construct_lh
+// times them on the operator and keeps the fastest per phase
+// (autotune_stream_shapes).  Shape 0 of each phase is the default.
 struct StreamShape {
   int nw, ns, sb, map;
 };
@@ -66,6 +66,38 @@ constexpr StreamShape kShapes2[kNumShapes2] = {{12, 2, 8192, 0}, {8, 3, 8192, 0}
                                                {10, 2, 8192, 0}, {8, 3, 8192, 1}};
 inline const StreamShape& stream_shape(int phase, int s) { return phase == 1 ? kShapes1[s] : kShapes2[s]; }
 inline int num_shapes(int phase) { return phase == 1 ? kNumShapes1 : kNumShapes2; }
+
+// Programmatic dependent launch of the product chain (phase 1 -> phase 2 ->
+// phase 3 -> next stage's phase 1): a kernel launched with the programmatic
+// stream-serialization attribute may start while its predecessor drains; it
+// first does what depends on nothing the predecessors write (barrier set-up,
+// the schedule, the first bulk copies of factor data), then waits for the
+// predecessor grid to complete (pdl_wait_prior; transitively all earlier
+// kernels of the stream).  pdl_launch_dependents lets the next grid start
+// as soon as this grid's SMs free up.  Both are no-ops in a grid launched
+// without the attribute.  HBI_PDL=0 launches the chain without it.
+__device__ __forceinline__ void pdl_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait_prior() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+bool pdl_enabled();
+
+// kernel launch, with the programmatic stream-serialization attribute when pdl
+template <typename... KArgs, typename... Args>
+cudaError_t launch_kernel(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, bool pdl,
+                          Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, k, args...);
+}
 
 // work items of the streamed product (plan_stream in hbi_structure.cpp)
 typedef S1Item S1ItemDev;

@@ -53,6 +53,8 @@ __device__ __forceinline__ double row_value(const MatDev& m, int r) {
 }
 
 __global__ void __launch_bounds__(256) p3_plain_kernel(MatDev m0, MatDev m1, int nmat, double* y0, double* y1) {
+  pdl_launch_dependents();
+  pdl_wait_prior();
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= m0.n) return;
   y0[r] = row_value(m0, r);
@@ -60,6 +62,8 @@ __global__ void __launch_bounds__(256) p3_plain_kernel(MatDev m0, MatDev m1, int
 }
 
 __global__ void __launch_bounds__(128) p3_rk_kernel(MatDev m0, MatDev m1, RkDev R, int s, double* __restrict__ xnext) {
+  pdl_launch_dependents();
+  pdl_wait_prior();
   if (R.flags && __ldcg(&R.flags[0])) return;
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   double emax = -1.0;
@@ -146,6 +150,8 @@ __global__ void __launch_bounds__(128) p3_rk_kernel(MatDev m0, MatDev m1, RkDev 
 // start of an attempt: stage state = accepted state, its slip rate and the
 // stage-0 matvec input; clear the attempt's error accumulators
 __global__ void rk_prepare_kernel(RkDev R) {
+  pdl_launch_dependents();
+  pdl_wait_prior();
   if (R.flags && __ldcg(&R.flags[0])) return;
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r == 0) {
@@ -165,12 +171,14 @@ __global__ void rk_prepare_kernel(RkDev R) {
 // ------------------------------------------------------------- launchers
 void launch_phase3_plain(const MatDev* mats, int nmat, double* const* y, cudaStream_t st) {
   const MatDev& m1 = nmat == 2 ? mats[1] : mats[0];
-  p3_plain_kernel<<<(mats[0].n + 255) / 256, 256, 0, st>>>(mats[0], m1, nmat, y[0], nmat == 2 ? y[1] : nullptr);
+  launch_kernel(p3_plain_kernel, dim3((mats[0].n + 255) / 256), dim3(256), 0, st, pdl_enabled(), mats[0], m1, nmat,
+                y[0], nmat == 2 ? y[1] : nullptr);
 }
 
 void launch_phase3_rk(const MatDev* mats, int nmat, const RkDev& rk, int stage, double* xnext, cudaStream_t st) {
   const MatDev& m1 = nmat == 2 ? mats[1] : mats[0];
-  p3_rk_kernel<<<(rk.n + 127) / 128, 128, 0, st>>>(mats[0], m1, rk, stage, xnext);
+  launch_kernel(p3_rk_kernel, dim3((rk.n + 127) / 128), dim3(128), 0, st, pdl_enabled(), mats[0], m1, rk, stage,
+                xnext);
 }
 
 void launch_rk_prepare(const RkDev& rk, cudaStream_t st) {

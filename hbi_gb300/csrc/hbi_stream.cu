@@ -236,7 +236,6 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
   constexpr int ESZ = sizeof(T);
   constexpr int BF = SB / 512;  // columns of a chunk of full-height (512-byte) segments
   extern __shared__ __align__(128) unsigned char smem[];
-  if (m0.skip && __ldcg(m0.skip)) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   Ring<NW, NS, SB> R(smem, warp);
   Acc* xs = (Acc*)R.mu;  // MAP 1: the current item's x tile (32 x VEC values)
@@ -285,6 +284,15 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
     }
   };
   for (int q = 0; q < NS; q++) produce();
+  // the factor copies above read only static data; x, z, the partials and
+  // the loop flags belong to earlier kernels of the stream
+  pdl_launch_dependents();
+  pdl_wait_prior();
+  if (m0.skip && __ldcg(m0.skip)) {
+    // a halted loop skips the product: let the copies already started land
+    drain<NS>(R.bar, 0, p_seq);
+    return;
+  }
   // consumer: item ids three ahead, descriptors two
   int c_k = 0, c_it = seq.at(0), c_i1 = seq.at(1), c_i2 = seq.at(2), c_i3 = seq.at(3), c_c0 = 0, c_seq = 0;
   S1ItemDev Dc = desc(c_it), Dn = desc(c_i1), Dnn = desc(c_i2);
@@ -531,7 +539,6 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
   static_assert(NS >= 2, "the multiplier gather runs one chunk ahead");
   static_assert(GA == 1 || (GA == 2 && NS >= 3), "a gather two chunks ahead needs three stages");
   extern __shared__ __align__(128) unsigned char smem[];
-  if (m0.skip && __ldcg(m0.skip)) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   Ring<NW, NS, SB> R(smem, warp);
   Acc* musm = (Acc*)R.mu;
@@ -606,6 +613,14 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
   Pend fifo[NS];
 #pragma unroll
   for (int q = 0; q < NS; q++) produce(fifo[q]);
+  // factor copies and column indices are static data; z, x, the partials and
+  // the loop flags belong to earlier kernels of the stream
+  pdl_launch_dependents();
+  pdl_wait_prior();
+  if (m0.skip && __ldcg(m0.skip)) {
+    drain<NS>(R.bar, 0, p_seq);
+    return;
+  }
   Acc mu[KP], mu2[KP];
   gather(fifo[0], mu);
   if constexpr (GA == 2) gather(fifo[1], mu2);
@@ -760,7 +775,8 @@ void launch_p1s(const MatDev& m0, const MatDev& m1, int nmat, const double* x, i
   constexpr int NW = kShapes1[S].nw, NS = kShapes1[S].ns, SB = kShapes1[S].sb, MAP = kShapes1[S].map;
   const int need = (n + NW - 1) / NW;
   const int grid = need < sm ? (need > 0 ? need : 1) : sm;
-  p1_stream_kernel<T, NW, NS, SB, MAP><<<grid, NW * 32, smem_bytes<NW, NS, SB>(), st>>>(m0, m1, nmat, x, S);
+  launch_kernel(p1_stream_kernel<T, NW, NS, SB, MAP>, dim3(grid), dim3(NW * 32), smem_bytes<NW, NS, SB>(), st,
+                pdl_enabled(), m0, m1, nmat, x, S);
 }
 
 template <typename T, int S>
@@ -768,7 +784,8 @@ void launch_p2s(const MatDev& m0, const MatDev& m1, int nmat, const double* x, i
   constexpr int NW = kShapes2[S].nw, NS = kShapes2[S].ns, SB = kShapes2[S].sb, GA = kShapes2[S].map + 1;
   const int need = (n + NW - 1) / NW;
   const int grid = need < sm ? (need > 0 ? need : 1) : sm;
-  p2_stream_kernel<T, NW, NS, SB, GA><<<grid, NW * 32, smem_bytes<NW, NS, SB>(), st>>>(m0, m1, nmat, x, S);
+  launch_kernel(p2_stream_kernel<T, NW, NS, SB, GA>, dim3(grid), dim3(NW * 32), smem_bytes<NW, NS, SB>(), st,
+                pdl_enabled(), m0, m1, nmat, x, S);
 }
 
 template <typename T>
@@ -829,6 +846,15 @@ void prepare_type() {
 }  // namespace
 
 int forced_stream_shape(int phase) { return env_shape(phase); }
+
+bool pdl_enabled() {
+  static int on = -1;
+  if (on < 0) {
+    const char* e = getenv("HBI_PDL");
+    on = (e && e[0] == '0') ? 0 : 1;
+  }
+  return on == 1;
+}
 
 // the large shared-memory opt-in of the phase kernels, once per process and
 // before any stream capture

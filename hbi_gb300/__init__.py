@@ -392,6 +392,7 @@ class RK:
         _check(lib().hbi_rk_create(C.byref(self.h), C.byref(p), lh_s.h, lh_n.h if lh_n is not None else None),
                "hbi_rk_create")
         self.n, self.lh = n, (lh_s, lh_n)
+        self._loops = weakref.WeakSet()  # time loops running on this handle's stream
         _register(self, 1)
 
     def set_state(self, y):
@@ -447,6 +448,10 @@ class RK:
         _check(lib().hbi_rk_attempt_async(self.h, C.c_double(h), C.c_double(eps)), "hbi_rk_attempt_async")
 
     def close(self):
+        # a time loop issues its work on this handle's stream: free it first
+        # (the garbage collector may finalise the two in either order)
+        for c in list(getattr(self, "_loops", ())):
+            c.close()
         if getattr(self, "h", None) and _lib is not None and not _closed:
             _lib.hbi_rk_free(self.h)
         self.h = None
@@ -482,6 +487,7 @@ class Cycle:
         else:
             _check(lib().hbi_cycle_create(C.byref(self.h), rk.h, _p(vel), _p(ds), C.byref(p)), "hbi_cycle_create")
         self.rk, self.n = rk, rk.n
+        rk._loops.add(self)
         _register(self, 0)
 
     def run(self, k_limit=0, t_limit=0.0):

@@ -125,7 +125,7 @@ struct MatDev {            // one H-matrix on the device
   double scale;            // result multiplier (1/ds0 for 3dph, else 1)
   const int* skip;         // when non-null and nonzero, phases 1-2 do nothing
   int* err;                // set to nonzero when a bulk copy did not arrive in time
-  long long wait;          // bound of a stage wait in SM clock cycles (0: one non-blocking probe)
+  long long wait;          // bound of a stage wait in SM clock cycles (0: every wait gives up at once)
   int ncnt;                // number of arrival counters in cnt
   // static warp schedules (hbi_structure.hpp, plan_warp_schedule), one per
   // launch shape s, for a grid of gw1[s] / gw2[s] warps: warp w walks

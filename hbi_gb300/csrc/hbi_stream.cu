@@ -69,18 +69,6 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(saddr(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
 // lane 0: wait for the phase `parity` of `bar` for at most kWaitCycles
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
   const long long t0 = clock64();
@@ -142,10 +130,10 @@ struct Ring {
 
 // wait for a stage's phase `parity`; all lanes poll together (the loop stays
 // converged) and acquire.  Returns false (and records the error) when the
-// copy did not arrive within `limit` SM clock cycles; limit 0 makes one
-// non-blocking probe.
+// copy did not arrive within `limit` SM clock cycles; a limit of 0 is spent
+// before the first probe, so every wait gives up (the error path on demand).
 __device__ __forceinline__ bool stage_ready(uint64_t* bar, uint32_t parity, int* err, long long limit) {
-  bool ok = limit > 0 ? mbar_try_wait(bar, parity) : mbar_test_wait(bar, parity);
+  bool ok = limit > 0 && mbar_try_wait(bar, parity);
   if (!ok && limit > 0) {
     const long long t0 = clock64();
     while (!(ok = mbar_try_wait(bar, parity)))

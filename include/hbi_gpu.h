@@ -145,9 +145,11 @@ int hbi_adot_lattice_hyp_dev(double* d_au, hbi_lhp* st_LHp, const double* d_u, v
 int hbi_lh_check_error(hbi_lhp* st_LHp);
 /* Test hook (no reference counterpart): the bound of the product kernels'
  * bulk-copy waits in SM clock cycles for products launched afterwards
- * (operators already bound to an RK handle keep theirs); 0 makes each wait a
- * single non-blocking probe, so that waits run out without anything being
- * wrong; a negative value restores the default bound. */
+ * (operators already bound to an RK handle keep theirs); 0 is a bound that
+ * is spent before the first probe, so every wait gives up -- the path of a
+ * wait that ran out (error word set, copies in flight drained with the
+ * default bound, early exit) without anything being wrong; a negative value
+ * restores the default bound. */
 int hbi_lh_set_wait_limit(hbi_lhp* st_LHp, long long cycles);
 
 /* The product of hbi_adot_lattice_hyp_dev without any device allocation.

@@ -4,10 +4,10 @@ reads, through the C ABI.
 Every wait of the phase kernels for one of their bulk copies is bounded; a
 wait that runs out sets the operator's device error word and the warp leaves
 after its copies in flight have landed.  These tests make the waits run out
-without anything being wrong: hbi_lh_set_wait_limit(lh, 0) turns each wait
-into a single non-blocking probe, which fails for nearly every stage because
-a copy from HBM takes far longer than one probe.  All copies are valid and
-are waited for before the kernel ends, so nothing faults or hangs.
+without anything being wrong: hbi_lh_set_wait_limit(lh, 0) gives each wait a
+bound that is spent before its first probe, so every wait gives up and takes
+the path of a timed-out one.  All copies are valid and are waited for (with
+the default bound) before the warp leaves, so nothing faults or hangs.
 
 Checked: the blocking product returns HBI_ERR_DEVICE, the asynchronous one
 reports it through hbi_lh_check_error, the device time loop stops with

@@ -882,6 +882,9 @@ static int construct_impl(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* c, int
 
 extern "C" int hbi_free_lh(hbi_lhp* h) {
   if (!h) return HBI_OK;
+  // RK handles, time loops and ensembles read the stores on streams of their
+  // own: let all device work end before the memory goes
+  cudaDeviceSynchronize();
   for (void* p : {h->d_vstore, h->d_ustore, (void*)h->d_s1, (void*)h->d_s2, (void*)h->d_cnt, h->d_part, h->d_z,
                   h->d_gpart, (void*)h->d_midx, (void*)h->d_grow0, (void*)h->d_gndl, (void*)h->d_gnch,
                   (void*)h->d_gpoff, (void*)h->d_row_fc, (void*)h->d_fc_ptr, (void*)h->d_fc_group, (void*)h->d_err,
@@ -1138,7 +1141,8 @@ extern "C" int hbi_rk_create(hbi_rk** out, const hbi_rsf_params* p, hbi_lhp* ls,
 
 extern "C" int hbi_rk_free(hbi_rk* r) {
   if (!r) return HBI_OK;
-  if (r->st) cudaStreamSynchronize(r->st);
+  // a time loop may still run on its own stream with this handle's state
+  cudaDeviceSynchronize();
   if (r->gexec) cudaGraphExecDestroy(r->gexec);
   for (double* p : r->allocs) cudaFree(p);
   if (r->h_ctl) cudaFreeHost(r->h_ctl);

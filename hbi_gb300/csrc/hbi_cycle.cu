@@ -795,6 +795,7 @@ extern "C" int hbi_cycle_free(hbi_cycle* c) {
   cudaFree(c->dprop);
   if (c->hring) cudaFreeHost(c->hring);
   if (c->hsnap) cudaFreeHost(c->hsnap);
+  if (c->st) cudaStreamDestroy(c->st);
   delete c;
   return HBI_OK;
 }
@@ -831,7 +832,14 @@ int cycle_create_impl(hbi_cycle** out, hbi_rk* rk, const double* vel, const doub
     delete c;
     return rc;
   }
-  c->st = (cudaStream_t)hbi_rk_stream(rk);
+  // the loop works on a stream of its own, after whatever the RK handle has
+  // enqueued: freeing the loop then never touches the RK handle's stream
+  if (cudaStreamSynchronize((cudaStream_t)hbi_rk_stream(rk)) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
+    c->st = nullptr;
+    delete c;
+    return cfail(HBI_ERR_CUDA, "hbi_cycle_create: stream");
+  }
   const int n = c->V.n;
   CycleConst& P = c->P;
   P.n = n;

@@ -68,14 +68,15 @@ inline const StreamShape& stream_shape(int phase, int s) { return phase == 1 ? k
 inline int num_shapes(int phase) { return phase == 1 ? kNumShapes1 : kNumShapes2; }
 
 // Programmatic dependent launch of the product chain (phase 1 -> phase 2 ->
-// phase 3 -> next stage's phase 1): a kernel launched with the programmatic
-// stream-serialization attribute may start while its predecessor drains; it
-// first does what depends on nothing the predecessors write (barrier set-up,
-// the schedule, the first bulk copies of factor data), then waits for the
-// predecessor grid to complete (pdl_wait_prior; transitively all earlier
-// kernels of the stream).  pdl_launch_dependents lets the next grid start
-// as soon as this grid's SMs free up.  Both are no-ops in a grid launched
-// without the attribute.  HBI_PDL=0 launches the chain without it.
+// phase 3; phase 1 itself starts after its predecessor has completed): a
+// kernel launched with the programmatic stream-serialization attribute may
+// start while its predecessor drains; it first does what depends on nothing
+// the predecessors write (barrier set-up, the schedule, the first bulk copies
+// of factor data), then waits for the predecessor grid to complete
+// (pdl_wait_prior; transitively all earlier kernels of the stream).
+// pdl_launch_dependents lets the next grid start as soon as this grid's SMs
+// free up.  Both are no-ops in a grid launched without the attribute.
+// HBI_PDL=0 launches the chain without it.
 __device__ __forceinline__ void pdl_launch_dependents() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }

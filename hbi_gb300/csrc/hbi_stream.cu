@@ -763,8 +763,12 @@ void launch_p1s(const MatDev& m0, const MatDev& m1, int nmat, const double* x, i
   constexpr int NW = kShapes1[S].nw, NS = kShapes1[S].ns, SB = kShapes1[S].sb, MAP = kShapes1[S].map;
   const int need = (n + NW - 1) / NW;
   const int grid = need < sm ? (need > 0 ? need : 1) : sm;
-  launch_kernel(p1_stream_kernel<T, NW, NS, SB, MAP>, dim3(grid), dim3(NW * 32), smem_bytes<NW, NS, SB>(), st,
-                pdl_enabled(), m0, m1, nmat, x, S);
+  // phase 1 starts after its predecessor has completed (no programmatic
+  // launch): a phase-1 block needs nearly all of an SM's registers, and one
+  // started early would keep the rest of the previous stage's phase-3 blocks
+  // off its SM
+  launch_kernel(p1_stream_kernel<T, NW, NS, SB, MAP>, dim3(grid), dim3(NW * 32), smem_bytes<NW, NS, SB>(), st, false,
+                m0, m1, nmat, x, S);
 }
 
 template <typename T, int S>

@@ -30,6 +30,7 @@ relative; a mismatch fails the gate and is listed, never dropped.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--store f32|bf16|f64]
   python bench.py --impl reference ...   # the CPU oracle port, all host cores
   python bench.py --mode matvec|ensemble  # product kernels alone / configuration c4
+  python bench.py --mode kernels --imax 128 --jmax 128  # one small run of every other kernel (for ncu)
 """
 import argparse
 import json
@@ -61,7 +62,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-same-precision", action="store_true")
-    ap.add_argument("--mode", default="step", choices=["step", "matvec", "ensemble"])
+    ap.add_argument("--mode", default="step", choices=["step", "matvec", "ensemble", "kernels"])
     ap.add_argument("--sim-config", default="c3", choices=["c3", "c2"],
                     help="workload of the sim-yr/h comparison (c3: the 200,000-triangle rough fault)")
     ap.add_argument("--sim-window-yr", type=float, default=20.0,
@@ -550,6 +551,45 @@ def run_reference(args):
     })
 
 
+def run_kernels_mode(args):
+    """One small run of every kernel outside the product's phases, sized for
+    an ncu capture: assembly of both H-matrices of the Okada plane at
+    imax x jmax (aca_plus, dense_fill), four Cash-Karp attempts (rk_prepare,
+    p3_rk), 60 steps of the device time loop (cycle_*) and a short proposer
+    fit on their trace (mlp_*).  Prints one JSON line of wall times; it is no
+    bench line."""
+    import hbi_gb300 as H
+    from hbi_gb300 import configs, proposer
+    w = configs.c2_3dph(args.imax, args.jmax)
+    ctl_s, ctl_n = H.Ctl(w.nd), H.Ctl(w.nd)
+    t0 = time.perf_counter()
+    lf_s = H.LeafMtxp(ctl_s, w.geometry("s"), w.eps_h)
+    lf_n = H.LeafMtxp(ctl_n, w.geometry("n"), w.eps_h)
+    lh_s, lh_n = H.LHp(lf_s, ctl_s, args.store), H.LHp(lf_n, ctl_n, args.store)
+    t1 = time.perf_counter()
+    ndc, lodc = H.HACApK_gen_lattice_vector(ctl_s)
+    y0, p = w.initial_state(lodc)
+    rk = H.RK(lh_s, lh_n, evlaw=w.evlaw, scale=w.scale, a=p["a"], b=p["b"], dc=p["dc"], f0=p["f0"], vpl=p["vpl"])
+    rk.set_state(y0)
+    for _ in range(4):
+        rk.attempt_async(1e5, 1e-5)
+    rk.check_error()
+    c = H.Cycle(rk, p["vel"], w.ds_area[lodc - 1], eps_r=1e-6)
+    t2 = time.perf_counter()
+    st = c.run(k_limit=60)
+    t3 = time.perf_counter()
+    X, T = proposer.training_set(c.trace())
+    wts, hist = proposer.train(X, T, epochs=3, min_steps=20)
+    t4 = time.perf_counter()
+    c.close(); rk.close()
+    for o in (lh_s, lh_n, lf_s, lf_n, ctl_s, ctl_n):
+        o.close()
+    print(json.dumps({"mode": "kernels", "workload": f"{w.name}: {w.nd} elements, {args.store} stores",
+                      "assembly_s": round(t1 - t0, 3), "loop_steps": st["k"], "loop_s": round(t3 - t2, 3),
+                      "proposer_samples": int(len(T)), "proposer_fit_s": round(t4 - t3, 3),
+                      "proposer_loss": float(hist[-1])}))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -558,6 +598,8 @@ def main():
         run_matvec_mode(args)
     elif args.mode == "ensemble":
         run_ensemble_mode(args)
+    elif args.mode == "kernels":
+        run_kernels_mode(args)
     else:
         run_ours(args)
 

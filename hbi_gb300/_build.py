@@ -21,7 +21,7 @@ NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcomp
            "-I" + CSRC]
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-I" + CSRC]
 
-CU = ["hbi_capi.cu", "hbi_aca.cu", "hbi_aca_okada.cu", "hbi_aca_td.cu", "hbi_aca_tdhs.cu", "hbi_matvec.cu", "hbi_stream.cu", "hbi_cycle.cu", "hbi_mlp.cu", "hbi_ensemble.cu", "hbi_ens.cu", "hbi_enstc.cu"]
+CU = ["hbi_capi.cu", "hbi_aca.cu", "hbi_aca_okada.cu", "hbi_aca_td.cu", "hbi_aca_tdhs.cu", "hbi_matvec.cu", "hbi_stream.cu", "hbi_cycle.cu", "hbi_mlp.cu", "hbi_umma_probe.cu", "hbi_ens.cu", "hbi_enstc.cu"]
 CPP = ["hbi_structure.cpp"]
 
 

@@ -234,20 +234,24 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
   __syncwarp();
   const int gw = blockIdx.x * NW + warp, GW = gridDim.x * NW;
   const int n0 = m0.ns1, ntot = nmat == 2 ? n0 + m1.ns1 : n0;
-  // the item's chunk width follows from this shape's stage size
+  // descriptors are loaded ahead of their use; the chunk width, which
+  // follows from this shape's stage size, is derived only when an item
+  // becomes current, so that no warp waits for a descriptor load it issued
+  // just before
   auto desc = [&](int it) -> S1ItemDev {
     S1ItemDev d{};
-    if (it < ntot) {
-      d = it < n0 ? m0.s1[it] : m1.s1[it - n0];
-      d.cc = chunk_cols(d.ntp, ESZ, SB);
-    }
+    if (it < ntot) d = it < n0 ? m0.s1[it] : m1.s1[it - n0];
+    return d;
+  };
+  auto current = [&](S1ItemDev d) {
+    d.cc = d.ntp > 0 ? chunk_cols(d.ntp, ESZ, SB) : 16;
     return d;
   };
   const WarpSeq seq = warp_seq(m0, m1, nmat, 1, shape, gw, GW, n0, ntot);
   // producer: walks this warp's items chunk by chunk, NS chunks ahead; the
   // item ids are fetched two items ahead, the descriptors one
   int p_k = 0, p_it = seq.at(0), p_itn = seq.at(1), p_itnn = seq.at(2), p_c0 = 0, p_seq = 0;
-  S1ItemDev Dp = desc(p_it), Dpn = desc(p_itn);
+  S1ItemDev Dp = current(desc(p_it)), Dpn = desc(p_itn);
   auto produce = [&]() {
     if (p_it >= ntot) return;
     const int nc = min(Dp.cc, Dp.ncols - p_c0);
@@ -267,7 +271,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
       p_itn = p_itnn;
       p_itnn = seq.at(p_k + 2);
       p_c0 = 0;
-      Dp = Dpn;
+      Dp = current(Dpn);
       Dpn = desc(p_itn);
     }
   };
@@ -283,7 +287,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
   }
   // consumer: item ids three ahead, descriptors two
   int c_k = 0, c_it = seq.at(0), c_i1 = seq.at(1), c_i2 = seq.at(2), c_i3 = seq.at(3), c_c0 = 0, c_seq = 0;
-  S1ItemDev Dc = desc(c_it), Dn = desc(c_i1), Dnn = desc(c_i2);
+  S1ItemDev Dc = current(desc(c_it)), Dn = desc(c_i1), Dnn = desc(c_i2);
   // x rows of an item: MAP 0, lane j of each column slot holds rows
   // j*VEC .. j*VEC+VEC-1; MAP 1, lane L holds rows L*VEC .. (for the tile)
   auto load_x = [&](const S1ItemDev& D, Acc* xv) {
@@ -493,7 +497,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
     c_i2 = c_i3;
     c_i3 = seq.at(c_k + 3);
     c_c0 = 0;
-    Dc = Dn;
+    Dc = current(Dn);
     Dn = Dnn;
 #pragma unroll
     for (int v = 0; v < VEC; v++) xc[v] = xn[v];
@@ -537,12 +541,15 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
   __syncwarp();
   const int gw = blockIdx.x * NW + warp, GW = gridDim.x * NW;
   const int n0 = m0.ns2, ntot = nmat == 2 ? n0 + m1.ns2 : n0;
+  // descriptors are loaded an item ahead; the chunk width is derived when
+  // the item becomes current (no wait on a load issued just before)
   auto desc = [&](int it) -> S2ItemDev {
     S2ItemDev d{};
-    if (it < ntot) {
-      d = it < n0 ? m0.s2[it] : m1.s2[it - n0];
-      d.cc = chunk_cols(d.ntp, ESZ, SB);
-    }
+    if (it < ntot) d = it < n0 ? m0.s2[it] : m1.s2[it - n0];
+    return d;
+  };
+  auto current = [&](S2ItemDev d) {
+    d.cc = d.ntp > 0 ? chunk_cols(d.ntp, ESZ, SB) : 16;
     return d;
   };
   // column indices of a chunk in flight: lane L holds columns L + 32 i
@@ -552,7 +559,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
   };
   const WarpSeq seq = warp_seq(m0, m1, nmat, 2, shape, gw, GW, n0, ntot);
   int p_k = 0, p_it = seq.at(0), p_itn = seq.at(1), p_itnn = seq.at(2), p_c0 = 0, p_seq = 0;
-  S2ItemDev Dp = desc(p_it), Dpn = desc(p_itn);
+  S2ItemDev Dp = current(desc(p_it)), Dpn = desc(p_itn);
   auto produce = [&](Pend& pd) {
     pd.nc = 0;
     pd.sec = 0;
@@ -584,7 +591,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
       p_itn = p_itnn;
       p_itnn = seq.at(p_k + 2);
       p_c0 = 0;
-      Dp = Dpn;
+      Dp = current(Dpn);
       Dpn = desc(p_itn);
     }
   };
@@ -613,7 +620,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
   gather(fifo[0], mu);
   if constexpr (GA == 2) gather(fifo[1], mu2);
   int c_k = 0, c_it = seq.at(0), c_i1 = seq.at(1), c_i2 = seq.at(2), c_c0 = 0, c_seq = 0;
-  S2ItemDev Dc = desc(c_it), Dn = desc(c_i1);
+  S2ItemDev Dc = current(desc(c_it)), Dn = desc(c_i1);
   Acc acc[VEC];
 #pragma unroll
   for (int v = 0; v < VEC; v++) acc[v] = 0;
@@ -696,7 +703,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
     c_i1 = c_i2;
     c_i2 = seq.at(c_k + 2);
     c_c0 = 0;
-    Dc = Dn;
+    Dc = current(Dn);
     Dn = desc(c_i1);
   }
 }

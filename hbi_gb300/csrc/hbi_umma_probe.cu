@@ -1,4 +1,4 @@
-// hbi_ensemble.cu -- tensor-core (tcgen05) building blocks of the ensemble
+// hbi_umma_probe.cu -- tensor-core (tcgen05) building blocks of the ensemble
 // product: one H-matrix applied to the slip-rate vectors of 64 simulations at
 // once, which turns each product into a dense multi-vector contraction.
 //

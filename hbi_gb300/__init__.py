@@ -43,7 +43,7 @@ EXPORTS = [
     "hbi_mlp_create", "hbi_mlp_free", "hbi_mlp_set_params", "hbi_mlp_get_params", "hbi_mlp_loss_grad",
     "hbi_mlp_train", "hbi_mlp_predict", "hbi_plan_emulate", "hbi_umma_probe",
     "hbi_ens_create", "hbi_ens_free", "hbi_ens_set_state", "hbi_ens_get_state", "hbi_ens_run",
-    "hbi_tc_plan_emulate", "hbi_ens_use_tensor_cores", "hbi_cycle_restart", "hbi_restart_point",
+    "hbi_tc_plan_emulate", "hbi_ens_use_tensor_cores", "hbi_ens_product", "hbi_cycle_restart", "hbi_restart_point",
     "hbi_plan_warp_schedule", "hbi_lh_check_error", "hbi_lh_set_wait_limit", "hbi_rk_check_error",
     "hbi_stream_shapes", "hbi_lh_tuning", "hbi_autotune_select", "hbi_lh_set_shapes",
     "hbi_partition_leaves", "hbi_construct_lh_part", "hbi_mlp_set_loss",
@@ -748,6 +748,19 @@ class Ensemble:
         _check(lib().hbi_ens_use_tensor_cores(self.h, lf_s.h, lf_n.h if lf_n is not None else None),
                "hbi_ens_use_tensor_cores")
         self.lf = (lf_s, lf_n)
+
+    def product(self, x, reps=0):
+        """One multi-vector product of both H-matrices on the 64 members'
+        vectors x (n, 64), cluster order (hbi_ens_product): returns (ys, yn,
+        ms per product or None)."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        if x.shape != (self.n, 64):
+            raise ValueError(f"x: shape {x.shape}, expected ({self.n}, 64)")
+        ys, yn = np.zeros_like(x), np.zeros_like(x)
+        ms = C.c_double(0.0)
+        _check(lib().hbi_ens_product(self.h, x.ctypes.data_as(_fp), ys.ctypes.data_as(_fp),
+                                     yn.ctypes.data_as(_fp), int(reps), C.byref(ms)), "hbi_ens_product")
+        return ys, yn, (ms.value if reps > 0 else None)
 
     def run(self, t_limit, eps_r=1e-6, dtinit=1.0, dtmax=1e10):
         st = EnsStatus()

@@ -1542,7 +1542,7 @@ extern "C" int hbi_tc_plan_emulate(int n, int nleaf, const int* lv6, const doubl
   }
   std::vector<double> z(std::max<int64_t>(T.zlen, 1), 0.0), part(std::max<int64_t>(T.plen1, 1), 0.0);
   for (const TcItem& it : T.p1) {
-    if (it.np % 8 || it.np > 256 || it.kp % 16 || it.kp > 256 || it.nv > it.np || it.kv > it.kp || it.m0 < 0 ||
+    if (it.np % 8 || it.np > 256 || it.kp % 16 || it.kp > kTcK1 || it.nv > it.np || it.kv > it.kp || it.m0 < 0 ||
         it.m0 + it.kv > n || it.out0 + it.nv > T.zlen || it.soff + (int64_t)it.kp * it.np * 2 > T.store1 ||
         (it.ntile > 1 && it.poff + (int64_t)it.ntile * it.nv > T.plen1))
       return fail(HBI_ERR_STATE, "tc phase-1 item out of bounds");

@@ -35,6 +35,7 @@
 #include <vector>
 
 #include "../../include/hbi_gpu.h"
+#include "hbi_enstc.cuh"
 #include "hbi_kernels.cuh"
 #include "hbi_rsf.cuh"
 
@@ -42,24 +43,7 @@ namespace hbi {
 int set_error(int code, const char* msg);
 int lhp_view(hbi_lhp* h, LhpView* v);
 int leaf_view(const hbi_leafmtxp* lf, const double** d_body, std::vector<int64_t>* off, std::vector<Leaf>* leaves);
-struct TcMat {
-  const TcItem* p1;
-  int n1;
-  const TcItem* p2;
-  int n2;
-  const __nv_bfloat16* s1;
-  const __nv_bfloat16* s2;
-  const int32_t* midx;
-  float* z;
-  float* part;
-  int* cnt;
-  float* gpart;
-  int* err;
-};
-size_t tc_smem_bytes();
-void tc_prepare();
-void launch_tc(int phase, const TcMat& a, const TcMat& b, int nmat, const float* x, int sm, cudaStream_t st);
-void launch_tcconv(const double* body, const TcCopy* map, int64_t nmap, __nv_bfloat16* dst, cudaStream_t st);
+
 
 namespace {
 
@@ -627,6 +611,16 @@ __global__ void update_e_kernel(EnsDev E) {
 size_t smem1() { return 2 * (size_t)kXT + 2 * (size_t)kChunk + 64; }
 size_t smem2() { return 2 * (size_t)(kChunk + kBrows) + 8 * 16 * EM * 4 + 64; }
 
+// y (element, member) = the group sums of one product, both matrices
+__global__ void __launch_bounds__(256) ens_sum_kernel(EnsMat A, EnsMat B, int nmat, int n, float* __restrict__ ys,
+                                                      float* __restrict__ yn) {
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)n * EM) return;
+  const int m = (int)(idx % EM), r = (int)(idx / EM);
+  ys[idx] = (float)group_sum_e(A, r, m);
+  if (nmat == 2) yn[idx] = (float)group_sum_e(B, r, m);
+}
+
 }  // namespace
 }  // namespace hbi
 
@@ -669,8 +663,8 @@ void enqueue_e(hbi_ens* e) {
     const float* xin = s == 0 ? E.x0 : E.xb[s & 1];
     float* xout = E.xb[(s + 1) & 1];
     if (e->tc) {
-      launch_tc(1, e->T[0], e->T[e->nmat - 1], e->nmat, xin, e->sm, st);
-      launch_tc(2, e->T[0], e->T[e->nmat - 1], e->nmat, xin, e->sm, st);
+      launch_tc(1, e->T[0], e->T[e->nmat - 1], e->nmat, xin, st);
+      launch_tc(2, e->T[0], e->T[e->nmat - 1], e->nmat, xin, st);
     } else {
       p1e_kernel<<<g1, 256, smem1(), st>>>(e->M[0], e->M[e->nmat - 1], e->nmat, xin);
       p2e_kernel<<<g1, 256, smem2(), st>>>(e->M[0], e->M[e->nmat - 1], e->nmat, xin);
@@ -838,6 +832,27 @@ extern "C" int hbi_ens_get_state(hbi_ens* e, double* y, double* slip, double* x)
   return HBI_OK;
 }
 
+namespace {
+// a product kernel that gave up a bulk-copy wait invalidates the results;
+// the operators' and the ensemble's arrival counters start over
+int ens_check_device(hbi_ens* e, const char* who) {
+  bool bad = false;
+  for (int k = 0; k < e->nmat; k++) {
+    const int t = take_device_error(e->M[k].m);
+    if (t < 0) return efail(HBI_ERR_CUDA, who);
+    if (t > 0) {
+      bad = true;
+      if (cudaMemset(e->M[k].cnt, 0, sizeof(int) * (size_t)std::max<int64_t>(e->ncnt_m[k], 1)) != cudaSuccess ||
+          (e->T[k].cnt &&
+           cudaMemset(e->T[k].cnt, 0, sizeof(int) * (size_t)std::max<int64_t>(e->ncnt_t[k], 1)) != cudaSuccess))
+        return efail(HBI_ERR_CUDA, who);
+    }
+  }
+  if (bad) return efail(HBI_ERR_DEVICE, "a product kernel gave up waiting for a bulk copy; the results are invalid");
+  return HBI_OK;
+}
+}  // namespace
+
 extern "C" int hbi_ens_run(hbi_ens* e, double eps_r, double dtinit, double dtmax, double t_limit,
                            hbi_ens_status* out) {
   if (!e || !(eps_r > 0) || !(dtinit > 0) || !(t_limit > 0)) return efail(HBI_ERR_ARG, "hbi_ens_run: arguments");
@@ -889,23 +904,59 @@ extern "C" int hbi_ens_run(hbi_ens* e, double eps_r, double dtinit, double dtmax
     }
     out->wall_s = wall;
   }
-  // a product kernel that gave up a bulk-copy wait invalidates the run; the
-  // operators' and the ensemble's arrival counters start over
-  bool bad = false;
-  for (int k = 0; k < e->nmat; k++) {
-    const int t = take_device_error(e->M[k].m);
-    if (t < 0) return efail(HBI_ERR_CUDA, "hbi_ens_run: device error word");
-    if (t > 0) {
-      bad = true;
-      if (cudaMemset(e->M[k].cnt, 0, sizeof(int) * (size_t)std::max<int64_t>(e->ncnt_m[k], 1)) != cudaSuccess ||
-          (e->T[k].cnt &&
-           cudaMemset(e->T[k].cnt, 0, sizeof(int) * (size_t)std::max<int64_t>(e->ncnt_t[k], 1)) != cudaSuccess))
-        return efail(HBI_ERR_CUDA, "hbi_ens_run: counter reset");
-    }
+  return ens_check_device(e, "hbi_ens_run");
+}
+
+extern "C" int hbi_ens_product(hbi_ens* e, const float* x, float* ys, float* yn, int reps, double* ms) {
+  if (!e || !x || !ys || (e->nmat == 2 && !yn) || reps < 0)
+    return efail(HBI_ERR_ARG, "hbi_ens_product: bad arguments");
+  const int64_t tot = (int64_t)e->n * EM;
+  const size_t bytes = (size_t)tot * sizeof(float);
+  float *dys = nullptr, *dyn = nullptr;
+  if (cudaMalloc(&dys, bytes) != cudaSuccess || cudaMalloc(&dyn, bytes) != cudaSuccess) {
+    cudaFree(dys);
+    return efail(HBI_ERR_NOMEM, "hbi_ens_product: output buffers");
   }
-  if (bad)
-    return efail(HBI_ERR_DEVICE, "hbi_ens_run: a product kernel gave up waiting for a bulk copy; the run is invalid");
-  return HBI_OK;
+  cudaStream_t st = e->st;
+  const int blocks = (int)((tot + 255) / 256);
+  auto once = [&]() {
+    if (e->tc) {
+      launch_tc(1, e->T[0], e->T[e->nmat - 1], e->nmat, e->E.x0, st);
+      launch_tc(2, e->T[0], e->T[e->nmat - 1], e->nmat, e->E.x0, st);
+    } else {
+      p1e_kernel<<<e->sm * 2, 256, smem1(), st>>>(e->M[0], e->M[e->nmat - 1], e->nmat, e->E.x0);
+      p2e_kernel<<<e->sm * 2, 256, smem2(), st>>>(e->M[0], e->M[e->nmat - 1], e->nmat, e->E.x0);
+    }
+    ens_sum_kernel<<<blocks, 256, 0, st>>>(e->M[0], e->M[e->nmat - 1], e->nmat, e->n, dys, dyn);
+  };
+  int rc = HBI_OK;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaMemcpyAsync(e->E.x0, x, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) rc = HBI_ERR_CUDA;
+  if (rc == HBI_OK) {
+    once();
+    if (reps > 0) {
+      cudaEventCreate(&e0);
+      cudaEventCreate(&e1);
+      cudaEventRecord(e0, st);
+      for (int r = 0; r < reps; r++) once();
+      cudaEventRecord(e1, st);
+    }
+    if (cudaStreamSynchronize(st) != cudaSuccess) rc = HBI_ERR_CUDA;
+  }
+  if (rc == HBI_OK && reps > 0 && ms) {
+    float t = 0.f;
+    cudaEventElapsedTime(&t, e0, e1);
+    *ms = (double)t / reps;
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (rc == HBI_OK && (cudaMemcpy(ys, dys, bytes, cudaMemcpyDeviceToHost) != cudaSuccess ||
+                       (e->nmat == 2 && cudaMemcpy(yn, dyn, bytes, cudaMemcpyDeviceToHost) != cudaSuccess)))
+    rc = HBI_ERR_CUDA;
+  cudaFree(dys);
+  cudaFree(dyn);
+  if (rc != HBI_OK) return efail(rc, "hbi_ens_product: CUDA");
+  return ens_check_device(e, "hbi_ens_product");
 }
 
 namespace {
@@ -925,13 +976,14 @@ int recapture(hbi_ens* e) {
 
 extern "C" int hbi_ens_use_tensor_cores(hbi_ens* e, const hbi_leafmtxp* lf_s, const hbi_leafmtxp* lf_n) {
   if (!e || !lf_s || (e->nmat == 2 && !lf_n)) return efail(HBI_ERR_ARG, "hbi_ens_use_tensor_cores: null");
+  TcPlan tcp[2];
   for (int k = 0; k < e->nmat; k++) {
     const double* body = nullptr;
     std::vector<int64_t> off;
     std::vector<Leaf> leaves;
     int rc = leaf_view(k ? lf_n : lf_s, &body, &off, &leaves);
     if (rc) return rc;
-    TcPlan P;
+    TcPlan& P = tcp[k];
     plan_tc(e->n, leaves, off, P);
     TcMat& T = e->T[k];
     auto upload = [&](const void* h, size_t bytes) -> void* {
@@ -968,6 +1020,26 @@ extern "C" int hbi_ens_use_tensor_cores(hbi_ens* e, const hbi_leafmtxp* lf_s, co
       e->allocs.pop_back();
     }
   }
+  // both matrices' items dealt over the SMs, longest first (cost = factor
+  // bytes + a fixed cost per item for its epilogue)
+  for (int ph = 1; ph <= 2; ph++) {
+    std::vector<int64_t> cost;
+    for (int k = 0; k < e->nmat; k++) {
+      const int cnt = ph == 1 ? e->T[k].n1 : e->T[k].n2;
+      const std::vector<TcItem>& items = ph == 1 ? tcp[k].p1 : tcp[k].p2;
+      for (int i = 0; i < cnt; i++) cost.push_back((int64_t)items[i].np * items[i].kp * 4 + 64 * 1024);
+    }
+    std::vector<int32_t> woff, witem;
+    plan_warp_schedule(cost, e->sm, woff, witem);
+    int32_t* doff = ealloc<int32_t>(e, woff.size(), false);
+    int32_t* ditem = ealloc<int32_t>(e, std::max<size_t>(witem.size(), 1), false);
+    if (!doff || !ditem) return efail(HBI_ERR_NOMEM, "hbi_ens_use_tensor_cores: schedule");
+    cudaMemcpy(doff, woff.data(), woff.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+    if (!witem.empty()) cudaMemcpy(ditem, witem.data(), witem.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+    e->T[0].boff[ph - 1] = doff;
+    e->T[0].bitem[ph - 1] = ditem;
+  }
+  e->T[0].G = e->sm;
   tc_prepare();
   e->tc = true;
   return recapture(e);

@@ -1,66 +1,67 @@
 // hbi_enstc.cu -- the ensemble's multi-vector product on the 5th-generation
 // tensor cores (tcgen05).
 //
-// Each contraction is D (64 members x N) = A (64 x K) * B^T, B (N x K) the
-// factor tile (plan_tc, hbi_structure.cpp):
-//   phase 1: N = the columns of a column group (z = V^T x), K = a tile's rows,
-//            A = the tile's rows of X (64 members);
+// Each contraction is D^T (N x 64 members) = F (N x K) * A (K x 64), F the
+// factor tile (plan_tc, hbi_structure.cpp) on the MMA's M side (128 rows per
+// MMA) and the members on its N side (N = 64):
+//   phase 1: N = the columns of a column group (z = V^T x), K = a tile's rows
+//            (up to 1,024), A = the tile's rows of X (64 members);
 //   phase 2: N = the rows of a row-group tile, K = the group's columns,
 //            A = the columns' multipliers (rows of z or X).
-// B is stored as BF16 hi + lo halves in the canonical no-swizzle K-major
+// F is stored as BF16 hi + lo halves in the canonical no-swizzle K-major
 // layout and arrives by cp.async.bulk (TMA) in stages of 32 K; the FP32 rows
-// of A arrive with it and are split into BF16 hi + lo by the block's threads
-// straight into the canonical layout.  One thread issues, per 16-K chunk,
-// D += A_hi B_hi + A_hi B_lo + A_lo B_hi (the lo x lo term is below FP32's
-// resolution), accumulating in tensor memory (FP32, 64 lanes x N columns);
-// tcgen05.commit on a stage's mbarrier releases the stage.  At the end of an
-// item the warpgroup reads D back with tcgen05.ld (M = 64: member i in lane
-// (i/16)*32 + i%16) and writes the 64 members' results.
+// of A arrive with it and are split into BF16 hi + lo in the canonical layout
+// by a converter warpgroup.  Accumulation is FP32 in tensor memory; the
+// kernel's roles and their hand-offs are described at tc_kernel.
 //
 // Every wait is bounded (about a second of SM clock); on a time-out the
-// operator's error word is set, the block waits (bounded) for its copies and
-// MMAs and releases its tensor memory before it leaves.
+// operator's error word is set, every role leaves its loop, the block waits
+// (bounded) for its copies and MMAs and releases its tensor memory.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
 
+#include "hbi_enstc.cuh"
 #include "hbi_kernels.cuh"
 #include "hbi_umma.cuh"
 
 namespace hbi {
 
-struct TcMat {            // one H-matrix's tensor-core stores and ensemble scratch
-  const TcItem* p1;
-  int n1;
-  const TcItem* p2;
-  int n2;
-  const __nv_bfloat16* s1;  // phase-1 store
-  const __nv_bfloat16* s2;  // phase-2 store
-  const int32_t* midx;
-  float* z;                 // zlen x 64
-  float* part;              // plen1 x 64
-  int* cnt;                 // per column group piece
-  float* gpart;             // rows of the row groups x 64 (the operator's phase-3 layout)
-  int* err;
-};
-
 namespace {
 
 constexpr int EMT = 64;
-constexpr int KC = 32;                    // K per stage
-constexpr int kB = 2 * 256 * 64;          // B hi+lo of 2 chunks at N = 256: 32 KB
-constexpr int kS = KC * EMT * 4;          // FP32 A rows: 8 KB
-constexpr int kA = 2 * 4096;              // A hi+lo of 2 chunks: 8 KB
-constexpr int kStageT = kB + kS + kA;
+constexpr int KC = 32;                       // K per stage: two 16-K MMA chunks
+constexpr int NST = 4;                       // stages
+constexpr int kFac = (KC / 16) * 256 * 64;   // factor hi + lo of a stage, N <= 256: 32 KB
+constexpr int kRows = KC * EMT * 4;          // the members' FP32 rows: 8 KB
+constexpr int kMem = (KC / 16) * 4096;       // the members' operand, hi + lo: 8 KB
+constexpr int kStage = kFac + kRows + kMem;  // 48 KB
+constexpr int kThreads = 320;                // producer, MMA, 4 converter and 4 epilogue warps
+constexpr uint32_t kTmemCols = 256;          // two accumulators x two 128-row blocks x 64 members
 constexpr long long kWaitT = 2LL << 30;
 
+struct Bars {
+  uint64_t full[NST];   // a stage's copies landed (producer's expect_tx)
+  uint64_t conv[NST];   // the stage's member operand is written (128 converter threads)
+  uint64_t empty[NST];  // the stage's MMAs are done (tcgen05.commit)
+  uint64_t accf[2];     // an accumulator holds a finished item (tcgen05.commit)
+  uint64_t acce[2];     // an accumulator was read back (128 epilogue threads)
+  uint64_t done;        // every MMA of the block is done (exit)
+  int abort;            // a role gave up waiting: every role leaves its loop
+  int flag;             // epilogue broadcast
+  uint32_t tslot;       // tensor-memory address
+};
+
 __device__ __forceinline__ uint32_t sa(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void binit(uint64_t* b) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sa(b)) : "memory");
+__device__ __forceinline__ void binit(uint64_t* b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(sa(b)), "r"(count) : "memory");
 }
 __device__ __forceinline__ void bexpect(uint64_t* b, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sa(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void barrive(uint64_t* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(sa(b)) : "memory");
 }
 __device__ __forceinline__ bool btry(uint64_t* b, uint32_t par) {
   uint32_t ok;
@@ -71,10 +72,26 @@ __device__ __forceinline__ bool btry(uint64_t* b, uint32_t par) {
       : "memory");
   return ok != 0;
 }
+// bounded wait, regardless of the abort flag (a block's own copies and MMAs
+// before it leaves)
 __device__ __forceinline__ bool bwait(uint64_t* b, uint32_t par) {
   const long long t0 = clock64();
   while (!btry(b, par))
     if (clock64() - t0 > kWaitT) return false;
+  return true;
+}
+// bounded wait of a role: gives up when another role did, or after the bound
+// (then records the error and tells the other roles)
+__device__ __forceinline__ bool rwait(uint64_t* b, uint32_t par, Bars* br, int* err) {
+  const long long t0 = clock64();
+  while (!btry(b, par)) {
+    if (*(volatile int*)&br->abort) return false;
+    if (clock64() - t0 > kWaitT) {
+      *(volatile int*)&br->abort = 1;
+      if (err) atomicExch(err, 1);
+      return false;
+    }
+  }
   return true;
 }
 __device__ __forceinline__ void bcopy(void* dst, const void* src, uint32_t bytes, uint64_t* b) {
@@ -84,217 +101,276 @@ __device__ __forceinline__ void bcopy(void* dst, const void* src, uint32_t bytes
                : "memory");
 }
 __device__ __forceinline__ void fasync() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void group_sync() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
 __device__ __forceinline__ int arrive_ar(int* p) {
   int old;
   asm volatile("atom.add.acq_rel.gpu.s32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
   return old;
 }
 
-// PH = 1: z = V^T x; PH = 2: partial row sums of U z + A x
+// One block per SM, four roles working on a ring of NST stages:
+//   warp 0        producer: bulk copies of the factor tile's chunks (BF16 hi
+//                 and lo halves, canonical K-major) and of the members' FP32
+//                 rows (phase 1: rows m0 + k of X; phase 2: one gathered row of
+//                 z or X per column);
+//   warps 2-5     converters: the FP32 rows to BF16 hi / lo in the canonical
+//                 K-major layout of the MMA's B operand (member, k);
+//   warp 1        MMA: one thread issues, per 16-K chunk and 128-row block of
+//                 the item, D += F_hi M_hi + F_hi M_lo + F_lo M_hi (M = 128
+//                 factor rows, N = 64 members, K = 16; the lo x lo term is
+//                 below FP32 resolution) into one of two tensor-memory
+//                 accumulators, and commits each stage back to the producer;
+//   warps 6-9     epilogue: read a finished accumulator (tcgen05.ld, one
+//                 thread per factor row, 64 members) and write the item's
+//                 rows, while the MMAs of the next item run in the other
+//                 accumulator.
+// PH = 1: z = V^T x (factor rows = the columns of a column group, K = the
+// rows of a tile); PH = 2: partial row sums U z + A x (factor rows = the rows
+// of a row-group tile, K = the group's columns).
 template <int PH>
-__global__ void __launch_bounds__(128, 2) tc_kernel(TcMat A, TcMat B, int nmat, const float* __restrict__ X) {
+__global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int nmat, const float* __restrict__ X) {
   extern __shared__ __align__(1024) unsigned char sm[];
-  unsigned char* stg[2] = {sm, sm + kStageT};
-  uint64_t* full = (uint64_t*)(sm + 2 * kStageT);
-  uint64_t* mmab = full + 2;
-  uint64_t* itemb = full + 4;
-  __shared__ uint32_t tslot;
-  __shared__ int sh_ok, sh_last;
+  Bars* br = reinterpret_cast<Bars*>(sm + NST * kStage);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
-    for (int i = 0; i < 5; i++) binit(&full[i]);
+    for (int s = 0; s < NST; s++) {
+      binit(&br->full[s], 1);
+      binit(&br->conv[s], 128);
+      binit(&br->empty[s], 1);
+    }
+    for (int b = 0; b < 2; b++) {
+      binit(&br->accf[b], 1);
+      binit(&br->acce[b], 128);
+    }
+    binit(&br->done, 1);
+    br->abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 0) umma::tmem_alloc(&tslot, 256);
+  if (warp == 0) umma::tmem_alloc(&br->tslot, kTmemCols);
   umma::fence_before();
   __syncthreads();
   umma::fence_after();
-  const uint32_t tbase = tslot;
+  const uint32_t tbase = br->tslot;
   const int n0 = PH == 1 ? A.n1 : A.n2;
   const int ntot = nmat == 2 ? n0 + (PH == 1 ? B.n1 : B.n2) : n0;
-  const int G = gridDim.x;
+  // this block's items
+  const int32_t* lst = nullptr;
+  int nit;
+  if (A.boff[PH - 1] && A.G == (int)gridDim.x) {
+    const int o0 = __ldg(&A.boff[PH - 1][blockIdx.x]);
+    nit = __ldg(&A.boff[PH - 1][blockIdx.x + 1]) - o0;
+    lst = A.bitem[PH - 1] + o0;
+  } else {
+    nit = (int)blockIdx.x < ntot ? (ntot - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  }
+  auto item_at = [&](int j) -> int { return lst ? __ldg(&lst[j]) : (int)blockIdx.x + j * (int)gridDim.x; };
   auto desc = [&](int it) -> TcItem {
-    TcItem d{};
-    if (it < ntot) d = PH == 1 ? (it < n0 ? A.p1[it] : B.p1[it - n0]) : (it < n0 ? A.p2[it] : B.p2[it - n0]);
-    return d;
+    return PH == 1 ? (it < n0 ? A.p1[it] : B.p1[it - n0]) : (it < n0 ? A.p2[it] : B.p2[it - n0]);
   };
-  int failed = 0;
-  // producer: stage q of the block's chunk sequence into stg[q & 1]
-  int p_it = blockIdx.x, p_k0 = 0, p_seq = 0;
-  TcItem Dp = desc(p_it);
-  auto produce = [&]() {
-    if (p_it >= ntot || failed) return;
-    const int s = p_seq & 1;
-    const TcMat& M = p_it < n0 ? A : B;
-    if (tid == 0 && p_seq >= 2) {
-      // the MMAs that read this stage before must be done
-      if (!bwait(&mmab[s], (uint32_t)(((p_seq - 2) >> 1) & 1))) failed = 1;
-    }
-    const int kc = min(KC, Dp.kp - p_k0);
-    const int nrow = max(0, min(kc, Dp.kv - p_k0));  // A rows that carry data
-    if (warp == 0 && !__shfl_sync(0xffffffffu, failed, 0)) {
-      const uint32_t bbytes = (uint32_t)((kc / 16) * Dp.np * 64);
-      const __nv_bfloat16* bsrc = (PH == 1 ? M.s1 : M.s2) + Dp.soff + (int64_t)(p_k0 / 16) * Dp.np * 32;
-      int mi = 0;
-      if (PH == 2 && lane < nrow) mi = __ldg(&M.midx[Dp.m0 + p_k0 + lane]);
-      if (lane == 0) {
-        fasync();
-        bexpect(&full[s], bbytes + (uint32_t)(nrow * EMT * 4));
-        bcopy(stg[s], bsrc, bbytes, &full[s]);
-        if (PH == 1 && nrow > 0)
-          bcopy(stg[s] + kB, X + (int64_t)(Dp.m0 + p_k0) * EMT, (uint32_t)(nrow * EMT * 4), &full[s]);
+  auto stage = [&](int s) -> unsigned char* { return sm + s * kStage; };
+
+  if (warp == 0) {
+    // ---------------------------------------------------------- producer
+    int q = 0;
+    for (int j = 0; j < nit; j++) {
+      const int it = item_at(j);
+      const TcItem D = desc(it);
+      const TcMat& M = it < n0 ? A : B;
+      bool ok = true;
+      for (int k0 = 0; k0 < D.kp; k0 += KC, q++) {
+        const int s = q % NST;
+        int w = 1;
+        if (q >= NST && lane == 0) w = rwait(&br->empty[s], (uint32_t)((q / NST - 1) & 1), br, A.err);
+        if (!__shfl_sync(0xffffffffu, w, 0)) {
+          ok = false;
+          break;
+        }
+        const int kc = min(KC, D.kp - k0);
+        const int nrow = max(0, min(kc, D.kv - k0));  // member rows that carry data
+        unsigned char* stg = stage(s);
+        const uint32_t fbytes = (uint32_t)((kc / 16) * D.np * 64);
+        const __nv_bfloat16* fsrc = (PH == 1 ? M.s1 : M.s2) + D.soff + (int64_t)(k0 / 16) * D.np * 32;
+        int mi = 0;
+        if (PH == 2 && lane < nrow) mi = __ldg(&M.midx[D.m0 + k0 + lane]);
+        if (lane == 0) {
+          fasync();
+          bexpect(&br->full[s], fbytes + (uint32_t)(nrow * EMT * 4));
+          bcopy(stg, fsrc, fbytes, &br->full[s]);
+          if (PH == 1 && nrow > 0)
+            bcopy(stg + kFac, X + (int64_t)(D.m0 + k0) * EMT, (uint32_t)(nrow * EMT * 4), &br->full[s]);
+        }
+        __syncwarp();
+        if (PH == 2 && lane < nrow) {
+          const float* src = mi >= 0 ? M.z + (int64_t)mi * EMT : X + (int64_t)(-mi - 1) * EMT;
+          fasync();
+          bcopy(stg + kFac + lane * EMT * 4, src, EMT * 4, &br->full[s]);
+        }
       }
+      if (!ok) break;
+    }
+    // the copies still in flight land before the block leaves (the last NST
+    // issued are the only ones whose phase can still be open)
+    if (lane == 0)
+      for (int r = max(0, q - NST); r < q; r++) bwait(&br->full[r % NST], (uint32_t)((r / NST) & 1));
+    __syncwarp();
+  } else if (warp == 1) {
+    // --------------------------------------------------------------- MMA
+    const uint32_t idesc = umma::idesc_bf16_f32(128, EMT);
+    int q = 0;
+    for (int j = 0; j < nit; j++) {
+      const int b = j & 1;
+      const TcItem D = desc(item_at(j));
+      int w = 1;
+      if (j >= 2 && lane == 0) w = rwait(&br->acce[b], (uint32_t)((j / 2 - 1) & 1), br, A.err);
+      if (!__shfl_sync(0xffffffffu, w, 0)) break;
+      const int nmb = (D.np + 127) / 128;
+      bool ok = true;
+      for (int k0 = 0; k0 < D.kp; k0 += KC, q++) {
+        const int s = q % NST;
+        if (lane == 0) w = rwait(&br->conv[s], (uint32_t)((q / NST) & 1), br, A.err);
+        if (!__shfl_sync(0xffffffffu, w, 0)) {
+          ok = false;
+          break;
+        }
+        if (lane == 0) {
+          umma::fence_after();
+          const int kc = min(KC, D.kp - k0);
+          const unsigned char* stg = stage(s);
+          for (int c = 0; c < kc / 16; c++) {
+            const unsigned char* mem = stg + kFac + kRows + c * 4096;
+            const uint64_t dmh = umma::smem_desc(mem, 1024, 128);
+            const uint64_t dml = umma::smem_desc(mem + 2048, 1024, 128);
+            for (int mb = 0; mb < nmb; mb++) {
+              const unsigned char* fac = stg + c * D.np * 64 + mb * 2048;
+              const uint64_t dfh = umma::smem_desc(fac, (uint32_t)D.np * 16, 128);
+              const uint64_t dfl = umma::smem_desc(fac + D.np * 32, (uint32_t)D.np * 16, 128);
+              const uint32_t d = tbase + (uint32_t)(b * 128 + mb * EMT);
+              umma::mma_bf16(d, dfh, dmh, idesc, (k0 > 0 || c > 0) ? 1 : 0);
+              umma::mma_bf16(d, dfh, dml, idesc, 1);
+              umma::mma_bf16(d, dfl, dmh, idesc, 1);
+            }
+          }
+          umma::commit(&br->empty[s]);
+        }
+        __syncwarp();
+      }
+      if (!ok) break;
+      if (lane == 0) umma::commit(&br->accf[b]);
       __syncwarp();
-      if (PH == 2 && lane < nrow) {
-        const float* src = mi >= 0 ? M.z + (int64_t)mi * EMT : X + (int64_t)(-mi - 1) * EMT;
-        fasync();
-        bcopy(stg[s] + kB + lane * EMT * 4, src, EMT * 4, &full[s]);
-      }
     }
-    p_seq++;
-    p_k0 += kc;
-    if (p_k0 >= Dp.kp) {
-      p_it += G;
-      p_k0 = 0;
-      Dp = desc(p_it);
+    // every MMA issued by this thread is done before the block leaves
+    if (lane == 0) {
+      umma::commit(&br->done);
+      bwait(&br->done, 0);
     }
-  };
-  produce();
-  produce();
-  int c_it = blockIdx.x, c_k0 = 0, c_seq = 0, nitem = 0;
-  TcItem Dc = desc(c_it);
-  while (c_it < ntot) {
-    const TcMat& M = c_it < n0 ? A : B;
-    const int s = c_seq & 1;
-    if (tid == 0) sh_ok = !failed && bwait(&full[s], (uint32_t)((c_seq >> 1) & 1));
-    __syncthreads();
-    if (!sh_ok) {
-      failed = 1;
-      break;
-    }
-    while (!btry(&full[s], (uint32_t)((c_seq >> 1) & 1))) {
-    }
-    const int kc = min(KC, Dc.kp - c_k0);
-    const int nrow = max(0, min(kc, Dc.kv - c_k0));
-    // A: FP32 rows (k, member) -> BF16 hi / lo, canonical K-major (member, k)
-    const float* rows = (const float*)(stg[s] + kB);
-    unsigned char* aop = stg[s] + kB + kS;
-    // one task = one core-matrix row: member m, 8 consecutive k -> 16 bytes
-    // of hi and 16 bytes of lo
-    for (int e = tid; e < (kc / 8) * EMT; e += blockDim.x) {
-      const int kb = e / EMT, m = e % EMT;
-      uint32_t hw[4], lw[4];
+    __syncwarp();
+  } else if (warp < 6) {
+    // -------------------------------------------------------- converters
+    const int ct = tid - 64;
+    int q = 0;
+    bool ok = true;
+    for (int j = 0; j < nit && ok; j++) {
+      const TcItem D = desc(item_at(j));
+      for (int k0 = 0; k0 < D.kp; k0 += KC, q++) {
+        const int s = q % NST;
+        if (!rwait(&br->full[s], (uint32_t)((q / NST) & 1), br, A.err)) {
+          ok = false;
+          break;
+        }
+        const int kc = min(KC, D.kp - k0);
+        const int nrow = max(0, min(kc, D.kv - k0));
+        const float* rows = (const float*)(stage(s) + kFac);
+        unsigned char* mop = stage(s) + kFac + kRows;
+        // one task = one core-matrix row: member m, 8 consecutive k -> 16
+        // bytes of hi and 16 bytes of lo
+        for (int e = ct; e < (kc / 8) * EMT; e += 128) {
+          const int kb = e / EMT, m = e % EMT;
+          uint32_t hw[4], lw[4];
 #pragma unroll
-      for (int i = 0; i < 4; i++) {
-        const int k0 = kb * 8 + 2 * i;
-        const float v0 = k0 < nrow ? rows[k0 * EMT + m] : 0.f;
-        const float v1 = k0 + 1 < nrow ? rows[(k0 + 1) * EMT + m] : 0.f;
-        const __nv_bfloat162 h2 = __floats2bfloat162_rn(v0, v1);
-        const float2 hf = __bfloat1622float2(h2);
-        const __nv_bfloat162 l2 = __floats2bfloat162_rn(v0 - hf.x, v1 - hf.y);
-        hw[i] = *reinterpret_cast<const uint32_t*>(&h2);
-        lw[i] = *reinterpret_cast<const uint32_t*>(&l2);
+          for (int i = 0; i < 4; i++) {
+            const int k = kb * 8 + 2 * i;
+            const float v0 = k < nrow ? rows[k * EMT + m] : 0.f;
+            const float v1 = k + 1 < nrow ? rows[(k + 1) * EMT + m] : 0.f;
+            const __nv_bfloat162 h2 = __floats2bfloat162_rn(v0, v1);
+            const float2 hf = __bfloat1622float2(h2);
+            const __nv_bfloat162 l2 = __floats2bfloat162_rn(v0 - hf.x, v1 - hf.y);
+            hw[i] = *reinterpret_cast<const uint32_t*>(&h2);
+            lw[i] = *reinterpret_cast<const uint32_t*>(&l2);
+          }
+          const uint32_t o = (uint32_t)(kb / 2) * 4096 + umma::kmajor_offset(m, (kb % 2) * 8, 1024, 128);
+          *reinterpret_cast<uint4*>(mop + o) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+          *reinterpret_cast<uint4*>(mop + o + 2048) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+        }
+        fasync();
+        barrive(&br->conv[s]);
       }
-      const uint32_t o = (uint32_t)(kb / 2) * 4096 + umma::kmajor_offset(m, (kb % 2) * 8, 1024, 128);
-      *reinterpret_cast<uint4*>(aop + o) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-      *reinterpret_cast<uint4*>(aop + o + 2048) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
     }
-    fasync();
-    umma::fence_before();
-    __syncthreads();
-    umma::fence_after();
-    const bool last = c_k0 + kc >= Dc.kp;
-    if (tid == 0) {
-      const uint32_t idesc = umma::idesc_bf16_f32(64, Dc.np);
-      for (int c = 0; c < kc / 16; c++) {
-        const unsigned char* bh = stg[s] + c * Dc.np * 64;
-        const uint64_t dbh = umma::smem_desc(bh, (uint32_t)Dc.np * 16, 128);
-        const uint64_t dbl = umma::smem_desc(bh + Dc.np * 32, (uint32_t)Dc.np * 16, 128);
-        const uint64_t dah = umma::smem_desc(aop + c * 4096, 1024, 128);
-        const uint64_t dal = umma::smem_desc(aop + c * 4096 + 2048, 1024, 128);
-        umma::mma_bf16(tbase, dah, dbh, idesc, (c_k0 > 0 || c > 0) ? 1 : 0);
-        umma::mma_bf16(tbase, dah, dbl, idesc, 1);
-        umma::mma_bf16(tbase, dal, dbh, idesc, 1);
-      }
-      umma::commit(&mmab[s]);
-      if (last) umma::commit(&itemb[0]);
-    }
-    c_seq++;
-    produce();
-    c_k0 += kc;
-    if (!last) continue;
-    // item done: D (64 x np) from tensor memory
-    if (tid == 0) sh_ok = !failed && bwait(&itemb[0], (uint32_t)(nitem & 1));
-    __syncthreads();
-    if (!sh_ok) {
-      failed = 1;
-      break;
-    }
-    while (!btry(&itemb[0], (uint32_t)(nitem & 1))) {
-    }
-    umma::fence_after();
-    {
-      const int m = 16 * warp + lane;  // valid for lane < 16
-      const uint32_t taddr = tbase + ((uint32_t)(32 * warp) << 16);
-      // 64 columns per round: four loads in flight, one wait
-      for (int n0c = 0; n0c < Dc.np; n0c += 64) {
+    __syncwarp();
+  } else {
+    // ---------------------------------------------------------- epilogue
+    const int et = tid - 192, quad = warp & 3;
+    for (int j = 0; j < nit; j++) {
+      const int b = j & 1;
+      const int it = item_at(j);
+      const TcItem D = desc(it);
+      const TcMat& M = it < n0 ? A : B;
+      if (et == 0) br->flag = rwait(&br->accf[b], (uint32_t)((j / 2) & 1), br, A.err) ? 1 : 0;
+      group_sync();
+      const int ok = br->flag;
+      group_sync();
+      if (!ok) break;
+      umma::fence_after();
+      const int nmb = (D.np + 127) / 128;
+      for (int mb = 0; mb < nmb; mb++) {
+        const int n = mb * 128 + 32 * quad + lane;  // factor row of this thread
+        const uint32_t taddr = tbase + ((uint32_t)(32 * quad) << 16) + (uint32_t)(b * 128 + mb * EMT);
         uint32_t v[4][16];
 #pragma unroll
-        for (int q = 0; q < 4; q++) umma::ld_32x32b_x16_nowait(taddr + n0c + 16 * q, v[q]);
+        for (int c = 0; c < 4; c++) umma::ld_32x32b_x16_nowait(taddr + 16 * c, v[c]);
         umma::wait_ld();
-        if (lane < 16) {
+        if (n < D.nv) {
+          float* dst;
+          if (PH == 2) dst = M.gpart + ((int64_t)D.out0 + n) * EMT;
+          else if (D.ntile == 1) dst = M.z + ((int64_t)D.out0 + n) * EMT;
+          else dst = M.part + ((int64_t)D.poff + (int64_t)D.tile * D.nv + n) * EMT;
 #pragma unroll
-          for (int q = 0; q < 4; q++)
+          for (int c = 0; c < 4; c++)
 #pragma unroll
-            for (int i = 0; i < 16; i++) {
-              const int nn = n0c + 16 * q + i;
-              if (nn < Dc.nv) {
-                float* dst;
-                if (PH == 2) dst = M.gpart + ((int64_t)Dc.out0 + nn) * EMT;
-                else if (Dc.ntile == 1) dst = M.z + ((int64_t)Dc.out0 + nn) * EMT;
-                else dst = M.part + ((int64_t)Dc.poff + (int64_t)Dc.tile * Dc.nv + nn) * EMT;
-                dst[m] = __uint_as_float(v[q][i]);
-              }
-            }
+            for (int i = 0; i < 16; i += 4)
+              *reinterpret_cast<float4*>(dst + 16 * c + i) =
+                  make_float4(__uint_as_float(v[c][i]), __uint_as_float(v[c][i + 1]), __uint_as_float(v[c][i + 2]),
+                              __uint_as_float(v[c][i + 3]));
         }
+        __syncwarp();
+      }
+      umma::fence_before();
+      barrive(&br->acce[b]);
+      if (PH == 1 && D.ntile > 1) {
+        // the last tile of a column group to arrive sums the tiles in order
+        __threadfence();
+        group_sync();
+        if (et == 0) br->flag = arrive_ar(&M.cnt[D.cg]) == D.ntile - 1;
+        group_sync();
+        if (br->flag) {
+          for (int idx = et; idx < D.nv * EMT; idx += 128) {
+            const int col = idx / EMT, mm = idx % EMT;
+            float t = 0.f;
+            for (int q = 0; q < D.ntile; q++)
+              t += __ldcg(&M.part[((int64_t)D.poff + (int64_t)q * D.nv + col) * EMT + mm]);
+            M.z[((int64_t)D.out0 + col) * EMT + mm] = t;
+          }
+          if (et == 0) M.cnt[D.cg] = 0;
+        }
+        group_sync();
       }
     }
-    umma::fence_before();
-    if (PH == 1 && Dc.ntile > 1) {
-      __threadfence();
-      __syncthreads();
-      if (tid == 0) sh_last = arrive_ar(&M.cnt[Dc.cg]) == Dc.ntile - 1;
-      __syncthreads();
-      if (sh_last) {
-        for (int idx = tid; idx < Dc.nv * EMT; idx += blockDim.x) {
-          const int col = idx / EMT, mm = idx % EMT;
-          float t = 0.f;
-          for (int q = 0; q < Dc.ntile; q++)
-            t += __ldcg(&M.part[((int64_t)Dc.poff + (int64_t)q * Dc.nv + col) * EMT + mm]);
-          M.z[((int64_t)Dc.out0 + col) * EMT + mm] = t;
-        }
-        if (tid == 0) M.cnt[Dc.cg] = 0;
-      }
-    }
-    __syncthreads();
-    nitem++;
-    c_it += G;
-    c_k0 = 0;
-    Dc = desc(c_it);
-  }
-  if (failed) {
-    // record, then let outstanding copies and MMAs finish (bounded) before
-    // the tensor memory is released
-    if (tid == 0) {
-      if (A.err) atomicExch(A.err, 1);
-      for (int q = c_seq; q < p_seq; q++) bwait(&full[q & 1], (uint32_t)((q >> 1) & 1));
-      for (int q = max(0, c_seq - 2); q < c_seq; q++) bwait(&mmab[q & 1], (uint32_t)((q >> 1) & 1));
-    }
+    __syncwarp();
   }
   umma::fence_before();
   __syncthreads();
+  umma::fence_after();
   if (warp == 0) {
-    umma::tmem_dealloc(tbase, 256);
+    umma::tmem_dealloc(tbase, kTmemCols);
     umma::tmem_relinquish();
   }
 }
@@ -323,19 +399,19 @@ __global__ void tcconv_kernel(const double* __restrict__ body, const TcCopy* __r
 
 }  // namespace
 
-size_t tc_smem_bytes() { return 2 * (size_t)kStageT + 64; }
+size_t tc_smem_bytes() { return (size_t)NST * kStage + sizeof(Bars); }
 
 void tc_prepare() {
   cudaFuncSetAttribute(tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes());
   cudaFuncSetAttribute(tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_smem_bytes());
 }
 
-void launch_tc(int phase, const TcMat& a, const TcMat& b, int nmat, const float* x, int sm, cudaStream_t st) {
+// one block per SM of the schedule's grid (a.G)
+void launch_tc(int phase, const TcMat& a, const TcMat& b, int nmat, const float* x, cudaStream_t st) {
   const int n = phase == 1 ? a.n1 + (nmat == 2 ? b.n1 : 0) : a.n2 + (nmat == 2 ? b.n2 : 0);
-  if (n == 0) return;
-  const int grid = n < 2 * sm ? n : 2 * sm;
-  if (phase == 1) tc_kernel<1><<<grid, 128, tc_smem_bytes(), st>>>(a, b, nmat, x);
-  else tc_kernel<2><<<grid, 128, tc_smem_bytes(), st>>>(a, b, nmat, x);
+  if (n == 0 || a.G <= 0) return;
+  if (phase == 1) tc_kernel<1><<<a.G, kThreads, tc_smem_bytes(), st>>>(a, b, nmat, x);
+  else tc_kernel<2><<<a.G, kThreads, tc_smem_bytes(), st>>>(a, b, nmat, x);
 }
 
 void launch_tcconv(const double* body, const TcCopy* map, int64_t nmap, __nv_bfloat16* dst, cudaStream_t st) {

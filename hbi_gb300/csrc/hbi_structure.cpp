@@ -419,9 +419,11 @@ void plan_warp_schedule(const std::vector<int64_t>& cost, int nwarps, std::vecto
 
 void plan_tc(int n, const std::vector<Leaf>& leaves, const std::vector<int64_t>& body_off, TcPlan& tp) {
   const int nl = (int)leaves.size();
-  const int TR = 256;
+  const int TR = 256;  // phase 2: rows of a tile
   tp = TcPlan();
-  // ---- phase 1: column groups; K = rows of a tile, N = columns (<= 256 per item)
+  // ---- phase 1: column groups; K = rows of a tile (<= kTcK1), N = columns
+  // (<= 256 per item): long tiles keep a group's sum in tensor memory, and
+  // only groups taller than kTcK1 rows meet in partial sums
   std::vector<std::pair<std::pair<int, int>, int>> ck;
   for (int i = 0; i < nl; i++)
     if (leaves[i].ltmtx == 1 && leaves[i].kt > 0) ck.push_back({{leaves[i].nstrtt - 1, -leaves[i].ndt}, i});
@@ -439,19 +441,19 @@ void plan_tc(int n, const std::vector<Leaf>& leaves, const std::vector<int64_t>&
       for (int k = 0; k < leaves[ck[e].second].kt; k++) cols.push_back({ck[e].second, k});
     }
     const int ncols = (int)cols.size();
-    const int ntile = (ndt + TR - 1) / TR;
+    const int ntile = (ndt + kTcK1 - 1) / kTcK1;
     for (int c0 = 0; c0 < ncols; c0 += 256) {
       const int nv = std::min(256, ncols - c0);
       const int np = (nv + 7) / 8 * 8;
       const int64_t poff0 = poff;
       if (ntile > 1) poff += (int64_t)ntile * nv;
       for (int t = 0; t < ntile; t++) {
-        const int kv = std::min(TR, ndt - t * TR);
+        const int kv = std::min(kTcK1, ndt - t * kTcK1);
         const int kp = (kv + 15) / 16 * 16;
         TcItem it{};
         it.soff = off;
         it.np = np; it.kp = kp; it.nv = nv; it.kv = kv;
-        it.m0 = col0 + t * TR;
+        it.m0 = col0 + t * kTcK1;
         it.out0 = (int32_t)(z + c0);
         it.cg = (int32_t)ncg;
         it.tile = t; it.ntile = ntile;
@@ -461,7 +463,8 @@ void plan_tc(int n, const std::vector<Leaf>& leaves, const std::vector<int64_t>&
           const int li = cols[c0 + c].first, k = cols[c0 + c].second;
           const Leaf& L = leaves[li];
           // V(row, k) at body + row + k*ndt; run along K (the tile's rows)
-          tp.copy1.push_back(TcCopy{off, body_off[li] + (int64_t)k * L.ndt + (int64_t)t * TR, np, c, 0, 0, 1, kv, 1});
+          tp.copy1.push_back(
+              TcCopy{off, body_off[li] + (int64_t)k * L.ndt + (int64_t)t * kTcK1, np, c, 0, 0, 1, kv, 1});
         }
         off += (int64_t)kp * np * 2;
       }

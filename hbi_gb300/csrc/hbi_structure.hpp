@@ -136,10 +136,11 @@ void plan_warp_schedule(const std::vector<int64_t>& cost, int nwarps, std::vecto
 // Both contractions as D (64 members x N) = A (64 x K) * B^T with B (N x K)
 // from the factor store: phase 2 N = the rows of a row-group tile (<= 256),
 // K = the group's columns; phase 1 N = the columns of a column group (<= 256
-// per item), K = the rows of a tile (<= 256).  B is stored as BF16 hi + lo
+// per item), K = the rows of a tile (<= kTcK1).  B is stored as BF16 hi + lo
 // halves (x = hi + lo to ~16 bits) in the canonical no-swizzle K-major layout,
 // per 16-K chunk: [hi: 2 K-blocks x N/8 core matrices of 8 x 8][lo: same].
 // N is padded to 8 and K to 16 with zeros.
+constexpr int kTcK1 = 1024;  // rows of a phase-1 tile (K of one item)
 struct TcItem {
   int64_t soff;            // bf16 element offset of the item's first chunk
   int32_t np, kp;          // N padded to 8, K padded to 16

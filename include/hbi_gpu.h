@@ -422,6 +422,16 @@ int hbi_ens_get_state(hbi_ens* e, double* y, double* slip, double* x);
 int hbi_ens_use_tensor_cores(hbi_ens* e, const hbi_leafmtxp* lf_s, const hbi_leafmtxp* lf_n);
 /* every member from x = 0 to exactly t_limit (s) */
 int hbi_ens_run(hbi_ens* e, double eps_r, double dtinit, double dtmax, double t_limit, hbi_ens_status* st);
+/* One multi-vector product of both H-matrices (the kernels the run uses:
+ * tensor cores after hbi_ens_use_tensor_cores, else CUDA cores) applied to the
+ * 64 members' vectors x[i * 64 + m] (cluster order, FP32, host): ys = H_s x,
+ * yn = H_n x (yn unused with one matrix), same layout.  With reps > 0 the
+ * product (phase 1, phase 2, group sums) is repeated reps more times and *ms
+ * receives the CUDA-event time of one.  Overwrites the ensemble's product
+ * input buffer (the next attempt rewrites it from the state).  The
+ * counterpart of HACApK_adot_lattice_hyp (m_HACApK_solve.f90:220) for 64
+ * right-hand sides. */
+int hbi_ens_product(hbi_ens* e, const float* x, float* ys, float* yn, int reps, double* ms);
 
 /* Host-only self check of the tensor-core plan of the ensemble product (no
  * reference counterpart): y = H x through that plan with the factors rounded

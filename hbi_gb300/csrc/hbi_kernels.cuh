@@ -76,7 +76,8 @@ inline int num_shapes(int phase) { return phase == 1 ? kNumShapes1 : kNumShapes2
 // (pdl_wait_prior; transitively all earlier kernels of the stream).
 // pdl_launch_dependents lets the next grid start as soon as this grid's SMs
 // free up.  Both are no-ops in a grid launched without the attribute.
-// HBI_PDL=0 launches the chain without it.
+// Off by default (a Cash-Karp attempt on the 65,536-element Okada plane took
+// 1.559 ms with it, 1.423 ms without); HBI_PDL=1 turns it on.
 __device__ __forceinline__ void pdl_launch_dependents() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }

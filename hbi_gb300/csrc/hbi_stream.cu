@@ -850,7 +850,7 @@ bool pdl_enabled() {
   static int on = -1;
   if (on < 0) {
     const char* e = getenv("HBI_PDL");
-    on = (e && e[0] == '0') ? 0 : 1;
+    on = (e && e[0] == '1') ? 1 : 0;
   }
   return on == 1;
 }

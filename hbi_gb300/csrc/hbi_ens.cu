@@ -419,7 +419,7 @@ __global__ void __launch_bounds__(256, 2) p2e_kernel(EnsMat A, EnsMat B, int nma
 
 // per (row, member): the covering groups' partial rows, coarse to fine, from
 // the flat per-fine-range offset list (independent loads, eight in flight)
-__device__ __forceinline__ double group_sum_e(const EnsMat& M, int r, int m) {
+__device__ __forceinline__ float group_sum_raw(const EnsMat& M, int r, int m) {
   const MatDev& d = M.m;
   const int f = __ldg(&d.row_fc[r]);
   const int e0 = __ldg(&d.fcb_ptr[f]), e1 = __ldg(&d.fcb_ptr[f + 1]);
@@ -433,7 +433,11 @@ __device__ __forceinline__ double group_sum_e(const EnsMat& M, int r, int m) {
     for (int u = 0; u < 8; u++) s += v[u];
   }
   for (; e < e1; e++) s += __ldcg(&M.gpart[((int64_t)__ldg(&d.fcb_base[e]) + r) * EM + m]);
-  return (double)s * d.scale;
+  return s;
+}
+// ... times the operator's scale (the traction of the stage)
+__device__ __forceinline__ double group_sum_e(const EnsMat& M, int r, int m) {
+  return (double)group_sum_raw(M, r, m) * M.m.scale;
 }
 
 // ---------------------------------------------------------------- phase 3
@@ -617,8 +621,8 @@ __global__ void __launch_bounds__(256) ens_sum_kernel(EnsMat A, EnsMat B, int nm
   const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (idx >= (int64_t)n * EM) return;
   const int m = (int)(idx % EM), r = (int)(idx / EM);
-  ys[idx] = (float)group_sum_e(A, r, m);
-  if (nmat == 2) yn[idx] = (float)group_sum_e(B, r, m);
+  ys[idx] = group_sum_raw(A, r, m);
+  if (nmat == 2) yn[idx] = group_sum_raw(B, r, m);
 }
 
 }  // namespace

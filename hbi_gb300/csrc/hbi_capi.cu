@@ -839,7 +839,7 @@ static int construct_impl(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* c, int
   // fewer for small operators
   for (int ph = 1; ph <= 2; ph++)
     for (int sh = 0; sh < num_shapes(ph); sh++) {
-      const int nw = stream_shape(ph, sh).nw, sb = stream_shape(ph, sh).sb;
+      const int nw = schedule_units(ph, stream_shape(ph, sh)), sb = stream_shape(ph, sh).sb;
       const int ni = ph == 1 ? (int)P.p1.size() : (int)P.p2.size();
       if (ni == 0) continue;
       const int need = (ni + nw - 1) / nw;

@@ -52,15 +52,21 @@ def test_shape_table_fits_the_kernels():
         assert len(shapes) >= 3 and shapes[0] == (12, 2, 8192, 0)
         for nw, ns, sb, lane_map in shapes:
             assert 1 <= nw <= 32 and ns >= 2 and sb in (8192, 16384)
-            assert lane_map in (0, 1)
-            smem = nw * ns * sb + nw * 128 * 8 + nw * ns * 8
+            assert lane_map in ((0, 1, 2) if phase == 1 else (0, 1))
+            if lane_map == 2:
+                # shared ring: ns stages + 64-byte headers, a 1 KB x tile per
+                # consumer warp, three barriers per stage; a producer warp more
+                assert sb == 8192 and nw + 1 <= 32 and nw <= ns
+                smem = ns * sb + ns * 64 + nw * 1024 + 3 * ns * 8 + 16
+            else:
+                smem = nw * ns * sb + nw * 128 * 8 + nw * ns * 8
             assert smem <= 227 * 1024
             for esz in (2, 4, 8):
                 for ntp in range(16 // esz, 512 // esz + 1, 16 // esz):
                     cc = (sb // (ntp * esz)) // 16 * 16
                     cc = min(cc, 128)
                     assert 16 <= cc <= 128 and cc * ntp * esz <= sb
-    assert {m for *_, m in H.stream_shapes(1)} == {0, 1}
+    assert {m for *_, m in H.stream_shapes(1)} == {0, 1, 2}
 
 
 def _vswz(c, nv):

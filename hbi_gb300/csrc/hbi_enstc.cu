@@ -168,45 +168,85 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
     return PH == 1 ? (it < n0 ? A.p1[it] : B.p1[it - n0]) : (it < n0 ? A.p2[it] : B.p2[it - n0]);
   };
   auto stage = [&](int s) -> unsigned char* { return sm + s * kStage; };
+  // every role walks the block's items in order; item ids are loaded two
+  // items ahead and descriptors one, so that no role waits on a descriptor
+  // load at an item boundary
+  struct Walk {
+    int j, it, itn, itnn;
+    TcItem D, Dn;
+  };
+  auto walk_init = [&](Walk& w) {
+    w.j = 0;
+    w.it = nit > 0 ? item_at(0) : 0;
+    w.itn = nit > 1 ? item_at(1) : 0;
+    w.itnn = nit > 2 ? item_at(2) : 0;
+    w.D = nit > 0 ? desc(w.it) : TcItem{};
+    w.Dn = nit > 1 ? desc(w.itn) : TcItem{};
+  };
+  auto walk_next = [&](Walk& w) {
+    w.j++;
+    w.it = w.itn;
+    w.D = w.Dn;
+    w.itn = w.itnn;
+    w.Dn = w.j + 1 < nit ? desc(w.itn) : TcItem{};
+    w.itnn = w.j + 2 < nit ? item_at(w.j + 2) : 0;
+  };
 
   if (warp == 0) {
     // ---------------------------------------------------------- producer
-    int q = 0;
-    for (int j = 0; j < nit; j++) {
-      const int it = item_at(j);
-      const TcItem D = desc(it);
-      const TcMat& M = it < n0 ? A : B;
-      bool ok = true;
-      for (int k0 = 0; k0 < D.kp; k0 += KC, q++) {
-        const int s = q % NST;
-        int w = 1;
-        if (q >= NST && lane == 0) w = rwait(&br->empty[s], (uint32_t)((q / NST - 1) & 1), br, A.err);
-        if (!__shfl_sync(0xffffffffu, w, 0)) {
-          ok = false;
-          break;
-        }
-        const int kc = min(KC, D.kp - k0);
-        const int nrow = max(0, min(kc, D.kv - k0));  // member rows that carry data
-        unsigned char* stg = stage(s);
-        const uint32_t fbytes = (uint32_t)((kc / 16) * D.np * 64);
-        const __nv_bfloat16* fsrc = (PH == 1 ? M.s1 : M.s2) + D.soff + (int64_t)(k0 / 16) * D.np * 32;
-        int mi = 0;
-        if (PH == 2 && lane < nrow) mi = __ldg(&M.midx[D.m0 + k0 + lane]);
-        if (lane == 0) {
-          fasync();
-          bexpect(&br->full[s], fbytes + (uint32_t)(nrow * EMT * 4));
-          bcopy(stg, fsrc, fbytes, &br->full[s]);
-          if (PH == 1 && nrow > 0)
-            bcopy(stg + kFac, X + (int64_t)(D.m0 + k0) * EMT, (uint32_t)(nrow * EMT * 4), &br->full[s]);
-        }
-        __syncwarp();
-        if (PH == 2 && lane < nrow) {
+    Walk W;
+    walk_init(W);
+    int q = 0, k0 = 0;
+    // phase 2: this stage's column indices, loaded one stage ahead
+    auto load_midx = [&]() -> int {
+      const int nrow = max(0, min(KC, W.D.kv - k0));
+      const TcMat& M = W.it < n0 ? A : B;
+      return (PH == 2 && W.j < nit && lane < nrow) ? __ldg(&M.midx[W.D.m0 + k0 + lane]) : 0;
+    };
+    int mi = load_midx();
+    while (W.j < nit) {
+      const TcItem& D = W.D;
+      const TcMat& M = W.it < n0 ? A : B;
+      const int s = q % NST;
+      int w = 1;
+      if (q >= NST && lane == 0) w = rwait(&br->empty[s], (uint32_t)((q / NST - 1) & 1), br, A.err);
+      if (!__shfl_sync(0xffffffffu, w, 0)) break;
+      const int kc = min(KC, D.kp - k0);
+      const int nrow = max(0, min(kc, D.kv - k0));  // member rows that carry data
+      unsigned char* stg = stage(s);
+      const uint32_t fbytes = (uint32_t)((kc / 16) * D.np * 64);
+      const __nv_bfloat16* fsrc = (PH == 1 ? M.s1 : M.s2) + D.soff + (int64_t)(k0 / 16) * D.np * 32;
+      if (lane == 0) {
+        fasync();
+        bexpect(&br->full[s], fbytes + (uint32_t)(nrow * EMT * 4));
+        bcopy(stg, fsrc, fbytes, &br->full[s]);
+        if (PH == 1 && nrow > 0)
+          bcopy(stg + kFac, X + (int64_t)(D.m0 + k0) * EMT, (uint32_t)(nrow * EMT * 4), &br->full[s]);
+      }
+      __syncwarp();
+      if (PH == 2) {
+        // runs of consecutive multiplier rows (a low-rank leaf's z columns,
+        // a dense leaf's x rows) go in one copy, issued by the run's first lane
+        const int prev = __shfl_up_sync(0xffffffffu, mi, 1);
+        const bool cont = lane > 0 && lane < nrow &&
+                          ((mi >= 0 && prev >= 0 && mi == prev + 1) || (mi < 0 && prev < 0 && mi == prev - 1));
+        const bool head = lane < nrow && !cont;
+        const unsigned heads = __ballot_sync(0xffffffffu, head);
+        if (head) {
+          const unsigned above = heads & ~((2u << lane) - 1u);
+          const int len = (above ? __ffs(above) - 1 : nrow) - lane;
           const float* src = mi >= 0 ? M.z + (int64_t)mi * EMT : X + (int64_t)(-mi - 1) * EMT;
           fasync();
-          bcopy(stg + kFac + lane * EMT * 4, src, EMT * 4, &br->full[s]);
+          bcopy(stg + kFac + lane * EMT * 4, src, (uint32_t)(len * EMT * 4), &br->full[s]);
         }
       }
-      if (!ok) break;
+      q++;
+      k0 += KC;
+      if (k0 >= D.kp) {
+        k0 = 0;
+        walk_next(W);
+      }
+      mi = load_midx();
     }
     // the copies still in flight land before the block leaves (the last NST
     // issued are the only ones whose phase can still be open)
@@ -217,9 +257,12 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
     // --------------------------------------------------------------- MMA
     const uint32_t idesc = umma::idesc_bf16_f32(128, EMT);
     int q = 0;
-    for (int j = 0; j < nit; j++) {
+    Walk W;
+    walk_init(W);
+    for (; W.j < nit; walk_next(W)) {
+      const int j = W.j;
       const int b = j & 1;
-      const TcItem D = desc(item_at(j));
+      const TcItem& D = W.D;
       int w = 1;
       if (j >= 2 && lane == 0) w = rwait(&br->acce[b], (uint32_t)((j / 2 - 1) & 1), br, A.err);
       if (!__shfl_sync(0xffffffffu, w, 0)) break;
@@ -269,8 +312,10 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
     const int ct = tid - 64;
     int q = 0;
     bool ok = true;
-    for (int j = 0; j < nit && ok; j++) {
-      const TcItem D = desc(item_at(j));
+    Walk W;
+    walk_init(W);
+    for (; W.j < nit && ok; walk_next(W)) {
+      const TcItem& D = W.D;
       for (int k0 = 0; k0 < D.kp; k0 += KC, q++) {
         const int s = q % NST;
         if (!rwait(&br->full[s], (uint32_t)((q / NST) & 1), br, A.err)) {
@@ -309,11 +354,13 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
   } else {
     // ---------------------------------------------------------- epilogue
     const int et = tid - 192, quad = warp & 3;
-    for (int j = 0; j < nit; j++) {
+    Walk W;
+    walk_init(W);
+    for (; W.j < nit; walk_next(W)) {
+      const int j = W.j;
       const int b = j & 1;
-      const int it = item_at(j);
-      const TcItem D = desc(it);
-      const TcMat& M = it < n0 ? A : B;
+      const TcItem& D = W.D;
+      const TcMat& M = W.it < n0 ? A : B;
       if (et == 0) br->flag = rwait(&br->accf[b], (uint32_t)((j / 2) & 1), br, A.err) ? 1 : 0;
       group_sync();
       const int ok = br->flag;

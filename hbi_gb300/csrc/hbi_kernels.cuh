@@ -53,7 +53,7 @@ constexpr long long kWaitCyclesDefault = 2LL << 30;
 // phase 1 the lane mapping (0: the lanes of a column segment split its rows
 // and reduce by shuffles; 1: one lane per column, no cross-lane reduction;
 // 2: as 1, the block's consumer warps fed from one shared ring of `ns`
-// stages by a producer warp -- p1_ring_kernel -- with `nw` consumer warps),
+// stages by producer warps -- p1_ring_kernel -- with `nw` consumer warps),
 // for phase 2 how far ahead the multipliers are gathered (0: one chunk, 1:
 // two).  Every shape is compiled for every storage type; hbi_construct_lh
 // times them on the operator and keeps the fastest per phase
@@ -64,7 +64,7 @@ struct StreamShape {
 constexpr int kNumShapes1 = 9, kNumShapes2 = 5, kMaxShapes = 9;
 constexpr StreamShape kShapes1[kNumShapes1] = {{12, 2, 8192, 0}, {8, 3, 8192, 0}, {6, 2, 16384, 0},
                                                {12, 2, 8192, 1}, {8, 3, 8192, 1}, {6, 2, 16384, 1},
-                                               {15, 24, 8192, 2}, {11, 24, 8192, 2}, {23, 24, 8192, 2}};
+                                               {16, 24, 8192, 2}, {12, 24, 8192, 2}, {20, 24, 8192, 2}};
 // work units of a block in a shape's static schedule: one per warp, one per
 // block for the shared-ring shapes (the producer walks the block's items)
 inline int schedule_units(int phase, const StreamShape& S) { return phase == 1 && S.map == 2 ? 1 : S.nw; }

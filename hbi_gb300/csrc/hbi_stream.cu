@@ -519,10 +519,12 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
 }
 
 // ------------------------------------------------------ phase 1, shared ring
-// The block's shared memory is one ring of R stages of 8 KB, filled by a
-// producer warp (warp 0) and consumed by NCW consumer warps in turn: stage
-// sequence number q lands in slot q mod R and is consumed by warp
-// 1 + q mod NCW.  More warps then work on the stages than a warp-private
+// The block's shared memory is one ring of R stages of 8 KB, filled by
+// kRingProducers producer warps (stage sequence number q by producer
+// q mod kRingProducers: issuing a stage's bulk copy costs a warp hundreds of
+// cycles, more than one SM's share of HBM bandwidth leaves per 8 KB) and
+// consumed by NCW consumer warps in turn: stage q lands in slot q mod R and
+// is consumed by consumer q mod NCW.  More warps then work on the stages than a warp-private
 // ring of the same memory would allow, and the consumers keep no item
 // bookkeeping: the producer walks the block's items (its static schedule),
 // and publishes each stage's descriptor in a header (its own barrier) before
@@ -533,7 +535,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
 // partials in tile order, resolved after the consumer's next stage so that
 // the atomic's round trip overlaps it.  After the block's last stage the
 // producer publishes one stop header per consumer.
-struct RingHdr {
+struct alignas(16) RingHdr {
   int32_t sec;         // matrix of the item (0: m0, 1: m1); -1: stop
   int32_t c0, nc, cc;  // first column of the stage in the item, its columns, the item's chunk width
   int32_t ntp, nt, x0, z0;
@@ -541,6 +543,8 @@ struct RingHdr {
   int32_t ncols, pad0, pad1, pad2;
 };
 static_assert(sizeof(RingHdr) == 64, "one 64-byte header per stage");
+
+constexpr int kRingProducers = 4;
 
 template <int NCW, int R>
 constexpr size_t ring_smem_bytes() {
@@ -580,7 +584,7 @@ __device__ __forceinline__ int atom_add_acq_rel(int* p, int v) {
 }
 
 template <typename T, int NCW, int R>
-__global__ void __launch_bounds__((NCW + 1) * 32, 1) p1_ring_kernel(MatDev m0, MatDev m1, int nmat,
+__global__ void __launch_bounds__((NCW + kRingProducers) * 32, 1) p1_ring_kernel(MatDev m0, MatDev m1, int nmat,
                                                                     const double* __restrict__ x, int shape) {
   typedef typename AccT<T>::type Acc;
   constexpr int VEC = 16 / sizeof(T);
@@ -606,8 +610,10 @@ __global__ void __launch_bounds__((NCW + 1) * 32, 1) p1_ring_kernel(MatDev m0, M
   }
   __syncthreads();
   const int n0 = m0.ns1, ntot = nmat == 2 ? n0 + m1.ns1 : n0;
-  if (warp == 0) {
-    // ------------------------------------------------------------ producer
+  if (warp < kRingProducers) {
+    // ----------------------------------------------------------- producers
+    // every producer walks the block's whole stage sequence and issues its
+    // own share (q mod kRingProducers == warp)
     const WarpSeq seq = warp_seq(m0, m1, nmat, 1, shape, blockIdx.x, gridDim.x, n0, ntot);
     auto desc = [&](int it) -> S1ItemDev {
       S1ItemDev d{};
@@ -636,6 +642,7 @@ __global__ void __launch_bounds__((NCW + 1) * 32, 1) p1_ring_kernel(MatDev m0, M
         const int cc = chunk_cols(D.ntp, ESZ, SB);
         const T* vsrc = (const T*)M.vstore + D.soff;
         for (int c0 = 0; c0 < D.ncols; c0 += cc, q++) {
+          if (q % kRingProducers != warp) continue;
           if (!claim(M)) {
             ok = false;
             break;
@@ -643,20 +650,11 @@ __global__ void __launch_bounds__((NCW + 1) * 32, 1) p1_ring_kernel(MatDev m0, M
           const int s = q % R;
           const int nc = min(cc, D.ncols - c0);
           if (lane == 0) {
-            RingHdr& h = hdr[s];
-            h.sec = sec;
-            h.c0 = c0;
-            h.nc = nc;
-            h.cc = cc;
-            h.ntp = D.ntp;
-            h.nt = D.nt;
-            h.x0 = D.x0;
-            h.z0 = D.z0;
-            h.cg = D.cg;
-            h.tile = D.tile;
-            h.ntile = D.ntile;
-            h.poff = D.poff;
-            h.ncols = D.ncols;
+            int4* h = reinterpret_cast<int4*>(&hdr[s]);
+            h[0] = make_int4(sec, c0, nc, cc);
+            h[1] = make_int4(D.ntp, D.nt, D.x0, D.z0);
+            h[2] = make_int4(D.cg, D.tile, D.ntile, D.poff);
+            h[3] = make_int4(D.ncols, 0, 0, 0);
             mbar_arrive(&hrdy[s]);  // release: the header before the flag
             const uint32_t bytes = (uint32_t)(nc * D.ntp * ESZ);
             fence_proxy_async();
@@ -672,6 +670,7 @@ __global__ void __launch_bounds__((NCW + 1) * 32, 1) p1_ring_kernel(MatDev m0, M
     }
     // one stop header per consumer
     for (int w = 0; w < NCW && ok; w++, q++) {
+      if (q % kRingProducers != warp) continue;
       if (!claim(m0)) {
         ok = false;
         break;
@@ -687,12 +686,13 @@ __global__ void __launch_bounds__((NCW + 1) * 32, 1) p1_ring_kernel(MatDev m0, M
     // copies still in flight land before the block leaves (only the last R
     // stages' phases can still be open)
     if (lane == 0)
-      for (int r = max(0, q - R); r < q; r++) mbar_wait_bounded(&full[r % R], (uint32_t)((r / R) & 1));
+      for (int r = max(0, q - R); r < q; r++)
+        if (r % kRingProducers == warp) mbar_wait_bounded(&full[r % R], (uint32_t)((r / R) & 1));
     __syncwarp();
     return;
   }
   // -------------------------------------------------------------- consumers
-  const int cw = warp - 1;
+  const int cw = warp - kRingProducers;
   Acc* xs = reinterpret_cast<Acc*>(xbase + (size_t)cw * 1024);
   int pend_old = 0, pend_add = 0, pend_cg = -1, pend_ntile = 0, pend_ncols = 0, pend_poff = 0, pend_z0 = 0,
       pend_sec = 0;
@@ -1032,7 +1032,8 @@ void launch_p1r(const MatDev& m0, const MatDev& m1, int nmat, const double* x, i
   static_assert(kShapes1[S].map == 2 && kShapes1[S].sb == 8192, "a shared-ring shape");
   // one block per SM; the static schedule has one unit per block
   const int grid = n < sm ? n : sm;
-  launch_kernel(p1_ring_kernel<T, NCW, R>, dim3(grid), dim3((NCW + 1) * 32), ring_smem_bytes<NCW, R>(), st, false,
+  launch_kernel(p1_ring_kernel<T, NCW, R>, dim3(grid), dim3((NCW + kRingProducers) * 32), ring_smem_bytes<NCW, R>(),
+                st, false,
                 m0, m1, nmat, x, S);
 }
 

@@ -55,8 +55,8 @@ def test_shape_table_fits_the_kernels():
             assert lane_map in ((0, 1, 2) if phase == 1 else (0, 1))
             if lane_map == 2:
                 # shared ring: ns stages + 64-byte headers, a 1 KB x tile per
-                # consumer warp, three barriers per stage; a producer warp more
-                assert sb == 8192 and nw + 1 <= 32 and nw <= ns
+                # consumer warp, three barriers per stage; four producer warps more
+                assert sb == 8192 and nw + 4 <= 32 and nw <= ns
                 smem = ns * sb + ns * 64 + nw * 1024 + 3 * ns * 8 + 16
             else:
                 smem = nw * ns * sb + nw * 128 * 8 + nw * ns * 8

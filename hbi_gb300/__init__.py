@@ -44,7 +44,7 @@ EXPORTS = [
     "hbi_mlp_train", "hbi_mlp_predict", "hbi_plan_emulate", "hbi_umma_probe",
     "hbi_ens_create", "hbi_ens_free", "hbi_ens_set_state", "hbi_ens_get_state", "hbi_ens_run",
     "hbi_tc_plan_emulate", "hbi_ens_use_tensor_cores", "hbi_ens_product", "hbi_cycle_restart", "hbi_restart_point",
-    "hbi_plan_warp_schedule", "hbi_lh_check_error", "hbi_lh_set_wait_limit", "hbi_rk_check_error",
+    "hbi_plan_warp_schedule", "hbi_plan_block_schedule", "hbi_lh_check_error", "hbi_lh_set_wait_limit", "hbi_rk_check_error",
     "hbi_stream_shapes", "hbi_lh_tuning", "hbi_autotune_select", "hbi_lh_set_shapes",
     "hbi_partition_leaves", "hbi_construct_lh_part", "hbi_mlp_set_loss",
 ]
@@ -284,8 +284,8 @@ class LHp:
         us = np.zeros(len(sh1) + len(sh2), dtype=np.float32)
         _check(lib().hbi_lh_tuning(self.h, C.byref(s1), C.byref(s2), us.ctypes.data_as(C.POINTER(C.c_float)),
                                    C.byref(src)), "hbi_lh_tuning")
-        name = lambda t: ("%dw x %d x %d KB%s" % (t[0], t[1], t[2] // 1024, " col" if t[3] else "") if t[3] < 2 else
-                          "ring %d x %d KB, %d consumers" % (t[1], t[2] // 1024, t[0]))
+        name = lambda t: "%dw x %d x %d KB%s%s" % (t[0], t[1], t[2] // 1024, " col" if t[3] else "",
+                                                 " blocks" if t[4] else "")
         return {"phase1": name(sh1[s1.value]), "phase2": name(sh2[s2.value]), "shape1": s1.value,
                 "shape2": s2.value, "source": {0: "timed", 1: "reused", 2: "forced"}.get(src.value, "?"),
                 "phase1_us": {name(t): round(float(us[i]), 2) for i, t in enumerate(sh1)},
@@ -628,12 +628,25 @@ class MLP:
 
 def stream_shapes(phase=1):
     """The compiled launch shapes of the phase-1 or phase-2 product kernel:
-    [(warps per block, stages per warp, stage bytes, lane mapping), ...]."""
+    [(warps per block, stages per warp, stage bytes, variant, schedule), ...]."""
     k = C.c_int()
     _check(lib().hbi_stream_shapes(int(phase), C.byref(k), None), "hbi_stream_shapes")
-    a = np.zeros(4 * k.value, dtype=np.int32)
+    a = np.zeros(5 * k.value, dtype=np.int32)
     _check(lib().hbi_stream_shapes(int(phase), C.byref(k), a.ctypes.data_as(_ip)), "hbi_stream_shapes")
-    return [tuple(int(v) for v in a[4 * s:4 * s + 4]) for s in range(k.value)]
+    return [tuple(int(v) for v in a[5 * s:5 * s + 5]) for s in range(k.value)]
+
+
+def plan_block_schedule(cost, key, nblocks, nw):
+    """The block schedule with locality (hbi_plan_block_schedule): returns
+    (woff[nblocks * nw + 1], witem[n])."""
+    cost = np.ascontiguousarray(cost, dtype=np.int64)
+    key = np.ascontiguousarray(key, dtype=np.int64)
+    woff = np.zeros(nblocks * nw + 1, dtype=np.int32)
+    witem = np.zeros(max(len(cost), 1), dtype=np.int32)
+    _check(lib().hbi_plan_block_schedule(len(cost), cost.ctypes.data_as(_i64p), key.ctypes.data_as(_i64p),
+                                         int(nblocks), int(nw), woff.ctypes.data_as(_ip), witem.ctypes.data_as(_ip)),
+           "hbi_plan_block_schedule")
+    return woff, witem[:len(cost)]
 
 
 def autotune_select(times):

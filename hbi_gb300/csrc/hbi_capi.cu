@@ -694,17 +694,30 @@ extern "C" int hbi_lh_set_shapes(hbi_lhp* h, int shape1, int shape2) {
   return HBI_OK;
 }
 
-extern "C" int hbi_stream_shapes(int phase, int* count, int* shapes4) {
+extern "C" int hbi_stream_shapes(int phase, int* count, int* shapes5) {
   if (!count || (phase != 1 && phase != 2)) return fail(HBI_ERR_ARG, "hbi_stream_shapes: bad arguments");
   *count = num_shapes(phase);
-  if (shapes4)
+  if (shapes5)
     for (int sh = 0; sh < num_shapes(phase); sh++) {
       const StreamShape& S = stream_shape(phase, sh);
-      shapes4[4 * sh] = S.nw;
-      shapes4[4 * sh + 1] = S.ns;
-      shapes4[4 * sh + 2] = S.sb;
-      shapes4[4 * sh + 3] = S.map;
+      shapes5[5 * sh] = S.nw;
+      shapes5[5 * sh + 1] = S.ns;
+      shapes5[5 * sh + 2] = S.sb;
+      shapes5[5 * sh + 3] = S.map;
+      shapes5[5 * sh + 4] = S.sched;
     }
+  return HBI_OK;
+}
+
+extern "C" int hbi_plan_block_schedule(int n, const int64_t* cost, const int64_t* key, int nblocks, int nw,
+                                       int32_t* woff, int32_t* witem) {
+  if (n < 0 || nblocks < 1 || nw < 1 || (n > 0 && (!cost || !key || !witem)) || !woff)
+    return fail(HBI_ERR_ARG, "hbi_plan_block_schedule: bad arguments");
+  std::vector<int64_t> c(cost, cost + n), k(key, key + n);
+  std::vector<int32_t> o, it;
+  plan_block_schedule(c, k, nblocks, nw, o, it);
+  std::copy(o.begin(), o.end(), woff);
+  std::copy(it.begin(), it.end(), witem);
   return HBI_OK;
 }
 
@@ -839,20 +852,24 @@ static int construct_impl(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* c, int
   // fewer for small operators
   for (int ph = 1; ph <= 2; ph++)
     for (int sh = 0; sh < num_shapes(ph); sh++) {
-      const int nw = schedule_units(ph, stream_shape(ph, sh)), sb = stream_shape(ph, sh).sb;
+      const StreamShape& S = stream_shape(ph, sh);
+      const int nw = S.nw, sb = S.sb;
       const int ni = ph == 1 ? (int)P.p1.size() : (int)P.p2.size();
       if (ni == 0) continue;
       const int need = (ni + nw - 1) / nw;
-      const int gw = (need < c->sm_count ? need : c->sm_count) * nw;
-      std::vector<int64_t> cost(ni);
+      const int nblk = need < c->sm_count ? need : c->sm_count;
+      const int gw = nblk * nw;
+      std::vector<int64_t> cost(ni), key(ni);
       for (int i = 0; i < ni; i++) {
         const int ncols = ph == 1 ? P.p1[i].ncols : P.p2[i].ncols, ntp = ph == 1 ? P.p1[i].ntp : P.p2[i].ntp;
         const int cc = chunk_cols(ntp, esz, sb);
         // bytes streamed plus ~1 KB worth of fixed cost per chunk
         cost[i] = (int64_t)ncols * ntp * esz + 1024 * (int64_t)((ncols + cc - 1) / cc);
+        key[i] = ph == 1 ? P.p1[i].soff : P.p2[i].soff;
       }
       std::vector<int32_t> woff, witem;
-      plan_warp_schedule(cost, gw, woff, witem);
+      if (S.sched == 1) plan_block_schedule(cost, key, nblk, nw, woff, witem);
+      else plan_warp_schedule(cost, gw, woff, witem);
       if (ph == 1) {
         CK(upload(&h->d_w1off[sh], woff, st));
         CK(upload(&h->d_w1item[sh], witem, st));

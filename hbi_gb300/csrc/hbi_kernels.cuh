@@ -49,27 +49,24 @@ enum { ST_F64 = 0, ST_F32 = 1, ST_BF16 = 2 };
 constexpr long long kWaitCyclesDefault = 2LL << 30;
 
 // Launch shapes of the phase kernels: warps per block (one block per SM),
-// shared-memory stages per warp and bytes per stage, and a variant: for
-// phase 1 the lane mapping (0: the lanes of a column segment split its rows
-// and reduce by shuffles; 1: one lane per column, no cross-lane reduction;
-// 2: as 1, the block's consumer warps fed from one shared ring of `ns`
-// stages by producer warps -- p1_ring_kernel -- with `nw` consumer warps),
-// for phase 2 how far ahead the multipliers are gathered (0: one chunk, 1:
-// two).  Every shape is compiled for every storage type; hbi_construct_lh
-// times them on the operator and keeps the fastest per phase
-// (autotune_stream_shapes).  Shape 0 of each phase is the default.
+// shared-memory stages per warp and bytes per stage, a variant -- for phase
+// 1 the lane mapping (0: the lanes of a column segment split its rows and
+// reduce by shuffles; 1: one lane per column, no cross-lane reduction), for
+// phase 2 how far ahead the multipliers are gathered (0: one chunk, 1: two)
+// -- and the static schedule (0: the phase's items dealt over all warps
+// longest first; 1: each block a run of items consecutive in the store,
+// plan_block_schedule).  Every shape is compiled for every storage type;
+// hbi_construct_lh times them on the operator and keeps the fastest per
+// phase (autotune_stream_shapes).  Shape 0 of each phase is the default.
 struct StreamShape {
-  int nw, ns, sb, map;
+  int nw, ns, sb, map, sched;
 };
-constexpr int kNumShapes1 = 9, kNumShapes2 = 5, kMaxShapes = 9;
-constexpr StreamShape kShapes1[kNumShapes1] = {{12, 2, 8192, 0}, {8, 3, 8192, 0}, {6, 2, 16384, 0},
-                                               {12, 2, 8192, 1}, {8, 3, 8192, 1}, {6, 2, 16384, 1},
-                                               {16, 24, 8192, 2}, {12, 24, 8192, 2}, {20, 24, 8192, 2}};
-// work units of a block in a shape's static schedule: one per warp, one per
-// block for the shared-ring shapes (the producer walks the block's items)
-inline int schedule_units(int phase, const StreamShape& S) { return phase == 1 && S.map == 2 ? 1 : S.nw; }
-constexpr StreamShape kShapes2[kNumShapes2] = {{12, 2, 8192, 0}, {8, 3, 8192, 0}, {6, 2, 16384, 0},
-                                               {10, 2, 8192, 0}, {8, 3, 8192, 1}};
+constexpr int kNumShapes1 = 8, kNumShapes2 = 6, kMaxShapes = 8;
+constexpr StreamShape kShapes1[kNumShapes1] = {{12, 2, 8192, 0, 0}, {8, 3, 8192, 0, 0}, {6, 2, 16384, 0, 0},
+                                               {12, 2, 8192, 1, 0}, {8, 3, 8192, 1, 0}, {6, 2, 16384, 1, 0},
+                                               {12, 2, 8192, 1, 1}, {12, 2, 8192, 0, 1}};
+constexpr StreamShape kShapes2[kNumShapes2] = {{12, 2, 8192, 0, 0}, {8, 3, 8192, 0, 0}, {6, 2, 16384, 0, 0},
+                                               {10, 2, 8192, 0, 0}, {8, 3, 8192, 1, 0}, {12, 2, 8192, 0, 1}};
 inline const StreamShape& stream_shape(int phase, int s) { return phase == 1 ? kShapes1[s] : kShapes2[s]; }
 inline int num_shapes(int phase) { return phase == 1 ? kNumShapes1 : kNumShapes2; }
 

@@ -518,244 +518,6 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
   resolve();
 }
 
-// ------------------------------------------------------ phase 1, shared ring
-// The block's shared memory is one ring of R stages of 8 KB, filled by
-// kRingProducers producer warps (stage sequence number q by producer
-// q mod kRingProducers: issuing a stage's bulk copy costs a warp hundreds of
-// cycles, more than one SM's share of HBM bandwidth leaves per 8 KB) and
-// consumed by NCW consumer warps in turn: stage q lands in slot q mod R and
-// is consumed by consumer q mod NCW.  More warps then work on the stages than a warp-private
-// ring of the same memory would allow, and the consumers keep no item
-// bookkeeping: the producer walks the block's items (its static schedule),
-// and publishes each stage's descriptor in a header (its own barrier) before
-// the data, so that a consumer loads the stage's x rows while the copy is in
-// flight.  Column sums as the lane-per-column mapping of p1_stream_kernel.
-// A column group of several row tiles counts its finished columns
-// (ncols x ntile in all); the stage that completes it sums the tiles'
-// partials in tile order, resolved after the consumer's next stage so that
-// the atomic's round trip overlaps it.  After the block's last stage the
-// producer publishes one stop header per consumer.
-struct alignas(16) RingHdr {
-  int32_t sec;         // matrix of the item (0: m0, 1: m1); -1: stop
-  int32_t c0, nc, cc;  // first column of the stage in the item, its columns, the item's chunk width
-  int32_t ntp, nt, x0, z0;
-  int32_t cg, tile, ntile, poff;
-  int32_t ncols, pad0, pad1, pad2;
-};
-static_assert(sizeof(RingHdr) == 64, "one 64-byte header per stage");
-
-constexpr int kRingProducers = 4;
-
-template <int NCW, int R>
-constexpr size_t ring_smem_bytes() {
-  return (size_t)R * 8192 + (size_t)R * sizeof(RingHdr) + (size_t)NCW * 1024 + (size_t)3 * R * 8 + 16;
-}
-
-// bounded wait of a ring role; all lanes poll (the loop stays converged).
-// Gives up when another warp of the block did (abort flag) or after `limit`
-// cycles (0: before the first probe), records the error and raises the flag.
-__device__ __forceinline__ bool ring_wait(uint64_t* bar, uint32_t parity, int* err, long long limit, int* abort_flag) {
-  bool ok = limit > 0 && mbar_try_wait(bar, parity);
-  if (!ok && limit > 0) {
-    const long long t0 = clock64();
-    while (!(ok = mbar_try_wait(bar, parity))) {
-      if (*(volatile int*)abort_flag) break;
-      if (clock64() - t0 > limit) break;
-    }
-  }
-  if (!__all_sync(0xffffffffu, ok)) {
-    if ((threadIdx.x & 31) == 0) {
-      if (err) atomicExch(err, 1);
-      *(volatile int*)abort_flag = 1;
-    }
-    return false;
-  }
-  return true;
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(saddr(bar)) : "memory");
-}
-
-__device__ __forceinline__ int atom_add_acq_rel(int* p, int v) {
-  int old;
-  asm volatile("atom.add.acq_rel.gpu.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
-  return old;
-}
-
-template <typename T, int NCW, int R>
-__global__ void __launch_bounds__((NCW + kRingProducers) * 32, 1) p1_ring_kernel(MatDev m0, MatDev m1, int nmat,
-                                                                    const double* __restrict__ x, int shape) {
-  typedef typename AccT<T>::type Acc;
-  constexpr int VEC = 16 / sizeof(T);
-  constexpr int ESZ = sizeof(T);
-  constexpr int SB = 8192;
-  static_assert(32 * VEC * sizeof(Acc) <= 1024, "a consumer's x tile fits its 1 KB buffer");
-  extern __shared__ __align__(128) unsigned char smem[];
-  RingHdr* hdr = reinterpret_cast<RingHdr*>(smem + (size_t)R * SB);
-  unsigned char* xbase = smem + (size_t)R * SB + (size_t)R * sizeof(RingHdr);
-  uint64_t* full = reinterpret_cast<uint64_t*>(xbase + (size_t)NCW * 1024);
-  uint64_t* hrdy = full + R;
-  uint64_t* empty = hrdy + R;
-  int* abort_flag = reinterpret_cast<int*>(empty + R);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < R; s++) {
-      mbar_init(&full[s], 1);
-      mbar_init(&hrdy[s], 1);
-      mbar_init(&empty[s], 1);
-    }
-    *abort_flag = 0;
-    fence_mbar_init();
-  }
-  __syncthreads();
-  const int n0 = m0.ns1, ntot = nmat == 2 ? n0 + m1.ns1 : n0;
-  if (warp < kRingProducers) {
-    // ----------------------------------------------------------- producers
-    // every producer walks the block's whole stage sequence and issues its
-    // own share (q mod kRingProducers == warp)
-    const WarpSeq seq = warp_seq(m0, m1, nmat, 1, shape, blockIdx.x, gridDim.x, n0, ntot);
-    auto desc = [&](int it) -> S1ItemDev {
-      S1ItemDev d{};
-      if (it < ntot) d = it < n0 ? m0.s1[it] : m1.s1[it - n0];
-      return d;
-    };
-    int q = 0;
-    bool ok = true;
-    // slot of stage q free: the stage R earlier in it was consumed
-    auto claim = [&](const MatDev& M) -> bool {
-      if (q < R) return true;
-      return ring_wait(&empty[q % R], (uint32_t)((q / R - 1) & 1), M.err, M.wait, abort_flag);
-    };
-    const bool halted = m0.skip && __ldcg(m0.skip);
-    if (!halted) {
-      // item ids one item ahead of their descriptors, descriptors one item
-      // ahead of their use
-      int it = seq.at(0), itn = seq.at(1), k = 0;
-      S1ItemDev Dn = desc(it);
-      while (it < ntot && ok) {
-        const S1ItemDev D = Dn;
-        const int sec = it >= n0 ? 1 : 0;
-        const MatDev& M = sec ? m1 : m0;
-        const int itnn = seq.at(k + 2);
-        Dn = desc(itn);
-        const int cc = chunk_cols(D.ntp, ESZ, SB);
-        const T* vsrc = (const T*)M.vstore + D.soff;
-        for (int c0 = 0; c0 < D.ncols; c0 += cc, q++) {
-          if (q % kRingProducers != warp) continue;
-          if (!claim(M)) {
-            ok = false;
-            break;
-          }
-          const int s = q % R;
-          const int nc = min(cc, D.ncols - c0);
-          if (lane == 0) {
-            int4* h = reinterpret_cast<int4*>(&hdr[s]);
-            h[0] = make_int4(sec, c0, nc, cc);
-            h[1] = make_int4(D.ntp, D.nt, D.x0, D.z0);
-            h[2] = make_int4(D.cg, D.tile, D.ntile, D.poff);
-            h[3] = make_int4(D.ncols, 0, 0, 0);
-            mbar_arrive(&hrdy[s]);  // release: the header before the flag
-            const uint32_t bytes = (uint32_t)(nc * D.ntp * ESZ);
-            fence_proxy_async();
-            mbar_expect_tx(&full[s], bytes);
-            bulk_g2s(smem + (size_t)s * SB, vsrc + (int64_t)c0 * D.ntp, bytes, &full[s]);
-          }
-          __syncwarp();
-        }
-        it = itn;
-        itn = itnn;
-        k++;
-      }
-    }
-    // one stop header per consumer
-    for (int w = 0; w < NCW && ok; w++, q++) {
-      if (q % kRingProducers != warp) continue;
-      if (!claim(m0)) {
-        ok = false;
-        break;
-      }
-      const int s = q % R;
-      if (lane == 0) {
-        hdr[s].sec = -1;
-        mbar_arrive(&hrdy[s]);
-        mbar_arrive(&full[s]);
-      }
-      __syncwarp();
-    }
-    // copies still in flight land before the block leaves (only the last R
-    // stages' phases can still be open)
-    if (lane == 0)
-      for (int r = max(0, q - R); r < q; r++)
-        if (r % kRingProducers == warp) mbar_wait_bounded(&full[r % R], (uint32_t)((r / R) & 1));
-    __syncwarp();
-    return;
-  }
-  // -------------------------------------------------------------- consumers
-  const int cw = warp - kRingProducers;
-  Acc* xs = reinterpret_cast<Acc*>(xbase + (size_t)cw * 1024);
-  int pend_old = 0, pend_add = 0, pend_cg = -1, pend_ntile = 0, pend_ncols = 0, pend_poff = 0, pend_z0 = 0,
-      pend_sec = 0;
-  auto resolve = [&]() {
-    if (pend_cg < 0) return;
-    const int last = __shfl_sync(0xffffffffu, pend_old + pend_add == pend_ncols * pend_ntile ? 1 : 0, 0);
-    if (last) {
-      __syncwarp();  // lane 0's acquire orders the reads of every lane
-      const MatDev& PM = pend_sec ? m1 : m0;
-      Acc* z = (Acc*)PM.z;
-      const Acc* part = (const Acc*)PM.part;
-      for (int col = lane; col < pend_ncols; col += 32) {
-        Acc t = 0;
-        for (int q = 0; q < pend_ntile; q++) t += __ldcg(&part[pend_poff + (int64_t)q * pend_ncols + col]);
-        z[pend_z0 + col] = t;
-      }
-      if (lane == 0) PM.cnt[pend_cg] = 0;
-    }
-    pend_cg = -1;
-  };
-  for (int q = cw;; q += NCW) {
-    const int s = q % R;
-    const uint32_t par = (uint32_t)((q / R) & 1);
-    if (!ring_wait(&hrdy[s], par, m0.err, m0.wait, abort_flag)) break;
-    const RingHdr H = hdr[s];
-    if (H.sec < 0) break;
-    // this stage's x rows (lane L: rows L*VEC ..), in flight with the copy
-    Acc xv[VEC];
-#pragma unroll
-    for (int v = 0; v < VEC; v++) {
-      const int r = lane * VEC + v;
-      xv[v] = r < H.nt ? (Acc)__ldg(&x[H.x0 + r]) : Acc(0);
-    }
-    const MatDev& M = H.sec ? m1 : m0;
-    if (!ring_wait(&full[s], par, M.err, M.wait, abort_flag)) break;
-#pragma unroll
-    for (int v = 0; v < VEC; v++) xs[lane * VEC + v] = xv[v];
-    __syncwarp();
-    Acc* z = (Acc*)M.z;
-    Acc* part = (Acc*)M.part;
-    p1_columns<T>((const T*)(smem + (size_t)s * SB), H.ntp, H.nc, H.cc, xs, lane, [&](int cl, Acc v) {
-      const int col = H.c0 + cl;
-      if (H.ntile == 1) z[H.z0 + col] = v;
-      else part[H.poff + (int64_t)H.tile * H.ncols + col] = v;
-    });
-    __syncwarp();  // the stage and the x tile are read
-    if (lane == 0) mbar_arrive(&empty[s]);
-    resolve();
-    if (H.ntile > 1) {
-      // columns done in the group; the arrival is resolved after the next stage
-      if (lane == 0) pend_old = atom_add_acq_rel(&M.cnt[H.cg], H.nc);
-      pend_add = H.nc;
-      pend_cg = H.cg;
-      pend_ntile = H.ntile;
-      pend_ncols = H.ncols;
-      pend_poff = H.poff;
-      pend_z0 = H.z0;
-      pend_sec = H.sec;
-    }
-  }
-  resolve();
-}
-
 // ---------------------------------------------------------------- phase 2
 // Item = one row tile of a row group over all its columns, streamed in chunks
 // of up to SB bytes.  A chunk's multipliers (z for low-rank columns, x for
@@ -1027,17 +789,6 @@ void launch_p1s(const MatDev& m0, const MatDev& m1, int nmat, const double* x, i
 }
 
 template <typename T, int S>
-void launch_p1r(const MatDev& m0, const MatDev& m1, int nmat, const double* x, int sm, int n, cudaStream_t st) {
-  constexpr int NCW = kShapes1[S].nw, R = kShapes1[S].ns;
-  static_assert(kShapes1[S].map == 2 && kShapes1[S].sb == 8192, "a shared-ring shape");
-  // one block per SM; the static schedule has one unit per block
-  const int grid = n < sm ? n : sm;
-  launch_kernel(p1_ring_kernel<T, NCW, R>, dim3(grid), dim3((NCW + kRingProducers) * 32), ring_smem_bytes<NCW, R>(),
-                st, false,
-                m0, m1, nmat, x, S);
-}
-
-template <typename T, int S>
 void launch_p2s(const MatDev& m0, const MatDev& m1, int nmat, const double* x, int sm, int n, cudaStream_t st) {
   constexpr int NW = kShapes2[S].nw, NS = kShapes2[S].ns, SB = kShapes2[S].sb, GA = kShapes2[S].map + 1;
   const int need = (n + NW - 1) / NW;
@@ -1051,17 +802,16 @@ void launch_typed(int phase, int shape, const MatDev& m0, const MatDev& m1, int 
                   cudaStream_t st) {
   const int n = phase == 1 ? m0.ns1 + (nmat == 2 ? m1.ns1 : 0) : m0.ns2 + (nmat == 2 ? m1.ns2 : 0);
   if (n == 0) return;
-  static_assert(kNumShapes1 == 9 && kNumShapes2 == 5, "one case per shape");
+  static_assert(kNumShapes1 == 8 && kNumShapes2 == 6, "one case per shape");
   if (phase == 1) {
     switch (shape) {
-      case 6: launch_p1r<T, 6>(m0, m1, nmat, x, sm, n, st); break;
-      case 7: launch_p1r<T, 7>(m0, m1, nmat, x, sm, n, st); break;
-      case 8: launch_p1r<T, 8>(m0, m1, nmat, x, sm, n, st); break;
       case 1: launch_p1s<T, 1>(m0, m1, nmat, x, sm, n, st); break;
       case 2: launch_p1s<T, 2>(m0, m1, nmat, x, sm, n, st); break;
       case 3: launch_p1s<T, 3>(m0, m1, nmat, x, sm, n, st); break;
       case 4: launch_p1s<T, 4>(m0, m1, nmat, x, sm, n, st); break;
       case 5: launch_p1s<T, 5>(m0, m1, nmat, x, sm, n, st); break;
+      case 6: launch_p1s<T, 6>(m0, m1, nmat, x, sm, n, st); break;
+      case 7: launch_p1s<T, 7>(m0, m1, nmat, x, sm, n, st); break;
       default: launch_p1s<T, 0>(m0, m1, nmat, x, sm, n, st);
     }
   } else {
@@ -1070,6 +820,7 @@ void launch_typed(int phase, int shape, const MatDev& m0, const MatDev& m1, int 
       case 2: launch_p2s<T, 2>(m0, m1, nmat, x, sm, n, st); break;
       case 3: launch_p2s<T, 3>(m0, m1, nmat, x, sm, n, st); break;
       case 4: launch_p2s<T, 4>(m0, m1, nmat, x, sm, n, st); break;
+      case 5: launch_p2s<T, 5>(m0, m1, nmat, x, sm, n, st); break;
       default: launch_p2s<T, 0>(m0, m1, nmat, x, sm, n, st);
     }
   }
@@ -1080,13 +831,6 @@ void prepare_p1() {
   constexpr int NW = kShapes1[S].nw, NS = kShapes1[S].ns, SB = kShapes1[S].sb, MAP = kShapes1[S].map;
   static_assert(smem_bytes<NW, NS, SB>() <= 227 * 1024, "shape exceeds the shared memory of a block");
   set_smem_once(p1_stream_kernel<T, NW, NS, SB, MAP>, smem_bytes<NW, NS, SB>());
-}
-
-template <typename T, int S>
-void prepare_p1r() {
-  constexpr int NCW = kShapes1[S].nw, R = kShapes1[S].ns;
-  static_assert(ring_smem_bytes<NCW, R>() <= 227 * 1024, "shape exceeds the shared memory of a block");
-  set_smem_once(p1_ring_kernel<T, NCW, R>, ring_smem_bytes<NCW, R>());
 }
 
 template <typename T, int S>
@@ -1104,14 +848,14 @@ void prepare_type() {
   prepare_p1<T, 3>();
   prepare_p1<T, 4>();
   prepare_p1<T, 5>();
-  prepare_p1r<T, 6>();
-  prepare_p1r<T, 7>();
-  prepare_p1r<T, 8>();
+  prepare_p1<T, 6>();
+  prepare_p1<T, 7>();
   prepare_p2<T, 0>();
   prepare_p2<T, 1>();
   prepare_p2<T, 2>();
   prepare_p2<T, 3>();
   prepare_p2<T, 4>();
+  prepare_p2<T, 5>();
 }
 
 }  // namespace

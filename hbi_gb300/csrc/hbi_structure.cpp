@@ -417,6 +417,42 @@ void plan_warp_schedule(const std::vector<int64_t>& cost, int nwarps, std::vecto
   for (int q = 0; q < n; q++) witem[fill[owner[q]]++] = order[q];
 }
 
+void plan_block_schedule(const std::vector<int64_t>& cost, const std::vector<int64_t>& key, int nblocks, int nw,
+                         std::vector<int32_t>& woff, std::vector<int32_t>& witem) {
+  const int n = (int)cost.size();
+  std::vector<int32_t> order(n);
+  for (int i = 0; i < n; i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key[a] < key[b]; });
+  int64_t total = 0;
+  for (int64_t c : cost) total += c;
+  // block b takes order[cut[b] .. cut[b + 1]): each cut where the running cost
+  // is nearest to total * b / nblocks
+  std::vector<int> cut(nblocks + 1, n);
+  cut[0] = 0;
+  int i = 0;
+  int64_t run = 0;
+  for (int b = 1; b < nblocks; b++) {
+    const double target = (double)total * b / nblocks;
+    while (i < n && (double)(run + cost[order[i]]) <= target) run += cost[order[i++]];
+    // one more item if that lands nearer the target
+    if (i < n && (double)(run + cost[order[i]]) - target < target - (double)run) run += cost[order[i++]];
+    cut[b] = i;
+  }
+  woff.assign((size_t)nblocks * nw + 1, 0);
+  witem.clear();
+  witem.reserve(n);
+  for (int b = 0; b < nblocks; b++) {
+    std::vector<int64_t> sub;
+    for (int q = cut[b]; q < cut[b + 1]; q++) sub.push_back(cost[order[q]]);
+    std::vector<int32_t> so, si;
+    plan_warp_schedule(sub, nw, so, si);
+    for (int w = 0; w < nw; w++) {
+      for (int e = so[w]; e < so[w + 1]; e++) witem.push_back(order[cut[b] + si[e]]);
+      woff[(size_t)b * nw + w + 1] = (int32_t)witem.size();
+    }
+  }
+}
+
 void plan_tc(int n, const std::vector<Leaf>& leaves, const std::vector<int64_t>& body_off, TcPlan& tp) {
   const int nl = (int)leaves.size();
   const int TR = 256;  // phase 2: rows of a tile

@@ -131,6 +131,13 @@ inline int chunk_cols(int ntp, int esz, int stage_bytes) {
 // that order.  woff (nwarps + 1) and witem are its CSR lists.
 void plan_warp_schedule(const std::vector<int64_t>& cost, int nwarps, std::vector<int32_t>& woff,
                         std::vector<int32_t>& witem);
+// Static schedule with locality: the items in order of `key` (their offset
+// in the store) are cut into nblocks consecutive runs of near-equal cost, and
+// each run is dealt over its block's nw warps longest first.  A block then
+// streams one compact region of the store instead of items from all over it.
+// woff (nblocks * nw + 1) and witem as plan_warp_schedule, warp b * nw + w.
+void plan_block_schedule(const std::vector<int64_t>& cost, const std::vector<int64_t>& key, int nblocks, int nw,
+                         std::vector<int32_t>& woff, std::vector<int32_t>& witem);
 
 // ---- tensor-core plan of the ensemble product ---------------------------
 // Both contractions as D (64 members x N) = A (64 x K) * B^T with B (N x K)

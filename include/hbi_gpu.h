@@ -189,11 +189,14 @@ int hbi_adot_lattice_hyp_phase_dev(double* d_au, hbi_lhp* st_LHp, const double* 
  * keeps the fastest per phase; operators whose plans have the same size
  * statistics reuse the choice; the environment variables HBI_STREAM_SHAPE1=s
  * and HBI_STREAM_SHAPE2=s force shape s of phase 1 / phase 2. */
-/* the compiled shapes of phase 1 or 2: *count, and shapes4[4*s .. 4*s+3] =
- * warps per block, stages per warp, stage bytes, lane mapping (phase 1: 0 =
- * the lanes of a column split its rows, 1 = one lane per column; phase 2: 0)
- * (shapes4 may be NULL) */
-int hbi_stream_shapes(int phase, int* count, int* shapes4);
+/* the compiled shapes of phase 1 or 2: *count, and shapes5[5*s .. 5*s+4] =
+ * warps per block, stages per warp, stage bytes, variant (phase 1: 0 = the
+ * lanes of a column split its rows, 1 = one lane per column; phase 2: how
+ * many chunks ahead the multipliers are gathered, minus one), schedule (0 =
+ * items over all warps longest first, 1 = per block a run of items
+ * consecutive in the store, see hbi_plan_block_schedule) (shapes5 may be
+ * NULL) */
+int hbi_stream_shapes(int phase, int* count, int* shapes5);
 /* the shapes chosen for phases 1 and 2, the median time in microseconds of
  * every shape (phase 1's shapes, then phase 2's; -1 if not timed) and how
  * they were chosen (0 timed, 1 reused, 2 forced or pinned) */
@@ -392,6 +395,13 @@ int hbi_plan_emulate(int n, int nleaf, const int* leaves6, const double* body, i
  * least-loaded of nwarps warps.  woff[nwarps + 1] and witem[n] receive the
  * CSR lists (warp w: witem[woff[w] .. woff[w+1])). */
 int hbi_plan_warp_schedule(int n, const int64_t* cost, int nwarps, int32_t* woff, int32_t* witem);
+/* Host-only (no reference counterpart): the schedule with locality -- the n
+ * items in order of key (their store offset) cut into nblocks consecutive
+ * runs of near-equal cost, each run dealt longest-first over its block's nw
+ * warps; woff[nblocks * nw + 1], witem[n] as hbi_plan_warp_schedule (warp
+ * b * nw + w). */
+int hbi_plan_block_schedule(int n, const int64_t* cost, const int64_t* key, int nblocks, int nw, int32_t* woff,
+                            int32_t* witem);
 
 /* ---- ensemble of simulations sharing one H-matrix pair (no reference
  * counterpart; configuration c4) -----------------------------------------

@@ -49,24 +49,49 @@ def test_near_ties_keep_the_earlier_shape():
 def test_shape_table_fits_the_kernels():
     for phase in (1, 2):
         shapes = H.stream_shapes(phase)
-        assert len(shapes) >= 3 and shapes[0] == (12, 2, 8192, 0)
-        for nw, ns, sb, lane_map in shapes:
+        assert len(shapes) >= 3 and shapes[0] == (12, 2, 8192, 0, 0)
+        for nw, ns, sb, variant, sched in shapes:
             assert 1 <= nw <= 32 and ns >= 2 and sb in (8192, 16384)
-            assert lane_map in ((0, 1, 2) if phase == 1 else (0, 1))
-            if lane_map == 2:
-                # shared ring: ns stages + 64-byte headers, a 1 KB x tile per
-                # consumer warp, three barriers per stage; four producer warps more
-                assert sb == 8192 and nw + 4 <= 32 and nw <= ns
-                smem = ns * sb + ns * 64 + nw * 1024 + 3 * ns * 8 + 16
-            else:
-                smem = nw * ns * sb + nw * 128 * 8 + nw * ns * 8
+            assert variant in (0, 1) and sched in (0, 1)
+            smem = nw * ns * sb + nw * 128 * 8 + nw * ns * 8
             assert smem <= 227 * 1024
             for esz in (2, 4, 8):
                 for ntp in range(16 // esz, 512 // esz + 1, 16 // esz):
                     cc = (sb // (ntp * esz)) // 16 * 16
                     cc = min(cc, 128)
                     assert 16 <= cc <= 128 and cc * ntp * esz <= sb
-    assert {m for *_, m in H.stream_shapes(1)} == {0, 1, 2}
+    assert {m for _, _, _, m, _ in H.stream_shapes(1)} == {0, 1}
+    # both schedules are candidates of both phases
+    for phase in (1, 2):
+        assert {s for *_, s in H.stream_shapes(phase)} == {0, 1}
+
+
+@pytest.mark.parametrize("nblocks,nw", [(1, 12), (7, 3), (152, 12)])
+def test_block_schedule_is_local_and_balanced(nblocks, nw):
+    """The schedule with locality: every item exactly once; each block's items
+    are consecutive in store order; block loads within one item of the
+    average; inside a block every warp's items in decreasing cost."""
+    rng = np.random.default_rng(nblocks + nw)
+    n = 5000
+    cost = rng.integers(512, 300_000, n)
+    key = rng.permutation(n).astype(np.int64) * 4096
+    woff, witem = H.plan_block_schedule(cost, key, nblocks, nw)
+    assert woff[0] == 0 and woff[-1] == n and np.all(np.diff(woff) >= 0)
+    assert np.array_equal(np.sort(witem), np.arange(n))
+    rank = np.empty(n, dtype=np.int64)
+    rank[np.argsort(key, kind="stable")] = np.arange(n)
+    loads = []
+    for b in range(nblocks):
+        items = witem[woff[b * nw]:woff[(b + 1) * nw]]
+        if len(items):
+            r = np.sort(rank[items])
+            assert r[-1] - r[0] + 1 == len(r)  # a run of consecutive items
+        loads.append(cost[items].sum())
+        for w in range(nw):
+            c = cost[witem[woff[b * nw + w]:woff[b * nw + w + 1]]]
+            assert np.all(np.diff(c) <= 0)
+    loads = np.array(loads)
+    assert np.abs(loads - cost.sum() / nblocks).max() <= cost.max()
 
 
 def _vswz(c, nv):

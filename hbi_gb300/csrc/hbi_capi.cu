@@ -209,6 +209,7 @@ struct hbi_lhp_s {
   int tune_source = 0;  // 0 timed, 1 cached from an operator of the same plan, 2 forced or pinned
   float tune_us[2][kMaxShapes] = {};
   int* d_err = nullptr;
+  int* d_dyn = nullptr;  // dynamic schedules: grab and exit counters of phases 1 and 2
   double *d_x = nullptr, *d_y = nullptr;
   MatDev md{};
   std::vector<Leaf> leaves;
@@ -819,6 +820,8 @@ static int construct_impl(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* c, int
   CK(cudaMemset(h->d_cnt, 0, sizeof(int) * std::max<int64_t>(P.ncg, 1)));
   CK(dalloc(&h->d_err, 1));
   CK(cudaMemset(h->d_err, 0, sizeof(int)));
+  CK(dalloc(&h->d_dyn, 4));
+  CK(cudaMemset(h->d_dyn, 0, sizeof(int) * 4));
   CK(cudaMalloc(&h->d_part, std::max<size_t>(P.plen1, 1) * acc));
   CK(cudaMalloc(&h->d_z, std::max<size_t>(P.zlen, 1) * acc));
   CK(cudaMemset(h->d_z, 0, std::max<size_t>(P.zlen, 1) * acc));
@@ -845,6 +848,7 @@ static int construct_impl(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* c, int
   m.scale = 1.0;
   m.skip = nullptr;
   m.err = h->d_err;
+  m.dyn = h->d_dyn;
   m.wait = kWaitCyclesDefault;
   m.ncnt = (int)P.ncg;
   // static warp schedules, one per launch shape, for the grid the phase
@@ -867,6 +871,7 @@ static int construct_impl(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* c, int
         cost[i] = (int64_t)ncols * ntp * esz + 1024 * (int64_t)((ncols + cc - 1) / cc);
         key[i] = ph == 1 ? P.p1[i].soff : P.p2[i].soff;
       }
+      if (S.sched == 2) continue;  // dynamic: the warps take the items in order from a counter
       std::vector<int32_t> woff, witem;
       if (S.sched == 1) plan_block_schedule(cost, key, nblk, nw, woff, witem);
       else plan_warp_schedule(cost, gw, woff, witem);
@@ -905,6 +910,7 @@ extern "C" int hbi_free_lh(hbi_lhp* h) {
   for (void* p : {h->d_vstore, h->d_ustore, (void*)h->d_s1, (void*)h->d_s2, (void*)h->d_cnt, h->d_part, h->d_z,
                   h->d_gpart, (void*)h->d_midx, (void*)h->d_grow0, (void*)h->d_gndl, (void*)h->d_gnch,
                   (void*)h->d_gpoff, (void*)h->d_row_fc, (void*)h->d_fc_ptr, (void*)h->d_fc_group, (void*)h->d_err,
+                  (void*)h->d_dyn,
                   (void*)h->d_fcb_ptr, (void*)h->d_fcb_base,
                   (void*)h->d_x, (void*)h->d_y})
     if (p) cudaFree(p);
@@ -926,7 +932,8 @@ int take_device_error(const MatDev& m) {
   if (!flag) return 0;
   // a warp that gave up left before its arrivals: the counters start over
   if (cudaMemset(m.err, 0, sizeof(int)) != cudaSuccess ||
-      (m.cnt && m.ncnt > 0 && cudaMemset(m.cnt, 0, sizeof(int) * (size_t)m.ncnt) != cudaSuccess))
+      (m.cnt && m.ncnt > 0 && cudaMemset(m.cnt, 0, sizeof(int) * (size_t)m.ncnt) != cudaSuccess) ||
+      (m.dyn && cudaMemset(m.dyn, 0, sizeof(int) * 4) != cudaSuccess))
     return HBI_ERR_CUDA;
   return 1;
 }

@@ -53,20 +53,22 @@ constexpr long long kWaitCyclesDefault = 2LL << 30;
 // 1 the lane mapping (0: the lanes of a column segment split its rows and
 // reduce by shuffles; 1: one lane per column, no cross-lane reduction), for
 // phase 2 how far ahead the multipliers are gathered (0: one chunk, 1: two)
-// -- and the static schedule (0: the phase's items dealt over all warps
-// longest first; 1: each block a run of items consecutive in the store,
-// plan_block_schedule).  Every shape is compiled for every storage type;
+// -- and the schedule (0: the phase's items dealt over all warps longest
+// first, statically; 1: each block a run of items consecutive in the store,
+// plan_block_schedule; 2: dynamic, every warp takes the next item, longest
+// first, from a counter when it needs one).  Every shape is compiled for every storage type;
 // hbi_construct_lh times them on the operator and keeps the fastest per
 // phase (autotune_stream_shapes).  Shape 0 of each phase is the default.
 struct StreamShape {
   int nw, ns, sb, map, sched;
 };
-constexpr int kNumShapes1 = 8, kNumShapes2 = 6, kMaxShapes = 8;
+constexpr int kNumShapes1 = 9, kNumShapes2 = 7, kMaxShapes = 9;
 constexpr StreamShape kShapes1[kNumShapes1] = {{12, 2, 8192, 0, 0}, {8, 3, 8192, 0, 0}, {6, 2, 16384, 0, 0},
                                                {12, 2, 8192, 1, 0}, {8, 3, 8192, 1, 0}, {6, 2, 16384, 1, 0},
-                                               {12, 2, 8192, 1, 1}, {12, 2, 8192, 0, 1}};
+                                               {12, 2, 8192, 1, 1}, {12, 2, 8192, 0, 1}, {12, 2, 8192, 1, 2}};
 constexpr StreamShape kShapes2[kNumShapes2] = {{12, 2, 8192, 0, 0}, {8, 3, 8192, 0, 0}, {6, 2, 16384, 0, 0},
-                                               {10, 2, 8192, 0, 0}, {8, 3, 8192, 1, 0}, {12, 2, 8192, 0, 1}};
+                                               {10, 2, 8192, 0, 0}, {8, 3, 8192, 1, 0}, {12, 2, 8192, 0, 1},
+                                               {12, 2, 8192, 0, 2}};
 inline const StreamShape& stream_shape(int phase, int s) { return phase == 1 ? kShapes1[s] : kShapes2[s]; }
 inline int num_shapes(int phase) { return phase == 1 ? kNumShapes1 : kNumShapes2; }
 
@@ -132,6 +134,7 @@ struct MatDev {            // one H-matrix on the device
   int* err;                // set to nonzero when a bulk copy did not arrive in time
   long long wait;          // bound of a stage wait in SM clock cycles (0: every wait gives up at once)
   int ncnt;                // number of arrival counters in cnt
+  int* dyn;                // dynamic schedules: [2 (phase - 1)] items taken, [2 (phase - 1) + 1] warps done
   // static warp schedules (hbi_structure.hpp, plan_warp_schedule), one per
   // launch shape s, for a grid of gw1[s] / gw2[s] warps: warp w walks
   // item[off[w] .. off[w+1]) of its phase

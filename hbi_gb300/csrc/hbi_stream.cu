@@ -113,18 +113,22 @@ __device__ __forceinline__ void lds16(const __nv_bfloat16* p, float* o) {
 __device__ __forceinline__ int log2ceil(int n) { return n <= 1 ? 0 : 32 - __clz(n - 1); }
 
 // shared memory of a block: per warp NS stages of SB bytes, then per warp the
-// 128 multipliers of its current phase-2 chunk, then the stage barriers
+// 128 multipliers of its current phase-2 chunk, then the stage barriers, then
+// per warp the item ids a dynamic schedule took (kHist)
 constexpr int kMaxCols = 128;  // columns of a chunk at most (chunk_cols)
 constexpr int kMu = kMaxCols * 8;
+constexpr int kHist = 16;
 template <int NW, int NS, int SB>
 struct Ring {
   unsigned char* buf;  // stage s at buf + s * SB
   void* mu;            // kMaxCols multipliers (Acc) of the warp
   uint64_t* bar;
+  int* hist;           // kHist item ids
   __device__ Ring(unsigned char* smem, int warp) {
     buf = smem + (size_t)warp * NS * SB;
     mu = smem + (size_t)NW * NS * SB + (size_t)warp * kMu;
     bar = reinterpret_cast<uint64_t*>(smem + (size_t)NW * NS * SB + (size_t)NW * kMu) + warp * NS;
+    hist = reinterpret_cast<int*>(smem + (size_t)NW * NS * SB + (size_t)NW * kMu + (size_t)NW * NS * 8) + warp * kHist;
   }
 };
 
@@ -165,12 +169,35 @@ __device__ __forceinline__ int arrive_acq_rel(int* p) {
 }
 
 // The items one warp walks, in order: the host's schedule when it was made
-// for this grid (m0's list, then m1's), else every GW-th item.  at(k) is the
-// k-th item, ntot past the end.
+// for this grid (m0's list, then m1's), else every GW-th item; or, with a
+// dynamic schedule, the items the warp takes from the phase's counter (both
+// lists in order, longest first within each), one grab issued ahead so that
+// its round trip overlaps the work, the ids kept in the warp's kHist slots
+// (a warp looks at most NS + 3 items ahead of the item it consumes).  at(k)
+// is the k-th item, ntot past the end.
 struct WarpSeq {
   const int32_t *a0 = nullptr, *a1 = nullptr;
   int len0 = 0, len1 = 0, n0 = 0, gw = 0, GW = 1, ntot = 0;
-  __device__ int at(int k) const {
+  int* ctr = nullptr;  // dynamic: the phase's item counter
+  int* hist = nullptr;
+  int ngrab = 0, pend = 0, lane = 0;  // pend: lane 0's grab in flight
+  __device__ void make_dynamic(int* counter, int* slots) {
+    ctr = counter;
+    hist = slots;
+    lane = threadIdx.x & 31;
+    if (lane == 0) pend = atomicAdd(ctr, 1);
+  }
+  __device__ int at(int k) {
+    if (ctr) {
+      while (ngrab <= k) {
+        const int v = __shfl_sync(0xffffffffu, pend, 0);
+        if (lane == 0) hist[ngrab % kHist] = v < ntot ? v : ntot;
+        __syncwarp();
+        ngrab++;
+        if (lane == 0) pend = atomicAdd(ctr, 1);
+      }
+      return hist[k % kHist];
+    }
     if (a0) {
       if (k < len0) return __ldg(&a0[k]);
       k -= len0;
@@ -180,6 +207,23 @@ struct WarpSeq {
     return it < ntot ? (int)it : ntot;
   }
 };
+
+// a warp of a dynamically scheduled phase leaves: its last grab is ordered
+// before it counts itself out, and the last warp of the grid out resets the
+// phase's counters for the next launch
+__device__ __forceinline__ void dyn_leave(const WarpSeq& q, int* exits, int nwarps) {
+  if (!q.ctr) return;
+  __syncwarp();
+  if (q.lane == 0) {
+    // release: the warp's grabs, the one still in flight included, come
+    // before its count; acquire: the last warp's reset comes after them all
+    if (arrive_acq_rel(exits) == nwarps - 1) {
+      atomicExch(q.ctr, 0);
+      atomicExch(exits, 0);
+    }
+  }
+  __syncwarp();
+}
 
 __device__ __forceinline__ WarpSeq warp_seq(const MatDev& m0, const MatDev& m1, int nmat, int phase, int shape,
                                             int gw, int GW, int n0, int ntot) {
@@ -273,7 +317,7 @@ __device__ __forceinline__ void p1_columns(const T* st, int ntp, int nc, int cc,
 // MAP 1: one lane per column (two lanes, each half the rows, when a chunk has
 // only 16 columns), the item's x tile in the warp's shared-memory buffer:
 // no cross-lane reduction, VEC independent accumulator chains per lane.
-template <typename T, int NW, int NS, int SB, int MAP>
+template <typename T, int NW, int NS, int SB, int MAP, bool DYN>
 __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev m1, int nmat,
                                                                const double* __restrict__ x, int shape) {
   typedef typename AccT<T>::type Acc;
@@ -304,7 +348,9 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
     d.cc = d.ntp > 0 ? chunk_cols(d.ntp, ESZ, SB) : 16;
     return d;
   };
-  const WarpSeq seq = warp_seq(m0, m1, nmat, 1, shape, gw, GW, n0, ntot);
+  WarpSeq seq = warp_seq(m0, m1, nmat, 1, shape, gw, GW, n0, ntot);
+  if constexpr (DYN) seq.make_dynamic(m0.dyn + 0, R.hist);
+  int* const exits = m0.dyn + 1;
   // producer: walks this warp's items chunk by chunk, NS chunks ahead; the
   // item ids are fetched two items ahead, the descriptors one
   int p_k = 0, p_it = seq.at(0), p_itn = seq.at(1), p_itnn = seq.at(2), p_c0 = 0, p_seq = 0;
@@ -340,6 +386,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
   if (m0.skip && __ldcg(m0.skip)) {
     // a halted loop skips the product: let the copies already started land
     drain<NS>(R.bar, 0, p_seq);
+    dyn_leave(seq, exits, GW);
     return;
   }
   // consumer: item ids three ahead, descriptors two
@@ -394,6 +441,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
     const int s = c_seq % NS;
     if (!stage_ready(&R.bar[s], (uint32_t)((c_seq / NS) & 1), M.err, M.wait)) {
       drain<NS>(R.bar, c_seq, p_seq);
+      dyn_leave(seq, exits, GW);
       return;
     }
     const int nc = min(Dc.cc, Dc.ncols - c_c0);
@@ -516,6 +564,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
     Dnn = desc(c_i2);
   }
   resolve();
+  dyn_leave(seq, exits, GW);
 }
 
 // ---------------------------------------------------------------- phase 2
@@ -531,7 +580,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
 // or more stages: the indices of chunk c + 2 are in the FIFO when chunk c
 // starts); two register sets of multipliers then cover two chunk times of
 // load latency.
-template <typename T, int NW, int NS, int SB, int GA>
+template <typename T, int NW, int NS, int SB, int GA, bool DYN>
 __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev m1, int nmat,
                                                                const double* __restrict__ x, int shape) {
   typedef typename AccT<T>::type Acc;
@@ -567,7 +616,9 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
     int32_t idx[KP];
     int nc, sec;
   };
-  const WarpSeq seq = warp_seq(m0, m1, nmat, 2, shape, gw, GW, n0, ntot);
+  WarpSeq seq = warp_seq(m0, m1, nmat, 2, shape, gw, GW, n0, ntot);
+  if constexpr (DYN) seq.make_dynamic(m0.dyn + 2, R.hist);
+  int* const exits = m0.dyn + 3;
   int p_k = 0, p_it = seq.at(0), p_itn = seq.at(1), p_itnn = seq.at(2), p_c0 = 0, p_seq = 0;
   S2ItemDev Dp = current(desc(p_it)), Dpn = desc(p_itn);
   auto produce = [&](Pend& pd) {
@@ -624,6 +675,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
   pdl_wait_prior();
   if (m0.skip && __ldcg(m0.skip)) {
     drain<NS>(R.bar, 0, p_seq);
+    dyn_leave(seq, exits, GW);
     return;
   }
   Acc mu[KP], mu2[KP];
@@ -640,6 +692,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
     const int s = c_seq % NS;
     if (!stage_ready(&R.bar[s], (uint32_t)((c_seq / NS) & 1), M.err, M.wait)) {
       drain<NS>(R.bar, c_seq, p_seq);
+      dyn_leave(seq, exits, GW);
       return;
     }
     const int nc = min(Dc.cc, Dc.ncols - c_c0);
@@ -716,6 +769,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
     Dc = current(Dn);
     Dn = desc(c_i1);
   }
+  dyn_leave(seq, exits, GW);
 }
 
 // ------------------------------------------------------ store conversion
@@ -747,7 +801,7 @@ namespace {
 // block's shared memory: NW x NS x SB + multipliers + barriers
 template <int NW, int NS, int SB>
 constexpr size_t smem_bytes() {
-  return (size_t)NW * NS * SB + (size_t)NW * kMu + (size_t)NW * NS * 8;
+  return (size_t)NW * NS * SB + (size_t)NW * kMu + (size_t)NW * NS * 8 + (size_t)NW * kHist * 4;
 }
 
 template <typename K>
@@ -784,8 +838,8 @@ void launch_p1s(const MatDev& m0, const MatDev& m1, int nmat, const double* x, i
   // launch): a phase-1 block needs nearly all of an SM's registers, and one
   // started early would keep the rest of the previous stage's phase-3 blocks
   // off its SM
-  launch_kernel(p1_stream_kernel<T, NW, NS, SB, MAP>, dim3(grid), dim3(NW * 32), smem_bytes<NW, NS, SB>(), st, false,
-                m0, m1, nmat, x, S);
+  launch_kernel(p1_stream_kernel<T, NW, NS, SB, MAP, kShapes1[S].sched == 2>, dim3(grid), dim3(NW * 32),
+                smem_bytes<NW, NS, SB>(), st, false, m0, m1, nmat, x, S);
 }
 
 template <typename T, int S>
@@ -793,8 +847,8 @@ void launch_p2s(const MatDev& m0, const MatDev& m1, int nmat, const double* x, i
   constexpr int NW = kShapes2[S].nw, NS = kShapes2[S].ns, SB = kShapes2[S].sb, GA = kShapes2[S].map + 1;
   const int need = (n + NW - 1) / NW;
   const int grid = need < sm ? (need > 0 ? need : 1) : sm;
-  launch_kernel(p2_stream_kernel<T, NW, NS, SB, GA>, dim3(grid), dim3(NW * 32), smem_bytes<NW, NS, SB>(), st,
-                pdl_enabled(), m0, m1, nmat, x, S);
+  launch_kernel(p2_stream_kernel<T, NW, NS, SB, GA, kShapes2[S].sched == 2>, dim3(grid), dim3(NW * 32),
+                smem_bytes<NW, NS, SB>(), st, pdl_enabled(), m0, m1, nmat, x, S);
 }
 
 template <typename T>
@@ -802,7 +856,7 @@ void launch_typed(int phase, int shape, const MatDev& m0, const MatDev& m1, int 
                   cudaStream_t st) {
   const int n = phase == 1 ? m0.ns1 + (nmat == 2 ? m1.ns1 : 0) : m0.ns2 + (nmat == 2 ? m1.ns2 : 0);
   if (n == 0) return;
-  static_assert(kNumShapes1 == 8 && kNumShapes2 == 6, "one case per shape");
+  static_assert(kNumShapes1 == 9 && kNumShapes2 == 7, "one case per shape");
   if (phase == 1) {
     switch (shape) {
       case 1: launch_p1s<T, 1>(m0, m1, nmat, x, sm, n, st); break;
@@ -812,6 +866,7 @@ void launch_typed(int phase, int shape, const MatDev& m0, const MatDev& m1, int 
       case 5: launch_p1s<T, 5>(m0, m1, nmat, x, sm, n, st); break;
       case 6: launch_p1s<T, 6>(m0, m1, nmat, x, sm, n, st); break;
       case 7: launch_p1s<T, 7>(m0, m1, nmat, x, sm, n, st); break;
+      case 8: launch_p1s<T, 8>(m0, m1, nmat, x, sm, n, st); break;
       default: launch_p1s<T, 0>(m0, m1, nmat, x, sm, n, st);
     }
   } else {
@@ -821,6 +876,7 @@ void launch_typed(int phase, int shape, const MatDev& m0, const MatDev& m1, int 
       case 3: launch_p2s<T, 3>(m0, m1, nmat, x, sm, n, st); break;
       case 4: launch_p2s<T, 4>(m0, m1, nmat, x, sm, n, st); break;
       case 5: launch_p2s<T, 5>(m0, m1, nmat, x, sm, n, st); break;
+      case 6: launch_p2s<T, 6>(m0, m1, nmat, x, sm, n, st); break;
       default: launch_p2s<T, 0>(m0, m1, nmat, x, sm, n, st);
     }
   }
@@ -830,14 +886,14 @@ template <typename T, int S>
 void prepare_p1() {
   constexpr int NW = kShapes1[S].nw, NS = kShapes1[S].ns, SB = kShapes1[S].sb, MAP = kShapes1[S].map;
   static_assert(smem_bytes<NW, NS, SB>() <= 227 * 1024, "shape exceeds the shared memory of a block");
-  set_smem_once(p1_stream_kernel<T, NW, NS, SB, MAP>, smem_bytes<NW, NS, SB>());
+  set_smem_once(p1_stream_kernel<T, NW, NS, SB, MAP, kShapes1[S].sched == 2>, smem_bytes<NW, NS, SB>());
 }
 
 template <typename T, int S>
 void prepare_p2() {
   constexpr int NW = kShapes2[S].nw, NS = kShapes2[S].ns, SB = kShapes2[S].sb, GA = kShapes2[S].map + 1;
   static_assert(smem_bytes<NW, NS, SB>() <= 227 * 1024, "shape exceeds the shared memory of a block");
-  set_smem_once(p2_stream_kernel<T, NW, NS, SB, GA>, smem_bytes<NW, NS, SB>());
+  set_smem_once(p2_stream_kernel<T, NW, NS, SB, GA, kShapes2[S].sched == 2>, smem_bytes<NW, NS, SB>());
 }
 
 template <typename T>
@@ -850,12 +906,14 @@ void prepare_type() {
   prepare_p1<T, 5>();
   prepare_p1<T, 6>();
   prepare_p1<T, 7>();
+  prepare_p1<T, 8>();
   prepare_p2<T, 0>();
   prepare_p2<T, 1>();
   prepare_p2<T, 2>();
   prepare_p2<T, 3>();
   prepare_p2<T, 4>();
   prepare_p2<T, 5>();
+  prepare_p2<T, 6>();
 }
 
 }  // namespace

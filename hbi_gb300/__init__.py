@@ -285,7 +285,7 @@ class LHp:
         _check(lib().hbi_lh_tuning(self.h, C.byref(s1), C.byref(s2), us.ctypes.data_as(C.POINTER(C.c_float)),
                                    C.byref(src)), "hbi_lh_tuning")
         name = lambda t: "%dw x %d x %d KB%s%s" % (t[0], t[1], t[2] // 1024, " col" if t[3] else "",
-                                                 {0: "", 1: " blocks", 2: " dynamic"}[t[4]])
+                                                 {0: "", 1: " blocks", 2: " dynamic", 3: " block-shared"}[t[4]])
         return {"phase1": name(sh1[s1.value]), "phase2": name(sh2[s2.value]), "shape1": s1.value,
                 "shape2": s2.value, "source": {0: "timed", 1: "reused", 2: "forced"}.get(src.value, "?"),
                 "phase1_us": {name(t): round(float(us[i]), 2) for i, t in enumerate(sh1)},

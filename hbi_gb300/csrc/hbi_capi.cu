@@ -862,7 +862,8 @@ static int construct_impl(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* c, int
       if (ni == 0) continue;
       const int need = (ni + nw - 1) / nw;
       const int nblk = need < c->sm_count ? need : c->sm_count;
-      const int gw = nblk * nw;
+      // schedule units: warps, or blocks for the block-shared schedule
+      const int gw = S.sched == 3 ? nblk : nblk * nw;
       std::vector<int64_t> cost(ni), key(ni);
       for (int i = 0; i < ni; i++) {
         const int ncols = ph == 1 ? P.p1[i].ncols : P.p2[i].ncols, ntp = ph == 1 ? P.p1[i].ntp : P.p2[i].ntp;

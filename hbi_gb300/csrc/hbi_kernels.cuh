@@ -56,19 +56,22 @@ constexpr long long kWaitCyclesDefault = 2LL << 30;
 // -- and the schedule (0: the phase's items dealt over all warps longest
 // first, statically; 1: each block a run of items consecutive in the store,
 // plan_block_schedule; 2: dynamic, every warp takes the next item, longest
-// first, from a counter when it needs one).  Every shape is compiled for every storage type;
+// first, from a global counter when it needs one; 3: the items dealt over
+// the blocks longest first, and each block's warps take its items from a
+// shared-memory counter).  Every shape is compiled for every storage type;
 // hbi_construct_lh times them on the operator and keeps the fastest per
 // phase (autotune_stream_shapes).  Shape 0 of each phase is the default.
 struct StreamShape {
   int nw, ns, sb, map, sched;
 };
-constexpr int kNumShapes1 = 9, kNumShapes2 = 7, kMaxShapes = 9;
+constexpr int kNumShapes1 = 10, kNumShapes2 = 8, kMaxShapes = 10;
 constexpr StreamShape kShapes1[kNumShapes1] = {{12, 2, 8192, 0, 0}, {8, 3, 8192, 0, 0}, {6, 2, 16384, 0, 0},
                                                {12, 2, 8192, 1, 0}, {8, 3, 8192, 1, 0}, {6, 2, 16384, 1, 0},
-                                               {12, 2, 8192, 1, 1}, {12, 2, 8192, 0, 1}, {12, 2, 8192, 1, 2}};
+                                               {12, 2, 8192, 1, 1}, {12, 2, 8192, 0, 1}, {12, 2, 8192, 1, 2},
+                                               {12, 2, 8192, 1, 3}};
 constexpr StreamShape kShapes2[kNumShapes2] = {{12, 2, 8192, 0, 0}, {8, 3, 8192, 0, 0}, {6, 2, 16384, 0, 0},
                                                {10, 2, 8192, 0, 0}, {8, 3, 8192, 1, 0}, {12, 2, 8192, 0, 1},
-                                               {12, 2, 8192, 0, 2}};
+                                               {12, 2, 8192, 0, 2}, {12, 2, 8192, 0, 3}};
 inline const StreamShape& stream_shape(int phase, int s) { return phase == 1 ? kShapes1[s] : kShapes2[s]; }
 inline int num_shapes(int phase) { return phase == 1 ? kNumShapes1 : kNumShapes2; }
 

@@ -124,11 +124,14 @@ struct Ring {
   void* mu;            // kMaxCols multipliers (Acc) of the warp
   uint64_t* bar;
   int* hist;           // kHist item ids
+  int* bctr;           // the block's item counter (block-shared schedule)
   __device__ Ring(unsigned char* smem, int warp) {
     buf = smem + (size_t)warp * NS * SB;
     mu = smem + (size_t)NW * NS * SB + (size_t)warp * kMu;
     bar = reinterpret_cast<uint64_t*>(smem + (size_t)NW * NS * SB + (size_t)NW * kMu) + warp * NS;
-    hist = reinterpret_cast<int*>(smem + (size_t)NW * NS * SB + (size_t)NW * kMu + (size_t)NW * NS * 8) + warp * kHist;
+    int* tail = reinterpret_cast<int*>(smem + (size_t)NW * NS * SB + (size_t)NW * kMu + (size_t)NW * NS * 8);
+    hist = tail + warp * kHist;
+    bctr = tail + NW * kHist;
   }
 };
 
@@ -181,16 +184,47 @@ struct WarpSeq {
   int* ctr = nullptr;  // dynamic: the phase's item counter
   int* hist = nullptr;
   int ngrab = 0, pend = 0, lane = 0;  // pend: lane 0's grab in flight
+  // dynamic: a warp's first two items are fixed (the largest 2 GW items,
+  // dealt in snake order), so that the grid does not start with one burst of
+  // atomics on the counter; the counter numbers the items after them
   __device__ void make_dynamic(int* counter, int* slots) {
     ctr = counter;
     hist = slots;
     lane = threadIdx.x & 31;
-    if (lane == 0) pend = atomicAdd(ctr, 1);
+    if (lane == 0) {
+      hist[0] = gw < ntot ? gw : ntot;
+      hist[1] = 2 * GW - 1 - gw < ntot ? 2 * GW - 1 - gw : ntot;
+      pend = atomicAdd(ctr, 1);
+    }
+    __syncwarp();
+    ngrab = 2;
+  }
+  // block-shared: the warps of a block take the block's items (the host's
+  // per-block list, longest first) from a shared-memory counter; hist keeps
+  // list positions
+  int* sctr = nullptr;
+  __device__ void make_block_shared(int* counter, int* slots) {
+    sctr = counter;
+    hist = slots;
+    lane = threadIdx.x & 31;
+    if (lane == 0) pend = atomicAdd(sctr, 1);
   }
   __device__ int at(int k) {
-    if (ctr) {
+    if (sctr) {
       while (ngrab <= k) {
         const int v = __shfl_sync(0xffffffffu, pend, 0);
+        if (lane == 0) hist[ngrab % kHist] = v;
+        __syncwarp();
+        ngrab++;
+        if (lane == 0) pend = atomicAdd(sctr, 1);
+      }
+      const int v = hist[k % kHist];
+      if (v < len0) return __ldg(&a0[v]);
+      return v - len0 < len1 ? n0 + __ldg(&a1[v - len0]) : ntot;
+    }
+    if (ctr) {
+      while (ngrab <= k) {
+        const int v = __shfl_sync(0xffffffffu, pend, 0) + 2 * GW;
         if (lane == 0) hist[ngrab % kHist] = v < ntot ? v : ntot;
         __syncwarp();
         ngrab++;
@@ -317,7 +351,7 @@ __device__ __forceinline__ void p1_columns(const T* st, int ntp, int nc, int cc,
 // MAP 1: one lane per column (two lanes, each half the rows, when a chunk has
 // only 16 columns), the item's x tile in the warp's shared-memory buffer:
 // no cross-lane reduction, VEC independent accumulator chains per lane.
-template <typename T, int NW, int NS, int SB, int MAP, bool DYN>
+template <typename T, int NW, int NS, int SB, int MAP, int SCHED>
 __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev m1, int nmat,
                                                                const double* __restrict__ x, int shape) {
   typedef typename AccT<T>::type Acc;
@@ -348,8 +382,18 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
     d.cc = d.ntp > 0 ? chunk_cols(d.ntp, ESZ, SB) : 16;
     return d;
   };
-  WarpSeq seq = warp_seq(m0, m1, nmat, 1, shape, gw, GW, n0, ntot);
-  if constexpr (DYN) seq.make_dynamic(m0.dyn + 0, R.hist);
+  WarpSeq seq;
+  if constexpr (SCHED == 3) {
+    // the block's list, shared by its warps through a counter
+    if (threadIdx.x == 0) *R.bctr = 0;
+    __syncthreads();
+    seq = warp_seq(m0, m1, nmat, 1, shape, blockIdx.x, gridDim.x, n0, ntot);
+    if (seq.a0) seq.make_block_shared(R.bctr, R.hist);
+    else seq = warp_seq(m0, m1, nmat, 1, shape, gw, GW, n0, ntot);
+  } else {
+    seq = warp_seq(m0, m1, nmat, 1, shape, gw, GW, n0, ntot);
+  }
+  if constexpr (SCHED == 2) seq.make_dynamic(m0.dyn + 0, R.hist);
   int* const exits = m0.dyn + 1;
   // producer: walks this warp's items chunk by chunk, NS chunks ahead; the
   // item ids are fetched two items ahead, the descriptors one
@@ -580,7 +624,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
 // or more stages: the indices of chunk c + 2 are in the FIFO when chunk c
 // starts); two register sets of multipliers then cover two chunk times of
 // load latency.
-template <typename T, int NW, int NS, int SB, int GA, bool DYN>
+template <typename T, int NW, int NS, int SB, int GA, int SCHED>
 __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev m1, int nmat,
                                                                const double* __restrict__ x, int shape) {
   typedef typename AccT<T>::type Acc;
@@ -616,8 +660,18 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
     int32_t idx[KP];
     int nc, sec;
   };
-  WarpSeq seq = warp_seq(m0, m1, nmat, 2, shape, gw, GW, n0, ntot);
-  if constexpr (DYN) seq.make_dynamic(m0.dyn + 2, R.hist);
+  WarpSeq seq;
+  if constexpr (SCHED == 3) {
+    // the block's list, shared by its warps through a counter
+    if (threadIdx.x == 0) *R.bctr = 0;
+    __syncthreads();
+    seq = warp_seq(m0, m1, nmat, 2, shape, blockIdx.x, gridDim.x, n0, ntot);
+    if (seq.a0) seq.make_block_shared(R.bctr, R.hist);
+    else seq = warp_seq(m0, m1, nmat, 2, shape, gw, GW, n0, ntot);
+  } else {
+    seq = warp_seq(m0, m1, nmat, 2, shape, gw, GW, n0, ntot);
+  }
+  if constexpr (SCHED == 2) seq.make_dynamic(m0.dyn + 2, R.hist);
   int* const exits = m0.dyn + 3;
   int p_k = 0, p_it = seq.at(0), p_itn = seq.at(1), p_itnn = seq.at(2), p_c0 = 0, p_seq = 0;
   S2ItemDev Dp = current(desc(p_it)), Dpn = desc(p_itn);
@@ -801,7 +855,7 @@ namespace {
 // block's shared memory: NW x NS x SB + multipliers + barriers
 template <int NW, int NS, int SB>
 constexpr size_t smem_bytes() {
-  return (size_t)NW * NS * SB + (size_t)NW * kMu + (size_t)NW * NS * 8 + (size_t)NW * kHist * 4;
+  return (size_t)NW * NS * SB + (size_t)NW * kMu + (size_t)NW * NS * 8 + (size_t)NW * kHist * 4 + 16;
 }
 
 template <typename K>
@@ -838,7 +892,7 @@ void launch_p1s(const MatDev& m0, const MatDev& m1, int nmat, const double* x, i
   // launch): a phase-1 block needs nearly all of an SM's registers, and one
   // started early would keep the rest of the previous stage's phase-3 blocks
   // off its SM
-  launch_kernel(p1_stream_kernel<T, NW, NS, SB, MAP, kShapes1[S].sched == 2>, dim3(grid), dim3(NW * 32),
+  launch_kernel(p1_stream_kernel<T, NW, NS, SB, MAP, kShapes1[S].sched>, dim3(grid), dim3(NW * 32),
                 smem_bytes<NW, NS, SB>(), st, false, m0, m1, nmat, x, S);
 }
 
@@ -847,7 +901,7 @@ void launch_p2s(const MatDev& m0, const MatDev& m1, int nmat, const double* x, i
   constexpr int NW = kShapes2[S].nw, NS = kShapes2[S].ns, SB = kShapes2[S].sb, GA = kShapes2[S].map + 1;
   const int need = (n + NW - 1) / NW;
   const int grid = need < sm ? (need > 0 ? need : 1) : sm;
-  launch_kernel(p2_stream_kernel<T, NW, NS, SB, GA, kShapes2[S].sched == 2>, dim3(grid), dim3(NW * 32),
+  launch_kernel(p2_stream_kernel<T, NW, NS, SB, GA, kShapes2[S].sched>, dim3(grid), dim3(NW * 32),
                 smem_bytes<NW, NS, SB>(), st, pdl_enabled(), m0, m1, nmat, x, S);
 }
 
@@ -856,7 +910,7 @@ void launch_typed(int phase, int shape, const MatDev& m0, const MatDev& m1, int 
                   cudaStream_t st) {
   const int n = phase == 1 ? m0.ns1 + (nmat == 2 ? m1.ns1 : 0) : m0.ns2 + (nmat == 2 ? m1.ns2 : 0);
   if (n == 0) return;
-  static_assert(kNumShapes1 == 9 && kNumShapes2 == 7, "one case per shape");
+  static_assert(kNumShapes1 == 10 && kNumShapes2 == 8, "one case per shape");
   if (phase == 1) {
     switch (shape) {
       case 1: launch_p1s<T, 1>(m0, m1, nmat, x, sm, n, st); break;
@@ -867,6 +921,7 @@ void launch_typed(int phase, int shape, const MatDev& m0, const MatDev& m1, int 
       case 6: launch_p1s<T, 6>(m0, m1, nmat, x, sm, n, st); break;
       case 7: launch_p1s<T, 7>(m0, m1, nmat, x, sm, n, st); break;
       case 8: launch_p1s<T, 8>(m0, m1, nmat, x, sm, n, st); break;
+      case 9: launch_p1s<T, 9>(m0, m1, nmat, x, sm, n, st); break;
       default: launch_p1s<T, 0>(m0, m1, nmat, x, sm, n, st);
     }
   } else {
@@ -877,6 +932,7 @@ void launch_typed(int phase, int shape, const MatDev& m0, const MatDev& m1, int 
       case 4: launch_p2s<T, 4>(m0, m1, nmat, x, sm, n, st); break;
       case 5: launch_p2s<T, 5>(m0, m1, nmat, x, sm, n, st); break;
       case 6: launch_p2s<T, 6>(m0, m1, nmat, x, sm, n, st); break;
+      case 7: launch_p2s<T, 7>(m0, m1, nmat, x, sm, n, st); break;
       default: launch_p2s<T, 0>(m0, m1, nmat, x, sm, n, st);
     }
   }
@@ -886,14 +942,14 @@ template <typename T, int S>
 void prepare_p1() {
   constexpr int NW = kShapes1[S].nw, NS = kShapes1[S].ns, SB = kShapes1[S].sb, MAP = kShapes1[S].map;
   static_assert(smem_bytes<NW, NS, SB>() <= 227 * 1024, "shape exceeds the shared memory of a block");
-  set_smem_once(p1_stream_kernel<T, NW, NS, SB, MAP, kShapes1[S].sched == 2>, smem_bytes<NW, NS, SB>());
+  set_smem_once(p1_stream_kernel<T, NW, NS, SB, MAP, kShapes1[S].sched>, smem_bytes<NW, NS, SB>());
 }
 
 template <typename T, int S>
 void prepare_p2() {
   constexpr int NW = kShapes2[S].nw, NS = kShapes2[S].ns, SB = kShapes2[S].sb, GA = kShapes2[S].map + 1;
   static_assert(smem_bytes<NW, NS, SB>() <= 227 * 1024, "shape exceeds the shared memory of a block");
-  set_smem_once(p2_stream_kernel<T, NW, NS, SB, GA, kShapes2[S].sched == 2>, smem_bytes<NW, NS, SB>());
+  set_smem_once(p2_stream_kernel<T, NW, NS, SB, GA, kShapes2[S].sched>, smem_bytes<NW, NS, SB>());
 }
 
 template <typename T>
@@ -907,6 +963,7 @@ void prepare_type() {
   prepare_p1<T, 6>();
   prepare_p1<T, 7>();
   prepare_p1<T, 8>();
+  prepare_p1<T, 9>();
   prepare_p2<T, 0>();
   prepare_p2<T, 1>();
   prepare_p2<T, 2>();
@@ -914,6 +971,7 @@ void prepare_type() {
   prepare_p2<T, 4>();
   prepare_p2<T, 5>();
   prepare_p2<T, 6>();
+  prepare_p2<T, 7>();
 }
 
 }  // namespace

@@ -195,8 +195,9 @@ int hbi_adot_lattice_hyp_phase_dev(double* d_au, hbi_lhp* st_LHp, const double* 
  * many chunks ahead the multipliers are gathered, minus one), schedule (0 =
  * items over all warps longest first, 1 = per block a run of items
  * consecutive in the store, see hbi_plan_block_schedule, 2 = dynamic: each
- * warp takes the next item from a counter when it needs one) (shapes5 may
- * be NULL) */
+ * warp takes the next item from a counter when it needs one, 3 = items dealt
+ * over the blocks, each block's warps taking them from a shared counter)
+ * (shapes5 may be NULL) */
 int hbi_stream_shapes(int phase, int* count, int* shapes5);
 /* the shapes chosen for phases 1 and 2, the median time in microseconds of
  * every shape (phase 1's shapes, then phase 2's; -1 if not timed) and how

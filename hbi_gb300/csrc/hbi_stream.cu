@@ -287,11 +287,63 @@ __device__ __forceinline__ WarpSeq warp_seq(const MatDev& m0, const MatDev& m1, 
 // x tile (32 x VEC values); put(cl, sum) receives chunk column cl.  With 16
 // columns per chunk, lanes L and L + 16 take halves of column L's vectors
 // (their logical indices; the swizzle permutes within the column).
+// the VEC x values of logical vector k of the x tile, as 16-byte loads
+__device__ __forceinline__ void ldx(const float* xs, int k, float (&o)[4]) {
+  const float4 v = reinterpret_cast<const float4*>(xs)[k];
+  o[0] = v.x;
+  o[1] = v.y;
+  o[2] = v.z;
+  o[3] = v.w;
+}
+__device__ __forceinline__ void ldx(const double* xs, int k, double (&o)[2]) {
+  const double2 v = reinterpret_cast<const double2*>(xs)[k];
+  o[0] = v.x;
+  o[1] = v.y;
+}
+__device__ __forceinline__ void ldx(const float* xs, int k, float (&o)[8]) {
+  const float4 a = reinterpret_cast<const float4*>(xs)[2 * k], b = reinterpret_cast<const float4*>(xs)[2 * k + 1];
+  o[0] = a.x;
+  o[1] = a.y;
+  o[2] = a.z;
+  o[3] = a.w;
+  o[4] = b.x;
+  o[5] = b.y;
+  o[6] = b.z;
+  o[7] = b.w;
+}
+
 template <typename T, typename Acc, typename Put>
 __device__ __forceinline__ void p1_columns(const T* st, int ntp, int nc, int cc, const Acc* xs, int lane, Put put) {
   constexpr int VEC = 16 / sizeof(T);
   const int nq = ntp / VEC;  // 16-byte vectors per column segment
-  if (cc <= 16) {
+  if (cc <= 16 && nq == 32) {
+    // full-height segments (512 bytes), 16 per chunk: lane L + 16h sums
+    // logical vectors 16h .. 16h + 15 of column L.  The swizzle of column L
+    // is L & 7 and permutes within aligned groups of eight, so the eight
+    // physical offsets are computed once and the loop is fully unrolled.
+    const int h = lane >> 4, cl = lane & 15;
+    Acc acc[VEC];
+#pragma unroll
+    for (int v = 0; v < VEC; v++) acc[v] = 0;
+    if (cl < nc) {
+      const T* cp = st + cl * ntp + 16 * h * VEC;
+      const int sw = cl & 7;
+      const Acc* xh = xs + 16 * h * VEC;
+#pragma unroll
+      for (int i = 0; i < 16; i++) {
+        Acc a[VEC], xv[VEC];
+        lds16(cp + ((i & 8) + ((i & 7) ^ sw)) * VEC, a);
+        ldx(xh, i, xv);
+#pragma unroll
+        for (int v = 0; v < VEC; v++) acc[v] += a[v] * xv[v];
+      }
+    }
+    Acc t = acc[0];
+#pragma unroll
+    for (int v = 1; v < VEC; v++) t += acc[v];
+    t += __shfl_xor_sync(0xffffffffu, t, 16);
+    if (h == 0 && cl < nc) put(cl, t);
+  } else if (cc <= 16) {
     const int h = lane >> 4, cl = lane & 15;
     const int half = (nq + 1) >> 1;
     const int k0 = h ? half : 0, k1 = h ? nq : half;
@@ -765,7 +817,41 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
     const int nq = Dc.ntp / VEC;
     const int lw = log2ceil(nq), LW = 1 << lw, CS = 32 >> lw;
     const int slot = lane >> lw, j = lane & (LW - 1);
-    if (j < nq) {
+    if (nq == 32 && nc == 16) {
+      // a full chunk of full-height segments (16 columns of 512 bytes): the
+      // same sums as below, unrolled, the multipliers read as 16-byte vectors
+      Acc acc2[VEC], m16[16];
+#pragma unroll
+      for (int v = 0; v < VEC; v++) acc2[v] = 0;
+#pragma unroll
+      for (int c = 0; c < 16; c += 16 / sizeof(Acc)) {
+        if constexpr (sizeof(Acc) == 4) {
+          const float4 q = reinterpret_cast<const float4*>(musm)[c / 4];
+          m16[c] = q.x;
+          m16[c + 1] = q.y;
+          m16[c + 2] = q.z;
+          m16[c + 3] = q.w;
+        } else {
+          const double2 q = reinterpret_cast<const double2*>(musm)[c / 2];
+          m16[c] = q.x;
+          m16[c + 1] = q.y;
+        }
+      }
+      const T* sj = st + j * VEC;
+#pragma unroll
+      for (int c = 0; c < 16; c += 2) {
+        Acc a[VEC], b[VEC];
+        lds16(sj + c * (32 * VEC), a);
+        lds16(sj + (c + 1) * (32 * VEC), b);
+#pragma unroll
+        for (int v = 0; v < VEC; v++) {
+          acc[v] += a[v] * m16[c];
+          acc2[v] += b[v] * m16[c + 1];
+        }
+      }
+#pragma unroll
+      for (int v = 0; v < VEC; v++) acc[v] += acc2[v];
+    } else if (j < nq) {
       // two accumulator sets over alternating columns: independent FMA chains
       Acc acc2[VEC];
 #pragma unroll

@@ -84,6 +84,26 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
       : "memory");
 }
 
+// L2 policy for data read once per product: evicted first, so that the
+// factor stream (~1 GB per stage of an RK attempt, against a 126 MB L2) does
+// not push out the small data every launch reads -- schedules, item
+// descriptors, x, z, partial sums
+__device__ __forceinline__ uint64_t l2_evict_first() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+
+// bulk copy of streamed factor data, with that policy
+__device__ __forceinline__ void bulk_g2s_stream(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
+                                                uint64_t pol) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+          saddr(dst)),
+      "l"(src), "r"(bytes), "r"(saddr(bar)), "l"(pol)
+      : "memory");
+}
+
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
@@ -460,7 +480,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
       const T* src = (const T*)(p_it < n0 ? m0.vstore : m1.vstore) + Dp.soff + (int64_t)p_c0 * Dp.ntp;
       fence_proxy_async();
       mbar_expect_tx(&R.bar[s], bytes);
-      bulk_g2s(R.buf + s * SB, src, bytes, &R.bar[s]);
+      bulk_g2s_stream(R.buf + s * SB, src, bytes, &R.bar[s], l2_evict_first());
     }
     p_seq++;
     p_c0 += nc;
@@ -741,7 +761,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
       const T* src = (const T*)PM.ustore + Dp.soff + (int64_t)p_c0 * Dp.ntp;
       fence_proxy_async();
       mbar_expect_tx(&R.bar[s], bytes);
-      bulk_g2s(R.buf + s * SB, src, bytes, &R.bar[s]);
+      bulk_g2s_stream(R.buf + s * SB, src, bytes, &R.bar[s], l2_evict_first());
     }
 #pragma unroll
     for (int i = 0; i < KP; i++) {

@@ -104,6 +104,16 @@ __device__ __forceinline__ void bulk(void* dst, const void* src, uint32_t bytes,
                "l"(src), "r"(bytes), "r"(sa(b))
                : "memory");
 }
+// factor chunks are read once per product: evicted first from L2
+__device__ __forceinline__ void bulk_stream(void* dst, const void* src, uint32_t bytes, uint64_t* b) {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+          sa(dst)),
+      "l"(src), "r"(bytes), "r"(sa(b)), "l"(pol)
+      : "memory");
+}
 __device__ __forceinline__ void fence_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 // block-wide bounded wait; false (and the error word set) on time-out
@@ -181,7 +191,7 @@ __global__ void __launch_bounds__(256, 2) p1e_kernel(EnsMat A, EnsMat B, int nma
       const float* src = (const float*)(p_it < n0 ? A.m.vstore : B.m.vstore) + Dp.soff + (int64_t)p_c0 * Dp.ntp;
       fence_async();
       bar_expect(&bar[s], bytes);
-      bulk(cs[s], src, bytes, &bar[s]);
+      bulk_stream(cs[s], src, bytes, &bar[s]);
     }
     p_seq++;
     p_c0 += nc;
@@ -321,7 +331,7 @@ __global__ void __launch_bounds__(256, 2) p2e_kernel(EnsMat A, EnsMat B, int nma
       if (lane == 0) {
         fence_async();
         bar_expect(&bar[s], (uint32_t)(nc * Dp.ntp * 4 + nc * EM * 4));
-        bulk(st[s], (const float*)PM.m.ustore + Dp.soff + (int64_t)p_c0 * Dp.ntp, (uint32_t)(nc * Dp.ntp * 4),
+        bulk_stream(st[s], (const float*)PM.m.ustore + Dp.soff + (int64_t)p_c0 * Dp.ntp, (uint32_t)(nc * Dp.ntp * 4),
              &bar[s]);
       }
       __syncwarp();

@@ -100,6 +100,17 @@ __device__ __forceinline__ void bcopy(void* dst, const void* src, uint32_t bytes
                "l"(src), "r"(bytes), "r"(sa(b))
                : "memory");
 }
+// factor chunks are read once per product: evicted first from L2, so that
+// z, X and the schedules stay resident
+__device__ __forceinline__ void bcopy_stream(void* dst, const void* src, uint32_t bytes, uint64_t* b) {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+          sa(dst)),
+      "l"(src), "r"(bytes), "r"(sa(b)), "l"(pol)
+      : "memory");
+}
 __device__ __forceinline__ void fasync() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void group_sync() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
 __device__ __forceinline__ int arrive_ar(int* p) {
@@ -219,7 +230,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
       if (lane == 0) {
         fasync();
         bexpect(&br->full[s], fbytes + (uint32_t)(nrow * EMT * 4));
-        bcopy(stg, fsrc, fbytes, &br->full[s]);
+        bcopy_stream(stg, fsrc, fbytes, &br->full[s]);
         if (PH == 1 && nrow > 0)
           bcopy(stg + kFac, X + (int64_t)(D.m0 + k0) * EMT, (uint32_t)(nrow * EMT * 4), &br->full[s]);
       }

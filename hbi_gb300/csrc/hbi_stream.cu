@@ -104,7 +104,6 @@ __device__ __forceinline__ void bulk_g2s_stream(void* dst, const void* src, uint
       : "memory");
 }
 
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
 // one 16-byte vector of shared memory as VEC accumulator values
@@ -478,7 +477,9 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
     if (lane == 0) {
       const uint32_t bytes = (uint32_t)(nc * Dp.ntp * ESZ);
       const T* src = (const T*)(p_it < n0 ? m0.vstore : m1.vstore) + Dp.soff + (int64_t)p_c0 * Dp.ntp;
-      fence_proxy_async();
+      // no proxy fence: the stage's only generic accesses are this warp's
+      // loads of its previous chunk, whose values were consumed (sums and
+      // stores issued, __syncwarp) before the copy that overwrites it
       mbar_expect_tx(&R.bar[s], bytes);
       bulk_g2s_stream(R.buf + s * SB, src, bytes, &R.bar[s], l2_evict_first());
     }
@@ -759,7 +760,8 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
     if (lane == 0) {
       const uint32_t bytes = (uint32_t)(nc * Dp.ntp * ESZ);
       const T* src = (const T*)PM.ustore + Dp.soff + (int64_t)p_c0 * Dp.ntp;
-      fence_proxy_async();
+      // no proxy fence: as in phase 1, the stage's previous contents were
+      // loaded and consumed before the copy that overwrites them
       mbar_expect_tx(&R.bar[s], bytes);
       bulk_g2s_stream(R.buf + s * SB, src, bytes, &R.bar[s], l2_evict_first());
     }

@@ -227,8 +227,11 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
       unsigned char* stg = stage(s);
       const uint32_t fbytes = (uint32_t)((kc / 16) * D.np * 64);
       const __nv_bfloat16* fsrc = (PH == 1 ? M.s1 : M.s2) + D.soff + (int64_t)(k0 / 16) * D.np * 32;
+      // no proxy fence before the copies: the factor region was last read by
+      // the MMAs (the same async proxy, ordered by the empty barrier) and the
+      // rows region by the converters, whose loads were consumed before they
+      // arrived
       if (lane == 0) {
-        fasync();
         bexpect(&br->full[s], fbytes + (uint32_t)(nrow * EMT * 4));
         bcopy_stream(stg, fsrc, fbytes, &br->full[s]);
         if (PH == 1 && nrow > 0)
@@ -247,7 +250,6 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
           const unsigned above = heads & ~((2u << lane) - 1u);
           const int len = (above ? __ffs(above) - 1 : nrow) - lane;
           const float* src = mi >= 0 ? M.z + (int64_t)mi * EMT : X + (int64_t)(-mi - 1) * EMT;
-          fasync();
           bcopy(stg + kFac + lane * EMT * 4, src, (uint32_t)(len * EMT * 4), &br->full[s]);
         }
       }

@@ -331,15 +331,10 @@ __device__ __forceinline__ void ldx(const float* xs, int k, float (&o)[8]) {
   o[7] = b.w;
 }
 
-// hold (optional): for full chunks of full-height segments the sum is not
-// stored but returned in *hold, its chunk column in *hcol (-1: none in this
-// lane), so that the caller can order the store after other work
 template <typename T, typename Acc, typename Put>
-__device__ __forceinline__ void p1_columns(const T* st, int ntp, int nc, int cc, const Acc* xs, int lane, Put put,
-                                           Acc* hold = nullptr, int* hcol = nullptr) {
+__device__ __forceinline__ void p1_columns(const T* st, int ntp, int nc, int cc, const Acc* xs, int lane, Put put) {
   constexpr int VEC = 16 / sizeof(T);
   const int nq = ntp / VEC;  // 16-byte vectors per column segment
-  if (hcol) *hcol = -1;
   if (cc <= 16 && nq == 32) {
     // full-height segments (512 bytes), 16 per chunk: lane L + 16h sums
     // logical vectors 16h .. 16h + 15 of column L.  The swizzle of column L
@@ -366,14 +361,7 @@ __device__ __forceinline__ void p1_columns(const T* st, int ntp, int nc, int cc,
 #pragma unroll
     for (int v = 1; v < VEC; v++) t += acc[v];
     t += __shfl_xor_sync(0xffffffffu, t, 16);
-    if (h == 0 && cl < nc) {
-      if (hold) {
-        *hold = t;
-        *hcol = cl;
-      } else {
-        put(cl, t);
-      }
-    }
+    if (h == 0 && cl < nc) put(cl, t);
   } else if (cc <= 16) {
     const int h = lane >> 4, cl = lane & 15;
     const int half = (nq + 1) >> 1;
@@ -544,29 +532,9 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
   load_x(Dc, xc);
   load_x(Dn, xn);
   put_x(xc);
-  // A finished multi-tile item arrives (acq_rel atomic on its group's
-  // counter) after the next chunk's sums, before that chunk's stores: the
-  // release then covers only stores at least a chunk old, which have landed,
-  // instead of waiting for the item's last stores.  The arrival is resolved
-  // one chunk later again, so that the atomic's round trip overlaps a chunk.
-  int arr_cg = -1, arr_ntile = 0, arr_ncols = 0, arr_poff = 0, arr_z0 = 0, arr_sec = 0;
+  // the arrival of a finished multi-tile item is resolved one chunk later, so
+  // that the atomic's round trip overlaps the next chunk
   int pend_old = 0, pend_cg = -1, pend_ntile = 0, pend_ncols = 0, pend_poff = 0, pend_z0 = 0, pend_sec = 0;
-  // the deferred arrival: returns the atomic's result (lane 0)
-  auto arrive_now = [&]() -> int {
-    int old = 0;
-    if (lane == 0) old = arrive_acq_rel(&(arr_sec ? m1 : m0).cnt[arr_cg]);
-    return old;
-  };
-  auto shift_arrival = [&](int old) {
-    pend_old = old;
-    pend_cg = arr_cg;
-    pend_ntile = arr_ntile;
-    pend_ncols = arr_ncols;
-    pend_poff = arr_poff;
-    pend_z0 = arr_z0;
-    pend_sec = arr_sec;
-    arr_cg = -1;
-  };
   auto resolve = [&]() {
     if (pend_cg < 0) return;
     const int last = __shfl_sync(0xffffffffu, pend_old == pend_ntile - 1 ? 1 : 0, 0);
@@ -602,10 +570,8 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
       if (Dc.ntile == 1) z[Dc.z0 + col] = v;
       else part[Dc.poff + (int64_t)Dc.tile * Dc.ncols + col] = v;
     };
-    Acc hold = 0;
-    int hcol = -1;
     if constexpr (MAP == 1) {
-      p1_columns<T>(st, Dc.ntp, nc, Dc.cc, xs, lane, [&](int cl, Acc v) { put(c_c0 + cl, v); }, &hold, &hcol);
+      p1_columns<T>(st, Dc.ntp, nc, Dc.cc, xs, lane, [&](int cl, Acc v) { put(c_c0 + cl, v); });
     } else {
       const int lw = log2ceil(nq), LW = 1 << lw, CS = 32 >> lw;
       const int slot = lane >> lw, j = lane & (LW - 1);
@@ -683,27 +649,22 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
       }
     }
     __syncwarp();
-    {
-      const bool arrive = arr_cg >= 0;
-      const int old = arrive ? arrive_now() : 0;
-      resolve();
-      if (arrive) shift_arrival(old);
-    }
-    if (hcol >= 0) put(c_c0 + hcol, hold);
     c_seq++;
     produce();
+    resolve();
     c_c0 += nc;
     if (c_c0 < Dc.ncols) continue;
     // item done: the last row tile of a column group to arrive sums the
-    // tiles in order (arrival after the next chunk, resolved after the one
-    // after)
+    // tiles in order (resolved after the next chunk)
     if (Dc.ntile > 1) {
-      arr_cg = Dc.cg;
-      arr_ntile = Dc.ntile;
-      arr_ncols = Dc.ncols;
-      arr_poff = Dc.poff;
-      arr_z0 = Dc.z0;
-      arr_sec = sec;
+      __syncwarp();
+      if (lane == 0) pend_old = arrive_acq_rel(&M.cnt[Dc.cg]);
+      pend_cg = Dc.cg;
+      pend_ntile = Dc.ntile;
+      pend_ncols = Dc.ncols;
+      pend_poff = Dc.poff;
+      pend_z0 = Dc.z0;
+      pend_sec = sec;
     }
     c_k++;
     c_it = c_i1;
@@ -718,12 +679,6 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
     put_x(xc);
     load_x(Dn, xn);
     Dnn = desc(c_i2);
-  }
-  __syncwarp();
-  if (arr_cg >= 0) {
-    const int old = arrive_now();
-    resolve();
-    shift_arrival(old);
   }
   resolve();
   dyn_leave(seq, exits, GW);

@@ -125,7 +125,8 @@ class Clocks:
 # H-matrix, from the ncu captures summarised under profiles/ (one entry per
 # factor storage that has been captured)
 NCU_TRAFFIC = {
-    "f32": {"phase1": 330.0e6, "phase2": 378.6e6, "source": "profiles/matvec_p1_p2_c2_256x256_f32.md"},
+    "f32": {"phase1": 327.2e6, "phase2": 376.6e6, "source": "profiles/matvec_p1_p2_c2_256x256_f32.md"},
+    "f64": {"phase1": 651.7e6, "phase2": 738.5e6, "source": "profiles/matvec_p1_p2_c2_256x256_f32.md (FP64 lines)"},
 }
 
 
@@ -205,11 +206,17 @@ def run_ensemble_mode(args):
     b_in, dc_m = configs.ensemble_params(64, seed=0)
     y, vel, b, dc, p = configs.ensemble_state(w, lodc, b_in, dc_m)
     T = args.window_yr * H.YEAR
-    res = {}
+    res, prod_ms = {}, {}
+    # algorithmic bytes of one multi-vector product: both factor stores once,
+    # the 64 members' input vectors, both outputs
+    prod_bytes = lh_s.info()["store_bytes"] + lh_n.info()["store_bytes"] + 3 * n * 64 * 4
+    X = np.random.default_rng(0).standard_normal((n, 64)).astype(np.float32)
     for product in ("cuda-cores", "tcgen05"):
         ens = H.Ensemble(lh_s, lh_n, b, dc, evlaw=w.evlaw, scale=w.scale, a=p["a"], f0=p["f0"], vpl=p["vpl"])
         if product == "tcgen05":
             ens.use_tensor_cores(lf_s, lf_n)
+        ens.product(X, reps=3)
+        prod_ms[product] = ens.product(X, reps=20)[2]
         ens.set_state(y, vel)
         st = ens.run(T, eps_r=1e-6)
         ye, se, xe = ens.get_state()
@@ -234,7 +241,12 @@ def run_ensemble_mode(args):
               "member0_state_rel_diff": float(np.linalg.norm(ye[:, 0] - y1) / np.linalg.norm(y1)),
               "product": "tcgen05 (BF16 hi+lo, FP32 accumulation in tensor memory)",
               "cuda_core_product_ms_per_attempt": round(res["cuda-cores"][0]["wall_s"] /
-                                                        max(1, res["cuda-cores"][0]["attempts"]) * 1e3, 3)})
+                                                        max(1, res["cuda-cores"][0]["attempts"]) * 1e3, 3),
+              "product_ms": {k: round(v, 4) for k, v in prod_ms.items()},
+              "product_gbs": {k: round(prod_bytes / (v * 1e-3) / 1e9, 1) for k, v in prod_ms.items()},
+              "product_bytes": prod_bytes,
+              "product_frac_of_hbm": {k: round(prod_bytes / (v * 1e-3) / 1e9 / peaks()[0], 3)
+                                      for k, v in prod_ms.items()}})
 
 
 # ------------------------------------------------------------ time loops

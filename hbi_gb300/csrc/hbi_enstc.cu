@@ -37,7 +37,7 @@ constexpr int kFac = (KC / 16) * 256 * 64;   // factor hi + lo of a stage, N <= 
 constexpr int kRows = KC * EMT * 4;          // the members' FP32 rows: 8 KB
 constexpr int kMem = (KC / 16) * 4096;       // the members' operand, hi + lo: 8 KB
 constexpr int kStage = kFac + kRows + kMem;  // 48 KB
-constexpr int kThreads = 320;                // producer, MMA, 4 converter and 4 epilogue warps
+constexpr int kThreads = 352;                // producer, MMA, 4 converter, 4 epilogue warps, producer
 constexpr uint32_t kTmemCols = 256;          // two accumulators x two 128-row blocks x 64 members
 constexpr long long kWaitT = 2LL << 30;
 
@@ -120,17 +120,18 @@ __device__ __forceinline__ int arrive_ar(int* p) {
 }
 
 // One block per SM, four roles working on a ring of NST stages:
-//   warp 0        producer: bulk copies of the factor tile's chunks (BF16 hi
-//                 and lo halves, canonical K-major) and of the members' FP32
-//                 rows (phase 1: rows m0 + k of X; phase 2: one gathered row of
-//                 z or X per column);
+//   warps 0, 10   producers, taking the stages in turn: bulk copies of the
+//                 factor tile's chunks (BF16 hi and lo halves, canonical
+//                 K-major) and of the members' FP32 rows (phase 1: rows
+//                 m0 + k of X; phase 2: the multiplier rows of z or X, one
+//                 copy per run of consecutive rows);
 //   warps 2-5     converters: the FP32 rows to BF16 hi / lo in the canonical
 //                 K-major layout of the MMA's B operand (member, k);
 //   warp 1        MMA: one thread issues, per 16-K chunk and 128-row block of
 //                 the item, D += F_hi M_hi + F_hi M_lo + F_lo M_hi (M = 128
 //                 factor rows, N = 64 members, K = 16; the lo x lo term is
 //                 below FP32 resolution) into one of two tensor-memory
-//                 accumulators, and commits each stage back to the producer;
+//                 accumulators, and commits each stage back to its producer;
 //   warps 6-9     epilogue: read a finished accumulator (tcgen05.ld, one
 //                 thread per factor row, 64 members) and write the item's
 //                 rows, while the MMAs of the next item run in the other
@@ -203,22 +204,36 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
     w.itnn = w.j + 2 < nit ? item_at(w.j + 2) : 0;
   };
 
-  if (warp == 0) {
-    // ---------------------------------------------------------- producer
+  if (warp == 0 || warp == 10) {
+    // --------------------------------------------------------- producers
+    // two producer warps take the stages in turn (stage q: producer q mod
+    // 2); issuing a stage's copies costs a warp about a thousand cycles
+    const int pi = warp == 0 ? 0 : 1;
     Walk W;
     walk_init(W);
     int q = 0, k0 = 0;
-    // phase 2: this stage's column indices, loaded one stage ahead
+    // phase 2: this stage's column indices
     auto load_midx = [&]() -> int {
       const int nrow = max(0, min(KC, W.D.kv - k0));
       const TcMat& M = W.it < n0 ? A : B;
       return (PH == 2 && W.j < nit && lane < nrow) ? __ldg(&M.midx[W.D.m0 + k0 + lane]) : 0;
     };
-    int mi = load_midx();
+    int mi = pi == 0 ? load_midx() : 0;
     while (W.j < nit) {
       const TcItem& D = W.D;
       const TcMat& M = W.it < n0 ? A : B;
       const int s = q % NST;
+      if ((q & 1) != pi) {
+        // the other producer's stage: only the walk advances
+        q++;
+        k0 += KC;
+        if (k0 >= D.kp) {
+          k0 = 0;
+          walk_next(W);
+        }
+        if ((q & 1) == pi) mi = load_midx();
+        continue;
+      }
       int w = 1;
       if (q >= NST && lane == 0) w = rwait(&br->empty[s], (uint32_t)((q / NST - 1) & 1), br, A.err);
       if (!__shfl_sync(0xffffffffu, w, 0)) break;
@@ -259,12 +274,13 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
         k0 = 0;
         walk_next(W);
       }
-      mi = load_midx();
+      if ((q & 1) == pi) mi = load_midx();
     }
-    // the copies still in flight land before the block leaves (the last NST
-    // issued are the only ones whose phase can still be open)
+    // this producer's copies still in flight land before the block leaves
+    // (the last NST stages are the only ones whose phase can still be open)
     if (lane == 0)
-      for (int r = max(0, q - NST); r < q; r++) bwait(&br->full[r % NST], (uint32_t)((r / NST) & 1));
+      for (int r = max(0, q - NST); r < q; r++)
+        if ((r & 1) == pi) bwait(&br->full[r % NST], (uint32_t)((r / NST) & 1));
     __syncwarp();
   } else if (warp == 1) {
     // --------------------------------------------------------------- MMA
@@ -364,7 +380,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
       }
     }
     __syncwarp();
-  } else {
+  } else if (warp < 10) {
     // ---------------------------------------------------------- epilogue
     const int et = tid - 192, quad = warp & 3;
     Walk W;

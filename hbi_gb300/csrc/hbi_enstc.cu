@@ -37,7 +37,8 @@ constexpr int kFac = (KC / 16) * 256 * 64;   // factor hi + lo of a stage, N <= 
 constexpr int kRows = KC * EMT * 4;          // the members' FP32 rows: 8 KB
 constexpr int kMem = (KC / 16) * 4096;       // the members' operand, hi + lo: 8 KB
 constexpr int kStage = kFac + kRows + kMem;  // 48 KB
-constexpr int kThreads = 352;                // producer, MMA, 4 converter, 4 epilogue warps, producer
+constexpr int kProducers = 4;                // producer warps: 0, then 10 ..
+constexpr int kThreads = (10 + kProducers - 1) * 32;  // + MMA, 4 converter and 4 epilogue warps
 constexpr uint32_t kTmemCols = 256;          // two accumulators x two 128-row blocks x 64 members
 constexpr long long kWaitT = 2LL << 30;
 
@@ -120,7 +121,7 @@ __device__ __forceinline__ int arrive_ar(int* p) {
 }
 
 // One block per SM, four roles working on a ring of NST stages:
-//   warps 0, 10   producers, taking the stages in turn: bulk copies of the
+//   warps 0, 10+  producers, taking the stages in turn: bulk copies of the
 //                 factor tile's chunks (BF16 hi and lo halves, canonical
 //                 K-major) and of the members' FP32 rows (phase 1: rows
 //                 m0 + k of X; phase 2: the multiplier rows of z or X, one
@@ -204,11 +205,12 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
     w.itnn = w.j + 2 < nit ? item_at(w.j + 2) : 0;
   };
 
-  if (warp == 0 || warp == 10) {
+  if (warp == 0 || warp >= 10) {
     // --------------------------------------------------------- producers
-    // two producer warps take the stages in turn (stage q: producer q mod
-    // 2); issuing a stage's copies costs a warp about a thousand cycles
-    const int pi = warp == 0 ? 0 : 1;
+    // the producer warps take the stages in turn (stage q: producer q mod
+    // kProducers); issuing a stage's copies costs a warp about a thousand
+    // cycles
+    const int pi = warp == 0 ? 0 : warp - 9;
     Walk W;
     walk_init(W);
     int q = 0, k0 = 0;
@@ -223,7 +225,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
       const TcItem& D = W.D;
       const TcMat& M = W.it < n0 ? A : B;
       const int s = q % NST;
-      if ((q & 1) != pi) {
+      if (q % kProducers != pi) {
         // the other producer's stage: only the walk advances
         q++;
         k0 += KC;
@@ -231,7 +233,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
           k0 = 0;
           walk_next(W);
         }
-        if ((q & 1) == pi) mi = load_midx();
+        if (q % kProducers == pi) mi = load_midx();
         continue;
       }
       int w = 1;
@@ -274,13 +276,13 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
         k0 = 0;
         walk_next(W);
       }
-      if ((q & 1) == pi) mi = load_midx();
+      if (q % kProducers == pi) mi = load_midx();
     }
     // this producer's copies still in flight land before the block leaves
     // (the last NST stages are the only ones whose phase can still be open)
     if (lane == 0)
       for (int r = max(0, q - NST); r < q; r++)
-        if ((r & 1) == pi) bwait(&br->full[r % NST], (uint32_t)((r / NST) & 1));
+        if (r % kProducers == pi) bwait(&br->full[r % NST], (uint32_t)((r / NST) & 1));
     __syncwarp();
   } else if (warp == 1) {
     // --------------------------------------------------------------- MMA

@@ -37,12 +37,8 @@ constexpr int kFac = (KC / 16) * 256 * 64;   // factor hi + lo of a stage, N <= 
 constexpr int kRows = KC * EMT * 4;          // the members' FP32 rows: 8 KB
 constexpr int kMem = (KC / 16) * 4096;       // the members' operand, hi + lo: 8 KB
 constexpr int kStage = kFac + kRows + kMem;  // 48 KB
-constexpr int kProducers = 2;                // producer warps: 0, then 10 ..
-constexpr int kThreads = (10 + kProducers - 1) * 32;  // + MMA, 4 converter and 4 epilogue warps
-// tensor memory: two item buffers x two accumulators (hi x hi; hi x lo +
-// lo x hi) x two 128-row blocks x 64 members; buffer b's accumulator a of
-// block mb at column 256 b + 128 a + 64 mb
-constexpr uint32_t kTmemCols = 512;
+constexpr int kThreads = 352;                // producer, MMA, 4 converter, 4 epilogue warps, producer
+constexpr uint32_t kTmemCols = 256;          // two accumulators x two 128-row blocks x 64 members
 constexpr long long kWaitT = 2LL << 30;
 
 struct Bars {
@@ -124,7 +120,7 @@ __device__ __forceinline__ int arrive_ar(int* p) {
 }
 
 // One block per SM, four roles working on a ring of NST stages:
-//   warps 0, 10+  producers, taking the stages in turn: bulk copies of the
+//   warps 0, 10   producers, taking the stages in turn: bulk copies of the
 //                 factor tile's chunks (BF16 hi and lo halves, canonical
 //                 K-major) and of the members' FP32 rows (phase 1: rows
 //                 m0 + k of X; phase 2: the multiplier rows of z or X, one
@@ -208,12 +204,11 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
     w.itnn = w.j + 2 < nit ? item_at(w.j + 2) : 0;
   };
 
-  if (warp == 0 || warp >= 10) {
+  if (warp == 0 || warp == 10) {
     // --------------------------------------------------------- producers
-    // the producer warps take the stages in turn (stage q: producer q mod
-    // kProducers); issuing a stage's copies costs a warp about a thousand
-    // cycles
-    const int pi = warp == 0 ? 0 : warp - 9;
+    // two producer warps take the stages in turn (stage q: producer q mod
+    // 2); issuing a stage's copies costs a warp about a thousand cycles
+    const int pi = warp == 0 ? 0 : 1;
     Walk W;
     walk_init(W);
     int q = 0, k0 = 0;
@@ -228,7 +223,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
       const TcItem& D = W.D;
       const TcMat& M = W.it < n0 ? A : B;
       const int s = q % NST;
-      if (q % kProducers != pi) {
+      if ((q & 1) != pi) {
         // the other producer's stage: only the walk advances
         q++;
         k0 += KC;
@@ -236,7 +231,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
           k0 = 0;
           walk_next(W);
         }
-        if (q % kProducers == pi) mi = load_midx();
+        if ((q & 1) == pi) mi = load_midx();
         continue;
       }
       int w = 1;
@@ -279,13 +274,13 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
         k0 = 0;
         walk_next(W);
       }
-      if (q % kProducers == pi) mi = load_midx();
+      if ((q & 1) == pi) mi = load_midx();
     }
     // this producer's copies still in flight land before the block leaves
     // (the last NST stages are the only ones whose phase can still be open)
     if (lane == 0)
       for (int r = max(0, q - NST); r < q; r++)
-        if (r % kProducers == pi) bwait(&br->full[r % NST], (uint32_t)((r / NST) & 1));
+        if ((r & 1) == pi) bwait(&br->full[r % NST], (uint32_t)((r / NST) & 1));
     __syncwarp();
   } else if (warp == 1) {
     // --------------------------------------------------------------- MMA
@@ -313,29 +308,18 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
           umma::fence_after();
           const int kc = min(KC, D.kp - k0);
           const unsigned char* stg = stage(s);
-          // descriptors of the stage's first chunk; the next chunk, block and
-          // half are offsets of their start address field (16-byte units,
-          // all within the 14-bit field: shared memory is below 256 KB)
-          const uint64_t dm0 = umma::smem_desc(stg + kFac + kRows, 1024, 128);
-          const uint64_t df0 = umma::smem_desc(stg, (uint32_t)D.np * 16, 128);
-          const uint32_t fchunk = (uint32_t)D.np * 4, flo = (uint32_t)D.np * 2;  // np * 64 and np * 32 bytes
-          const uint32_t acc = (k0 > 0) ? 1u : 0u;
           for (int c = 0; c < kc / 16; c++) {
-            const uint64_t dmh = dm0 + (uint64_t)(c * 256), dml = dmh + 128;
-            const uint32_t first = (acc || c > 0) ? 1u : 0u;
-            // independent accumulators (hi x hi; the cross terms) and row
-            // blocks, issued side by side so that their MMAs overlap
+            const unsigned char* mem = stg + kFac + kRows + c * 4096;
+            const uint64_t dmh = umma::smem_desc(mem, 1024, 128);
+            const uint64_t dml = umma::smem_desc(mem + 2048, 1024, 128);
             for (int mb = 0; mb < nmb; mb++) {
-              const uint64_t dfh = df0 + (uint64_t)(c * fchunk + mb * 128);
-              umma::mma_bf16(tbase + (uint32_t)(b * 256 + mb * EMT), dfh, dmh, idesc, first);
-            }
-            for (int mb = 0; mb < nmb; mb++) {
-              const uint64_t dfh = df0 + (uint64_t)(c * fchunk + mb * 128);
-              umma::mma_bf16(tbase + (uint32_t)(b * 256 + 128 + mb * EMT), dfh, dml, idesc, first);
-            }
-            for (int mb = 0; mb < nmb; mb++) {
-              const uint64_t dfl = df0 + (uint64_t)(c * fchunk + mb * 128 + flo);
-              umma::mma_bf16(tbase + (uint32_t)(b * 256 + 128 + mb * EMT), dfl, dmh, idesc, 1);
+              const unsigned char* fac = stg + c * D.np * 64 + mb * 2048;
+              const uint64_t dfh = umma::smem_desc(fac, (uint32_t)D.np * 16, 128);
+              const uint64_t dfl = umma::smem_desc(fac + D.np * 32, (uint32_t)D.np * 16, 128);
+              const uint32_t d = tbase + (uint32_t)(b * 128 + mb * EMT);
+              umma::mma_bf16(d, dfh, dmh, idesc, (k0 > 0 || c > 0) ? 1 : 0);
+              umma::mma_bf16(d, dfh, dml, idesc, 1);
+              umma::mma_bf16(d, dfl, dmh, idesc, 1);
             }
           }
           umma::commit(&br->empty[s]);
@@ -415,34 +399,25 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
       const int nmb = (D.np + 127) / 128;
       for (int mb = 0; mb < nmb; mb++) {
         const int n = mb * 128 + 32 * quad + lane;  // factor row of this thread
-        const uint32_t taddr = tbase + ((uint32_t)(32 * quad) << 16) + (uint32_t)(b * 256 + mb * EMT);
-        float* dst = nullptr;
-        if (PH == 2) dst = M.gpart + ((int64_t)D.out0 + n) * EMT;
-        else if (D.ntile == 1) dst = M.z + ((int64_t)D.out0 + n) * EMT;
-        else dst = M.part + ((int64_t)D.poff + (int64_t)D.tile * D.nv + n) * EMT;
-        // 32 members at a time: hi x hi plus the cross terms
+        const uint32_t taddr = tbase + ((uint32_t)(32 * quad) << 16) + (uint32_t)(b * 128 + mb * EMT);
+        uint32_t v[4][16];
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
-          uint32_t v[2][16], u[2][16];
+        for (int c = 0; c < 4; c++) umma::ld_32x32b_x16_nowait(taddr + 16 * c, v[c]);
+        umma::wait_ld();
+        if (n < D.nv) {
+          float* dst;
+          if (PH == 2) dst = M.gpart + ((int64_t)D.out0 + n) * EMT;
+          else if (D.ntile == 1) dst = M.z + ((int64_t)D.out0 + n) * EMT;
+          else dst = M.part + ((int64_t)D.poff + (int64_t)D.tile * D.nv + n) * EMT;
 #pragma unroll
-          for (int c = 0; c < 2; c++) {
-            umma::ld_32x32b_x16_nowait(taddr + 32 * h + 16 * c, v[c]);
-            umma::ld_32x32b_x16_nowait(taddr + 128 + 32 * h + 16 * c, u[c]);
-          }
-          umma::wait_ld();
-          if (n < D.nv) {
+          for (int c = 0; c < 4; c++)
 #pragma unroll
-            for (int c = 0; c < 2; c++)
-#pragma unroll
-              for (int i = 0; i < 16; i += 4)
-                *reinterpret_cast<float4*>(dst + 32 * h + 16 * c + i) =
-                    make_float4(__uint_as_float(v[c][i]) + __uint_as_float(u[c][i]),
-                                __uint_as_float(v[c][i + 1]) + __uint_as_float(u[c][i + 1]),
-                                __uint_as_float(v[c][i + 2]) + __uint_as_float(u[c][i + 2]),
-                                __uint_as_float(v[c][i + 3]) + __uint_as_float(u[c][i + 3]));
-          }
-          __syncwarp();
+            for (int i = 0; i < 16; i += 4)
+              *reinterpret_cast<float4*>(dst + 16 * c + i) =
+                  make_float4(__uint_as_float(v[c][i]), __uint_as_float(v[c][i + 1]), __uint_as_float(v[c][i + 2]),
+                              __uint_as_float(v[c][i + 3]));
         }
+        __syncwarp();
       }
       umma::fence_before();
       barrive(&br->acce[b]);

@@ -77,13 +77,6 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
   return true;
 }
 
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(saddr(dst)),
-      "l"(src), "r"(bytes), "r"(saddr(bar))
-      : "memory");
-}
-
 // L2 policy for data read once per product: evicted first, so that the
 // factor stream (~1 GB per stage of an RK attempt, against a 126 MB L2) does
 // not push out the small data every launch reads -- schedules, item

@@ -52,9 +52,8 @@ constexpr long long kWaitCyclesDefault = 2LL << 30;
 // shared-memory stages per warp and bytes per stage, a variant -- for phase
 // 1 the lane mapping (0: the lanes of a column segment split its rows and
 // reduce by shuffles; 1: one lane per column, no cross-lane reduction), for
-// phase 2 how far ahead the multipliers are gathered (0: one chunk; 1: two,
-// with three stages; 2: two with two stages, each chunk's column indices
-// loaded when the chunk before it is issued) -- and the schedule (0: the phase's items dealt over all warps longest
+// phase 2 how far ahead the multipliers are gathered (0: one chunk, 1: two)
+// -- and the schedule (0: the phase's items dealt over all warps longest
 // first, statically; 1: each block a run of items consecutive in the store,
 // plan_block_schedule; 2: dynamic, every warp takes the next item, longest
 // first, from a global counter when it needs one; 3: the items dealt over
@@ -65,15 +64,14 @@ constexpr long long kWaitCyclesDefault = 2LL << 30;
 struct StreamShape {
   int nw, ns, sb, map, sched;
 };
-constexpr int kNumShapes1 = 10, kNumShapes2 = 10, kMaxShapes = 10;
+constexpr int kNumShapes1 = 10, kNumShapes2 = 8, kMaxShapes = 10;
 constexpr StreamShape kShapes1[kNumShapes1] = {{12, 2, 8192, 0, 0}, {8, 3, 8192, 0, 0}, {6, 2, 16384, 0, 0},
                                                {12, 2, 8192, 1, 0}, {8, 3, 8192, 1, 0}, {6, 2, 16384, 1, 0},
                                                {12, 2, 8192, 1, 1}, {12, 2, 8192, 0, 1}, {12, 2, 8192, 1, 2},
                                                {12, 2, 8192, 1, 3}};
 constexpr StreamShape kShapes2[kNumShapes2] = {{12, 2, 8192, 0, 0}, {8, 3, 8192, 0, 0}, {6, 2, 16384, 0, 0},
                                                {10, 2, 8192, 0, 0}, {8, 3, 8192, 1, 0}, {12, 2, 8192, 0, 1},
-                                               {12, 2, 8192, 0, 2}, {12, 2, 8192, 0, 3}, {12, 2, 8192, 2, 0},
-                                               {12, 2, 8192, 2, 3}};
+                                               {12, 2, 8192, 0, 2}, {12, 2, 8192, 0, 3}};
 inline const StreamShape& stream_shape(int phase, int s) { return phase == 1 ? kShapes1[s] : kShapes2[s]; }
 inline int num_shapes(int phase) { return phase == 1 ? kNumShapes1 : kNumShapes2; }
 

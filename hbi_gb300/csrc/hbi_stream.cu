@@ -698,7 +698,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
   constexpr int ESZ = sizeof(T);
   constexpr int KP = kMaxCols / 32;  // multipliers per lane of one chunk
   static_assert(NS >= 2, "the multiplier gather runs one chunk ahead");
-  static_assert(GA == 1 || GA == 3 || (GA == 2 && NS >= 3), "a gather two chunks ahead needs three stages");
+  static_assert(GA == 1 || (GA == 2 && NS >= 3), "a gather two chunks ahead needs three stages");
   extern __shared__ __align__(128) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   Ring<NW, NS, SB> R(smem, warp);
@@ -741,27 +741,6 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
   int* const exits = m0.dyn + 3;
   int p_k = 0, p_it = seq.at(0), p_itn = seq.at(1), p_itnn = seq.at(2), p_c0 = 0, p_seq = 0;
   S2ItemDev Dp = current(desc(p_it)), Dpn = desc(p_itn);
-  // GA 3: the column indices of the chunk the producer issues next, loaded
-  // when the chunk before it was issued, so that the multiplier gather can
-  // run two chunks ahead with two stages
-  Pend nxt;
-  auto load_next = [&]() {
-    nxt.nc = 0;
-    nxt.sec = 0;
-#pragma unroll
-    for (int i = 0; i < KP; i++) nxt.idx[i] = 0;
-    if (p_it >= ntot) return;
-    const int nc = min(Dp.cc, Dp.ncols - p_c0);
-    const MatDev& PM = p_it < n0 ? m0 : m1;
-#pragma unroll
-    for (int i = 0; i < KP; i++) {
-      const int k = lane + 32 * i;
-      if (k < nc) nxt.idx[i] = __ldg(&PM.midx[Dp.m0 + p_c0 + k]);
-    }
-    nxt.nc = nc;
-    nxt.sec = p_it >= n0;
-  };
-  if constexpr (GA == 3) load_next();
   auto produce = [&](Pend& pd) {
     pd.nc = 0;
     pd.sec = 0;
@@ -779,17 +758,13 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
       mbar_expect_tx(&R.bar[s], bytes);
       bulk_g2s_stream(R.buf + s * SB, src, bytes, &R.bar[s], l2_evict_first());
     }
-    if constexpr (GA == 3) {
-      pd = nxt;
-    } else {
 #pragma unroll
-      for (int i = 0; i < KP; i++) {
-        const int k = lane + 32 * i;
-        if (k < nc) pd.idx[i] = __ldg(&PM.midx[Dp.m0 + p_c0 + k]);
-      }
-      pd.nc = nc;
-      pd.sec = p_it >= n0;
+    for (int i = 0; i < KP; i++) {
+      const int k = lane + 32 * i;
+      if (k < nc) pd.idx[i] = __ldg(&PM.midx[Dp.m0 + p_c0 + k]);
     }
+    pd.nc = nc;
+    pd.sec = p_it >= n0;
     p_seq++;
     p_c0 += nc;
     if (p_c0 >= Dp.ncols) {
@@ -801,7 +776,6 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
       Dp = current(Dpn);
       Dpn = desc(p_itn);
     }
-    if constexpr (GA == 3) load_next();
   };
   auto gather = [&](const Pend& pd, Acc* mu) {
     const Acc* zv = (const Acc*)(pd.sec ? m1.z : m0.z);
@@ -827,7 +801,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
   }
   Acc mu[KP], mu2[KP];
   gather(fifo[0], mu);
-  if constexpr (GA >= 2) gather(fifo[1], mu2);
+  if constexpr (GA == 2) gather(fifo[1], mu2);
   int c_k = 0, c_it = seq.at(0), c_i1 = seq.at(1), c_i2 = seq.at(2), c_c0 = 0, c_seq = 0;
   S2ItemDev Dc = current(desc(c_it)), Dn = desc(c_i1);
   Acc acc[VEC];
@@ -852,11 +826,6 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
 #pragma unroll
       for (int i = 0; i < KP; i++) mu[i] = mu2[i];
       gather(fifo[2], mu2);
-    } else if constexpr (GA == 3) {
-      // the chunk after next: its indices are the producer's next ones
-#pragma unroll
-      for (int i = 0; i < KP; i++) mu[i] = mu2[i];
-      gather(nxt, mu2);
     } else {
       gather(fifo[1], mu);
     }
@@ -1042,7 +1011,7 @@ void launch_typed(int phase, int shape, const MatDev& m0, const MatDev& m1, int 
                   cudaStream_t st) {
   const int n = phase == 1 ? m0.ns1 + (nmat == 2 ? m1.ns1 : 0) : m0.ns2 + (nmat == 2 ? m1.ns2 : 0);
   if (n == 0) return;
-  static_assert(kNumShapes1 == 10 && kNumShapes2 == 10, "one case per shape");
+  static_assert(kNumShapes1 == 10 && kNumShapes2 == 8, "one case per shape");
   if (phase == 1) {
     switch (shape) {
       case 1: launch_p1s<T, 1>(m0, m1, nmat, x, sm, n, st); break;
@@ -1065,8 +1034,6 @@ void launch_typed(int phase, int shape, const MatDev& m0, const MatDev& m1, int 
       case 5: launch_p2s<T, 5>(m0, m1, nmat, x, sm, n, st); break;
       case 6: launch_p2s<T, 6>(m0, m1, nmat, x, sm, n, st); break;
       case 7: launch_p2s<T, 7>(m0, m1, nmat, x, sm, n, st); break;
-      case 8: launch_p2s<T, 8>(m0, m1, nmat, x, sm, n, st); break;
-      case 9: launch_p2s<T, 9>(m0, m1, nmat, x, sm, n, st); break;
       default: launch_p2s<T, 0>(m0, m1, nmat, x, sm, n, st);
     }
   }
@@ -1106,8 +1073,6 @@ void prepare_type() {
   prepare_p2<T, 5>();
   prepare_p2<T, 6>();
   prepare_p2<T, 7>();
-  prepare_p2<T, 8>();
-  prepare_p2<T, 9>();
 }
 
 }  // namespace

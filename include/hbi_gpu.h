@@ -191,9 +191,8 @@ int hbi_adot_lattice_hyp_phase_dev(double* d_au, hbi_lhp* st_LHp, const double* 
  * and HBI_STREAM_SHAPE2=s force shape s of phase 1 / phase 2. */
 /* the compiled shapes of phase 1 or 2: *count, and shapes5[5*s .. 5*s+4] =
  * warps per block, stages per warp, stage bytes, variant (phase 1: 0 = the
- * lanes of a column split its rows, 1 = one lane per column; phase 2: 0 =
- * multipliers gathered one chunk ahead, 1 = two (three stages), 2 = two with
- * the column indices loaded a chunk early), schedule (0 =
+ * lanes of a column split its rows, 1 = one lane per column; phase 2: how
+ * many chunks ahead the multipliers are gathered, minus one), schedule (0 =
  * items over all warps longest first, 1 = per block a run of items
  * consecutive in the store, see hbi_plan_block_schedule, 2 = dynamic: each
  * warp takes the next item from a counter when it needs one, 3 = items dealt

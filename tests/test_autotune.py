@@ -52,7 +52,7 @@ def test_shape_table_fits_the_kernels():
         assert len(shapes) >= 3 and shapes[0] == (12, 2, 8192, 0, 0)
         for nw, ns, sb, variant, sched in shapes:
             assert 1 <= nw <= 32 and ns >= 2 and sb in (8192, 16384)
-            assert variant in ((0, 1) if phase == 1 else (0, 1, 2)) and sched in (0, 1, 2, 3)
+            assert variant in (0, 1) and sched in (0, 1, 2, 3)
             smem = nw * ns * sb + nw * 128 * 8 + nw * ns * 8
             assert smem <= 227 * 1024
             for esz in (2, 4, 8):

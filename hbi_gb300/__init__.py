@@ -284,12 +284,14 @@ class LHp:
         us = np.zeros(len(sh1) + len(sh2), dtype=np.float32)
         _check(lib().hbi_lh_tuning(self.h, C.byref(s1), C.byref(s2), us.ctypes.data_as(C.POINTER(C.c_float)),
                                    C.byref(src)), "hbi_lh_tuning")
-        name = lambda t: "%dw x %d x %d KB%s%s" % (t[0], t[1], t[2] // 1024, " col" if t[3] else "",
-                                                 {0: "", 1: " blocks", 2: " dynamic", 3: " block-shared"}[t[4]])
-        return {"phase1": name(sh1[s1.value]), "phase2": name(sh2[s2.value]), "shape1": s1.value,
+        def name(t, phase):
+            variant = (" col" if t[3] else "") if phase == 1 else (" gather+2" if t[3] else "")
+            sched = {0: "", 1: " blocks", 2: " dynamic", 3: " block-shared"}[t[4]]
+            return "%dw x %d x %d KB%s%s" % (t[0], t[1], t[2] // 1024, variant, sched)
+        return {"phase1": name(sh1[s1.value], 1), "phase2": name(sh2[s2.value], 2), "shape1": s1.value,
                 "shape2": s2.value, "source": {0: "timed", 1: "reused", 2: "forced"}.get(src.value, "?"),
-                "phase1_us": {name(t): round(float(us[i]), 2) for i, t in enumerate(sh1)},
-                "phase2_us": {name(t): round(float(us[len(sh1) + i]), 2) for i, t in enumerate(sh2)}}
+                "phase1_us": {name(t, 1): round(float(us[i]), 2) for i, t in enumerate(sh1)},
+                "phase2_us": {name(t, 2): round(float(us[len(sh1) + i]), 2) for i, t in enumerate(sh2)}}
 
     def set_shapes(self, shape1, shape2):
         """Pin the launch shapes (indices into stream_shapes()) of phases 1 and 2."""

@@ -204,8 +204,6 @@ struct hbi_lhp_s {
   int32_t *d_fcb_ptr = nullptr, *d_fcb_base = nullptr;
   int32_t *d_w1off[kNumShapes1] = {}, *d_w1item[kNumShapes1] = {}, *d_w2off[kNumShapes2] = {},
           *d_w2item[kNumShapes2] = {};
-  S1Item* d_w1first[kNumShapes1] = {};
-  S2Item* d_w2first[kNumShapes2] = {};
   // launch shapes chosen for phases 1 and 2, the median time (us) of every
   // shape per phase as timed at construction, and how the choice was made
   int tune_source = 0;  // 0 timed, 1 cached from an operator of the same plan, 2 forced or pinned
@@ -884,26 +882,12 @@ static int construct_impl(hbi_lhp** out, const hbi_leafmtxp* lf, hbi_ctl* c, int
         m.gw1[sh] = gw;
         m.w1off[sh] = h->d_w1off[sh];
         m.w1item[sh] = h->d_w1item[sh];
-        if (S.sched <= 1) {
-          std::vector<S1Item> first(gw, S1Item{});
-          for (int w = 0; w < gw; w++)
-            if (woff[w] < woff[w + 1]) first[w] = P.p1[witem[woff[w]]];
-          CK(upload(&h->d_w1first[sh], first, st));
-          m.w1first[sh] = h->d_w1first[sh];
-        }
       } else {
         CK(upload(&h->d_w2off[sh], woff, st));
         CK(upload(&h->d_w2item[sh], witem, st));
         m.gw2[sh] = gw;
         m.w2off[sh] = h->d_w2off[sh];
         m.w2item[sh] = h->d_w2item[sh];
-        if (S.sched <= 1) {
-          std::vector<S2Item> first(gw, S2Item{});
-          for (int w = 0; w < gw; w++)
-            if (woff[w] < woff[w + 1]) first[w] = P.p2[witem[woff[w]]];
-          CK(upload(&h->d_w2first[sh], first, st));
-          m.w2first[sh] = h->d_w2first[sh];
-        }
       }
     }
   m.shape1 = m.shape2 = 0;
@@ -932,10 +916,10 @@ extern "C" int hbi_free_lh(hbi_lhp* h) {
                   (void*)h->d_x, (void*)h->d_y})
     if (p) cudaFree(p);
   for (int sh = 0; sh < kNumShapes1; sh++)
-    for (void* p : {(void*)h->d_w1off[sh], (void*)h->d_w1item[sh], (void*)h->d_w1first[sh]})
+    for (void* p : {(void*)h->d_w1off[sh], (void*)h->d_w1item[sh]})
       if (p) cudaFree(p);
   for (int sh = 0; sh < kNumShapes2; sh++)
-    for (void* p : {(void*)h->d_w2off[sh], (void*)h->d_w2item[sh], (void*)h->d_w2first[sh]})
+    for (void* p : {(void*)h->d_w2off[sh], (void*)h->d_w2item[sh]})
       if (p) cudaFree(p);
   delete h;
   return HBI_OK;

@@ -142,10 +142,6 @@ struct MatDev {            // one H-matrix on the device
   // launch shape s, for a grid of gw1[s] / gw2[s] warps: warp w walks
   // item[off[w] .. off[w+1]) of its phase
   const int32_t *w1off[kNumShapes1], *w1item[kNumShapes1], *w2off[kNumShapes2], *w2item[kNumShapes2];
-  // each warp's first item descriptor under the static schedules (zero when
-  // the warp has none), so that a warp's first copy waits for one load
-  const S1ItemDev* w1first[kNumShapes1];
-  const S2ItemDev* w2first[kNumShapes2];
   int gw1[kNumShapes1], gw2[kNumShapes2];
   int shape1, shape2;      // launch shapes of phases 1 and 2 (indices into kShapes1 / kShapes2)
 };

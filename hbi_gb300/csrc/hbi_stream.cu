@@ -459,23 +459,10 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
   }
   if constexpr (SCHED == 2) seq.make_dynamic(m0.dyn + 0, R.hist);
   int* const exits = m0.dyn + 1;
-  // the first item's descriptor: under a static schedule from the warp's
-  // own slot (loaded beside the schedule offsets), else through its id
-  S1ItemDev Dfirst;
-  {
-    const bool own = SCHED <= 1 && seq.a0 && m0.w1first[shape] && (nmat == 1 || m1.w1first[shape]);
-    if (own) {
-      const S1ItemDev f0 = m0.w1first[shape][gw];
-      const S1ItemDev f1 = nmat == 2 ? m1.w1first[shape][gw] : f0;
-      Dfirst = current(seq.len0 > 0 ? f0 : f1);
-    } else {
-      Dfirst = current(desc(seq.at(0)));
-    }
-  }
   // producer: walks this warp's items chunk by chunk, NS chunks ahead; the
   // item ids are fetched two items ahead, the descriptors one
   int p_k = 0, p_it = seq.at(0), p_itn = seq.at(1), p_itnn = seq.at(2), p_c0 = 0, p_seq = 0;
-  S1ItemDev Dp = Dfirst, Dpn = desc(p_itn);
+  S1ItemDev Dp = current(desc(p_it)), Dpn = desc(p_itn);
   auto produce = [&]() {
     if (p_it >= ntot) return;
     const int nc = min(Dp.cc, Dp.ncols - p_c0);
@@ -514,7 +501,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p1_stream_kernel(MatDev m0, MatDev
   }
   // consumer: item ids three ahead, descriptors two
   int c_k = 0, c_it = seq.at(0), c_i1 = seq.at(1), c_i2 = seq.at(2), c_i3 = seq.at(3), c_c0 = 0, c_seq = 0;
-  S1ItemDev Dc = Dfirst, Dn = desc(c_i1), Dnn = desc(c_i2);
+  S1ItemDev Dc = current(desc(c_it)), Dn = desc(c_i1), Dnn = desc(c_i2);
   // x rows of an item: MAP 0, lane j of each column slot holds rows
   // j*VEC .. j*VEC+VEC-1; MAP 1, lane L holds rows L*VEC .. (for the tile)
   auto load_x = [&](const S1ItemDev& D, Acc* xv) {
@@ -752,21 +739,8 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
   }
   if constexpr (SCHED == 2) seq.make_dynamic(m0.dyn + 2, R.hist);
   int* const exits = m0.dyn + 3;
-  // the first item's descriptor: under a static schedule from the warp's
-  // own slot (loaded beside the schedule offsets), else through its id
-  S2ItemDev Dfirst;
-  {
-    const bool own = SCHED <= 1 && seq.a0 && m0.w2first[shape] && (nmat == 1 || m1.w2first[shape]);
-    if (own) {
-      const S2ItemDev f0 = m0.w2first[shape][gw];
-      const S2ItemDev f1 = nmat == 2 ? m1.w2first[shape][gw] : f0;
-      Dfirst = current(seq.len0 > 0 ? f0 : f1);
-    } else {
-      Dfirst = current(desc(seq.at(0)));
-    }
-  }
   int p_k = 0, p_it = seq.at(0), p_itn = seq.at(1), p_itnn = seq.at(2), p_c0 = 0, p_seq = 0;
-  S2ItemDev Dp = Dfirst, Dpn = desc(p_itn);
+  S2ItemDev Dp = current(desc(p_it)), Dpn = desc(p_itn);
   auto produce = [&](Pend& pd) {
     pd.nc = 0;
     pd.sec = 0;
@@ -829,7 +803,7 @@ __global__ void __launch_bounds__(NW * 32, 1) p2_stream_kernel(MatDev m0, MatDev
   gather(fifo[0], mu);
   if constexpr (GA == 2) gather(fifo[1], mu2);
   int c_k = 0, c_it = seq.at(0), c_i1 = seq.at(1), c_i2 = seq.at(2), c_c0 = 0, c_seq = 0;
-  S2ItemDev Dc = Dfirst, Dn = desc(c_i1);
+  S2ItemDev Dc = current(desc(c_it)), Dn = desc(c_i1);
   Acc acc[VEC];
 #pragma unroll
   for (int v = 0; v < VEC; v++) acc[v] = 0;

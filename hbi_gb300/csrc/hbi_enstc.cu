@@ -308,16 +308,14 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
           umma::fence_after();
           const int kc = min(KC, D.kp - k0);
           const unsigned char* stg = stage(s);
-          // descriptors of the stage's first chunk; the next chunk, row block
-          // and half are offsets of the start-address field (16-byte units;
-          // shared memory is below 256 KB, so the 14-bit field cannot carry)
-          const uint64_t dm0 = umma::smem_desc(stg + kFac + kRows, 1024, 128);
-          const uint64_t df0 = umma::smem_desc(stg, (uint32_t)D.np * 16, 128);
-          const uint32_t fchunk = (uint32_t)D.np * 4, flo = (uint32_t)D.np * 2;  // np * 64 and np * 32 bytes
           for (int c = 0; c < kc / 16; c++) {
-            const uint64_t dmh = dm0 + (uint64_t)(c * 256), dml = dmh + 128;
+            const unsigned char* mem = stg + kFac + kRows + c * 4096;
+            const uint64_t dmh = umma::smem_desc(mem, 1024, 128);
+            const uint64_t dml = umma::smem_desc(mem + 2048, 1024, 128);
             for (int mb = 0; mb < nmb; mb++) {
-              const uint64_t dfh = df0 + (uint64_t)(c * fchunk + mb * 128), dfl = dfh + flo;
+              const unsigned char* fac = stg + c * D.np * 64 + mb * 2048;
+              const uint64_t dfh = umma::smem_desc(fac, (uint32_t)D.np * 16, 128);
+              const uint64_t dfl = umma::smem_desc(fac + D.np * 32, (uint32_t)D.np * 16, 128);
               const uint32_t d = tbase + (uint32_t)(b * 128 + mb * EMT);
               umma::mma_bf16(d, dfh, dmh, idesc, (k0 > 0 || c > 0) ? 1 : 0);
               umma::mma_bf16(d, dfh, dml, idesc, 1);

@@ -8,16 +8,20 @@
 // whole columns that fill one shared-memory stage (8 KB or 16 KB).  Each warp
 // of a block owns NS stages with one mbarrier each; one lane starts a
 // cp.async.bulk (TMA) copy of a chunk into a free stage while the warp
-// consumes an earlier stage.  The small per-item operands (x rows) are loaded
-// one item ahead of their use, phase 2's multipliers one chunk ahead.
+// consumes an earlier stage; the copies carry an L2 evict-first policy, so
+// that the factor stream does not evict the small data every launch reads.
+// The small per-item operands (x rows) are loaded one item ahead of their
+// use, phase 2's multipliers one chunk ahead.  Which items a warp walks is
+// set by the launch shape's schedule (WarpSeq).
 //
-// Lanes work on a stage as column slots: a segment of ntp rows is covered by
-// LW = pow2ceil(ntp / VEC) lanes with one 16-byte vector each, and CS = 32/LW
-// slots take different columns.  Phase 1 reduces each column over its LW
-// lanes (z = V^T x, partial per row tile, combined by the last tile of a
-// column group); phase 2 accumulates y rows per lane and reduces over the
-// slots once per item.  Every sum has a fixed order: results are
-// deterministic run to run.
+// Phase 1 maps lanes to a stage in one of two ways: column slots (a segment
+// of ntp rows covered by LW = pow2ceil(ntp / VEC) lanes with one 16-byte
+// vector each, CS = 32/LW slots side by side, reduced by shuffles) or one
+// lane per column over the swizzled V store (p1_columns).  A column's sum
+// is final per row tile (z), or a partial combined by the last tile of a
+// column group to arrive.  Phase 2 accumulates y rows per lane over the
+// column slots and reduces over the slots once per item.  Every sum has a
+// fixed order: results are deterministic run to run.
 //
 // Waits are bounded: a stage that does not complete within the operator's
 // wait bound (~1 s of SM clock) sets the operator's error word, the warp waits

@@ -62,13 +62,17 @@ def test_plan_on_aca_factors(oracle):
     assert np.linalg.norm(y - ref) <= 1e-12 * np.linalg.norm(ref)
 
 
-@pytest.mark.parametrize("shape", [(64, 32), (150, 30), (40, 40)])
+@pytest.mark.parametrize("shape", [(64, 32), (150, 30), (40, 40), (128, 64)])
 def test_tc_plan_matches_oracle_product(oracle, shape):
     """The ensemble's tensor-core plan: canonical BF16 hi+lo stores walked on
-    the host.  hi + lo carries ~16 bits of each factor: 1e-4 relative."""
+    the host.  hi + lo carries ~16 bits of each factor: 1e-4 relative.  The
+    128 x 64 plane has column groups taller than the 1,024-row phase-1
+    tiles, so their tiles meet in partial sums."""
     xcol, ycol, zcol, _, _ = mesh.mesh_3ddip(shape[0], shape[1], 0.1, 30.0)
     coord = np.stack([xcol, ycol, zcol], 1)
     n, lv, off, body = _random_factors(oracle, coord, seed=shape[1])
+    if shape == (128, 64):
+        assert max(int(r[5]) for r in lv if r[0] == 1) > 1024
     Ho = oracle.HMatrix.from_body(n, lv, off, body)
     x = np.random.default_rng(2).standard_normal(n)
     ref = Ho.matvec(x)

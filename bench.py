@@ -446,9 +446,11 @@ def run_ours(args):
     for hnd in (lf_s, lf_n, ctl_s, ctl_n):
         hnd.close()
 
-    # ---- sim-yr/h: plain FP64 form against the mixed + learned form ----
+    # ---- sim-yr/h: plain FP64 form against the mixed + learned form (one
+    # GPU runs only: the comparison takes minutes, and the other ranks of a
+    # multi-GPU run would hold their GPUs idle meanwhile) ----
     cyc = None
-    if rank == 0 and args.sim_window_yr > 0:
+    if rank == 0 and world == 1 and args.sim_window_yr > 0:
         from hbi_gb300 import configs
         cyc = compare_time_loops(args, configs.c3_3dnt() if args.sim_config == "c3" else w)
 

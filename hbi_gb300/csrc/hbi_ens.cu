@@ -131,9 +131,14 @@ __device__ bool block_wait(uint64_t* b, uint32_t par, int* err, int* sh_ok) {
   }
   __syncthreads();
   const int ok = *sh_ok;
-  if (ok)
-    while (!bar_try(b, par)) {
-    }
+  // every thread observes the completed phase itself (acquire); the phase
+  // stays completed until this block refills the stage, so the probe passes
+  // at once -- bounded all the same
+  if (ok) {
+    const long long t1 = clock64();
+    while (!bar_try(b, par))
+      if (clock64() - t1 > kWait) break;
+  }
   return ok != 0;
 }
 

@@ -305,7 +305,8 @@ class LHp:
 
     def set_wait_limit(self, cycles):
         """Test hook: bound of the product kernels' bulk-copy waits (SM clock
-        cycles; 0 = one non-blocking probe; negative = the default)."""
+        cycles; 0 = every wait gives up before its first probe; negative = the
+        default).  An ensemble created on the operator afterwards inherits it."""
         _check(lib().hbi_lh_set_wait_limit(self.h, C.c_longlong(int(cycles))), "hbi_lh_set_wait_limit")
 
     def phase_bytes(self):

@@ -116,16 +116,17 @@ __device__ __forceinline__ void bulk_stream(void* dst, const void* src, uint32_t
 }
 __device__ __forceinline__ void fence_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-// block-wide bounded wait; false (and the error word set) on time-out
-__device__ bool block_wait(uint64_t* b, uint32_t par, int* err, int* sh_ok) {
+// block-wide bounded wait; false (and the error word set) on time-out.
+// limit: the operator's bound in SM clock cycles; 0 is spent before the
+// first probe, so every wait gives up (the error path on demand)
+__device__ bool block_wait(uint64_t* b, uint32_t par, int* err, long long limit, int* sh_ok) {
   if (threadIdx.x == 0) {
-    const long long t0 = clock64();
-    int ok = 1;
-    while (!bar_try(b, par))
-      if (clock64() - t0 > kWait) {
-        ok = 0;
-        break;
-      }
+    int ok = limit > 0 && bar_try(b, par);
+    if (!ok && limit > 0) {
+      const long long t0 = clock64();
+      while (!(ok = bar_try(b, par)))
+        if (clock64() - t0 > limit) break;
+    }
     *sh_ok = ok;
     if (!ok && err) atomicExch(err, 1);
   }
@@ -222,14 +223,14 @@ __global__ void __launch_bounds__(256, 2) p1e_kernel(EnsMat A, EnsMat B, int nma
   while (c_it < ntot) {
     const EnsMat& M = c_it < n0 ? A : B;
     if (c_c0 == 0) {
-      if (!block_wait(&bar[2 + (j & 1)], (uint32_t)((j >> 1) & 1), M.m.err, &sh_ok)) {
+      if (!block_wait(&bar[2 + (j & 1)], (uint32_t)((j >> 1) & 1), M.m.err, M.m.wait, &sh_ok)) {
         drain_e(bar, c_seq, p_seq, -1);
         return;
       }
       issue_x(c_it + G, j + 1);
     }
     const int s = c_seq & 1;
-    if (!block_wait(&bar[s], (uint32_t)((c_seq >> 1) & 1), M.m.err, &sh_ok)) {
+    if (!block_wait(&bar[s], (uint32_t)((c_seq >> 1) & 1), M.m.err, M.m.wait, &sh_ok)) {
       drain_e(bar, c_seq, p_seq, c_it + G < ntot ? j + 1 : -1);
       return;
     }
@@ -364,7 +365,7 @@ __global__ void __launch_bounds__(256, 2) p2e_kernel(EnsMat A, EnsMat B, int nma
   while (c_it < ntot) {
     const EnsMat& M = c_it < n0 ? A : B;
     const int s = c_seq & 1;
-    if (!block_wait(&bar[s], (uint32_t)((c_seq >> 1) & 1), M.m.err, &sh_ok)) {
+    if (!block_wait(&bar[s], (uint32_t)((c_seq >> 1) & 1), M.m.err, M.m.wait, &sh_ok)) {
       drain_e(bar, c_seq, p_seq, -1);
       return;
     }
@@ -1027,6 +1028,7 @@ extern "C" int hbi_ens_use_tensor_cores(hbi_ens* e, const hbi_leafmtxp* lf_s, co
     e->ncnt_t[k] = P.ncg;
     T.gpart = e->M[k].gpart;
     T.err = e->M[k].m.err;
+    T.wait = e->M[k].m.wait;
     if (!T.p1 || !T.p2 || !T.midx || !s1 || !s2 || !T.z || !T.part || !T.cnt)
       return efail(HBI_ERR_NOMEM, "hbi_ens_use_tensor_cores: allocation");
     for (int ph = 1; ph <= 2; ph++) {

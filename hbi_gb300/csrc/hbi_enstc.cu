@@ -80,13 +80,14 @@ __device__ __forceinline__ bool bwait(uint64_t* b, uint32_t par) {
     if (clock64() - t0 > kWaitT) return false;
   return true;
 }
-// bounded wait of a role: gives up when another role did, or after the bound
-// (then records the error and tells the other roles)
-__device__ __forceinline__ bool rwait(uint64_t* b, uint32_t par, Bars* br, int* err) {
+// bounded wait of a role: gives up when another role did, or after `limit`
+// cycles (then records the error and tells the other roles); a limit of 0 is
+// spent before the first probe (the error path on demand)
+__device__ __forceinline__ bool rwait(uint64_t* b, uint32_t par, Bars* br, int* err, long long limit) {
   const long long t0 = clock64();
-  while (!btry(b, par)) {
+  while (limit <= 0 || !btry(b, par)) {
     if (*(volatile int*)&br->abort) return false;
-    if (clock64() - t0 > kWaitT) {
+    if (limit <= 0 || clock64() - t0 > limit) {
       *(volatile int*)&br->abort = 1;
       if (err) atomicExch(err, 1);
       return false;
@@ -235,7 +236,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
         continue;
       }
       int w = 1;
-      if (q >= NST && lane == 0) w = rwait(&br->empty[s], (uint32_t)((q / NST - 1) & 1), br, A.err);
+      if (q >= NST && lane == 0) w = rwait(&br->empty[s], (uint32_t)((q / NST - 1) & 1), br, A.err, A.wait);
       if (!__shfl_sync(0xffffffffu, w, 0)) break;
       const int kc = min(KC, D.kp - k0);
       const int nrow = max(0, min(kc, D.kv - k0));  // member rows that carry data
@@ -293,13 +294,13 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
       const int b = j & 1;
       const TcItem& D = W.D;
       int w = 1;
-      if (j >= 2 && lane == 0) w = rwait(&br->acce[b], (uint32_t)((j / 2 - 1) & 1), br, A.err);
+      if (j >= 2 && lane == 0) w = rwait(&br->acce[b], (uint32_t)((j / 2 - 1) & 1), br, A.err, A.wait);
       if (!__shfl_sync(0xffffffffu, w, 0)) break;
       const int nmb = (D.np + 127) / 128;
       bool ok = true;
       for (int k0 = 0; k0 < D.kp; k0 += KC, q++) {
         const int s = q % NST;
-        if (lane == 0) w = rwait(&br->conv[s], (uint32_t)((q / NST) & 1), br, A.err);
+        if (lane == 0) w = rwait(&br->conv[s], (uint32_t)((q / NST) & 1), br, A.err, A.wait);
         if (!__shfl_sync(0xffffffffu, w, 0)) {
           ok = false;
           break;
@@ -347,7 +348,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
       const TcItem& D = W.D;
       for (int k0 = 0; k0 < D.kp; k0 += KC, q++) {
         const int s = q % NST;
-        if (!rwait(&br->full[s], (uint32_t)((q / NST) & 1), br, A.err)) {
+        if (!rwait(&br->full[s], (uint32_t)((q / NST) & 1), br, A.err, A.wait)) {
           ok = false;
           break;
         }
@@ -390,7 +391,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_kernel(TcMat A, TcMat B, int n
       const int b = j & 1;
       const TcItem& D = W.D;
       const TcMat& M = W.it < n0 ? A : B;
-      if (et == 0) br->flag = rwait(&br->accf[b], (uint32_t)((j / 2) & 1), br, A.err) ? 1 : 0;
+      if (et == 0) br->flag = rwait(&br->accf[b], (uint32_t)((j / 2) & 1), br, A.err, A.wait) ? 1 : 0;
       group_sync();
       const int ok = br->flag;
       group_sync();

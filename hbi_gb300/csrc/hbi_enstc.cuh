@@ -23,6 +23,7 @@ struct TcMat {            // one H-matrix's tensor-core stores and ensemble scra
   int* cnt;                 // per column group piece
   float* gpart;             // rows of the row groups x 64 (the operator's phase-3 layout)
   int* err;
+  long long wait;           // bound of a wait (SM clock cycles; 0: every wait gives up), the operator's
   // static schedule of both matrices' items over G blocks (first matrix's
   // view only): block b walks bitem[ph][boff[ph][b] .. boff[ph][b + 1]),
   // item i < n of the first matrix, else item i - n of the second

@@ -149,7 +149,8 @@ int hbi_lh_check_error(hbi_lhp* st_LHp);
  * is spent before the first probe, so every wait gives up -- the path of a
  * wait that ran out (error word set, copies in flight drained with the
  * default bound, early exit) without anything being wrong; a negative value
- * restores the default bound. */
+ * restores the default bound.  Ensembles (hbi_ens_create) take the bound of
+ * their operators at creation. */
 int hbi_lh_set_wait_limit(hbi_lhp* st_LHp, long long cycles);
 
 /* The product of hbi_adot_lattice_hyp_dev without any device allocation.

@@ -106,3 +106,44 @@ def test_time_loop_stops_on_a_wait_that_ran_out():
     rk3, c3 = loop()
     c3.run(k_limit=20)
     assert np.array_equal(c2.trace(), c3.trace())
+
+
+@pytest.mark.parametrize("tc", [False, True])
+def test_ensemble_product_reports_a_wait_that_ran_out(tc):
+    """The ensemble's product kernels (CUDA cores, and the tcgen05 kernel,
+    whose roles then all leave and release tensor memory) take the bound of
+    the operators they were created on: hbi_ens_product returns
+    HBI_ERR_DEVICE; an ensemble created after the default bound is restored
+    gives the product bit for bit."""
+    w = configs.c2_3dph(32, 16)
+    ctl_s, ctl_n = H.Ctl(w.nd), H.Ctl(w.nd)
+    lf_s = H.LeafMtxp(ctl_s, w.geometry("s"), w.eps_h)
+    lf_n = H.LeafMtxp(ctl_n, w.geometry("n"), w.eps_h)
+    lh = (H.LHp(lf_s, ctl_s, "f32"), H.LHp(lf_n, ctl_n, "f32"))
+    ndc, lodc = H.HACApK_gen_lattice_vector(ctl_s)
+    b_in, dc_m = configs.ensemble_params(64, seed=1)
+    y, vel, b, dc, p = configs.ensemble_state(w, lodc, b_in, dc_m)
+    X = np.random.default_rng(4).standard_normal((w.nd, 64)).astype(np.float32)
+
+    def ensemble():
+        e = H.Ensemble(*lh, b, dc, evlaw=w.evlaw, scale=w.scale, a=p["a"], f0=p["f0"], vpl=p["vpl"])
+        if tc:
+            e.use_tensor_cores(lf_s, lf_n)
+        return e
+
+    e = ensemble()
+    ys, yn, _ = e.product(X)
+    e.close()
+    for o in lh:
+        o.set_wait_limit(0)
+    e = ensemble()
+    with pytest.raises(H.HBIError) as err:
+        e.product(X)
+    assert err.value.code == H.HBI_ERR_DEVICE
+    e.close()
+    for o in lh:
+        o.set_wait_limit(-1)
+    e = ensemble()
+    ys2, yn2, _ = e.product(X)
+    e.close()
+    assert np.array_equal(ys, ys2) and np.array_equal(yn, yn2)
